@@ -1,0 +1,164 @@
+/*
+ * mmh.h -- C ABI of the GB300 (sm_103a) MMH reconstruction library.
+ *
+ * Drop-in replacement for the hot path of pandaPQY/Moving-Mesh-reconstruction
+ * (Fortran 90, directory mmh/): the curvilinear multigrid solve, the
+ * grid-compression limiter, the relaxing-TVD density update and the spectral
+ * outputs.  Each drop-in entry point below replaces one Fortran subroutine and
+ * keeps its argument meaning; arrays are the caller's, in the Fortran layout
+ * (column-major, a(i,j,k) at a[(i-1) + n*((j-1) + n*(k-1))], u(nf,n,n,n)
+ * component-fastest), periodic in all three directions.
+ *
+ * Differences from the Fortran calling convention:
+ *   - every call takes a context created by mmh_create (device buffers, FFT
+ *     plans, stream, configuration) instead of compile-time NG and COMMON state;
+ *   - errors are returned as negative codes (mmh_strerror) instead of
+ *     write + stop/pause; nothing exits the process;
+ *   - diagnostics the Fortran prints are returned in an mmh_diag struct.
+ *
+ * A context is not thread-safe; use one context per host thread / stream.
+ */
+#ifndef MMH_H
+#define MMH_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MMH_OK 0
+#define MMH_ERR_ARG (-1)         /* bad argument (null pointer, nred != 1, iopt != 2, ...) */
+#define MMH_ERR_SIZE (-2)        /* grid not a cube / size out of range / size mismatch with context */
+#define MMH_ERR_NOTPOW2 (-3)     /* grid size not a power of two */
+#define MMH_ERR_CUDA (-4)        /* CUDA runtime or cuFFT failure */
+#define MMH_ERR_NAN (-5)         /* NaN or Inf detected in a residual or sum */
+#define MMH_ERR_DIVERGED (-6)    /* tolerance schedule hit max_cycles without reaching tol */
+#define MMH_ERR_UNSUPPORTED (-7) /* e.g. relaxing with nonzero momentum/energy components */
+#define MMH_ERR_RANGE (-8)       /* a summed value is outside the exact-sum range |x| < 2^32 */
+#define MMH_ERR_NOMEM (-9)       /* device allocation failed */
+
+/* precision forms */
+#define MMH_FP64 0  /* everything in FP64 (bit-identical to the CPU restatement) */
+#define MMH_MIXED 1 /* FP32 inner V-cycles inside an FP64 defect-correction loop */
+
+/* multigrid schedules */
+#define MMH_SCHED_REF 0 /* reference: one V-cycle, 4*NG/n sweeps per level (mgtemplate.f90) */
+#define MMH_SCHED_TOL 1 /* V(nu1,nu2) cycles until ||r||_inf <= tol*||rhs||_inf */
+
+typedef struct mmh_ctx mmh_ctx;
+
+typedef struct mmh_config {
+  int n;          /* NG: top-level grid size, power of two, 8..1024 (mmh/dimen.f90:1) */
+  int precision;  /* MMH_FP64 or MMH_MIXED (MMH_MIXED requires MMH_SCHED_TOL) */
+  int schedule;   /* MMH_SCHED_REF or MMH_SCHED_TOL */
+  int nu1, nu2;   /* pre/post Gauss-Seidel sweeps per level, tolerance schedule */
+  int max_cycles; /* V-cycle / outer-iteration cap, tolerance schedule */
+  double tol;     /* relative max-norm residual target, tolerance schedule */
+  int device;     /* CUDA device ordinal */
+  void* stream;   /* cudaStream_t to run on; NULL: the context creates its own */
+} mmh_config;
+
+/* Diagnostics: the quantities the Fortran prints (mg64.f90:43-45,
+ * limiter.f90:657-667, main.f90:97-105). */
+typedef struct mmh_diag {
+  double r1;        /* top-level max-norm residual after pre-smoothing (last cycle) */
+  double relaxerr;  /* top-level max-norm residual after post-smoothing (last cycle) */
+  double rhsnorm;   /* max |rhs| after rgzerosum */
+  double resid_rel; /* final ||r||_inf/||rhs||_inf (FP64 residual in MMH_MIXED) */
+  int vcycles;      /* V-cycles (MMH_FP64) or outer corrections (MMH_MIXED) run */
+  int guards;       /* coarse-level corrections discarded by the divergence guard */
+  int status;       /* status of the call */
+  int pad;
+  long long nexpand;   /* cells hit by the expansion limiter (pass 1) */
+  long long ncompress; /* cells hit by the compression limiter (second test) */
+  double cmax, detmin, detmax, fluxmax, fluxmin, rho2;
+} mmh_diag;
+
+/* ---- context ----------------------------------------------------------- */
+void mmh_config_default(mmh_config* cfg, int n);
+int mmh_create(mmh_ctx** ctx, const mmh_config* cfg);
+int mmh_destroy(mmh_ctx* ctx);
+const char* mmh_strerror(int code);
+int mmh_sync(mmh_ctx* ctx);
+/* number of kernels this library has launched in the process (all contexts) */
+unsigned long long mmh_launch_count(void);
+
+/* ---- drop-ins for the Fortran subroutines (host arrays, default real) ---- */
+
+/* calcdefp(defp,tmp,tmp2,def,u,dtold1,dtaumesh,nfluid)       mmh/limiter.f90:17
+ * defp(n,n,n) out; tmp(n,n,n) and tmp2(n+2,n,n) are scratch as in the
+ * reference (tmp(1..3,1,1) return rho2, xlum, temp; tmp2 is not written);
+ * u(nfluid,n,n,n) with u(2:nfluid) == 0 (state at rest, as main.f90 sets it). */
+int mmh_calcdefp(mmh_ctx* ctx, float* defp, float* tmp, float* tmp2, const float* def, const float* u, float dtold1,
+                 float dtaumesh, int nfluid, mmh_diag* diag);
+int mmh_calcdefp_f64(mmh_ctx* ctx, double* defp, double* tmp, double* tmp2, const double* def, const double* u,
+                     double dtold1, double dtaumesh, int nfluid, mmh_diag* diag);
+
+/* multigrid(u,rhs,defpot,ubig,dx,nx,ny,nz,nu,nred,iopt)    mmh/multigrid.f90:16
+ * u in/out, rhs in/out (rgzerosum is applied in place), iopt must be 2
+ * (potential-flow solver), nred must be 1, nx = ny = nz <= NG. */
+int mmh_multigrid(mmh_ctx* ctx, float* u, float* rhs, const float* defpot, const float* ubig, float dx, int nx,
+                  int ny, int nz, int nu, int nred, int iopt, mmh_diag* diag);
+int mmh_multigrid_f64(mmh_ctx* ctx, double* u, double* rhs, const double* defpot, const double* ubig, double dx,
+                      int nx, int ny, int nz, int nu, int nred, int iopt, mmh_diag* diag);
+
+/* relaxing(u,def,defp,cmax,dt,nfluidcmp)                     mmh/relaxing.f90:21
+ * u(nfluidcmp,n,n,n) in/out; components 2..nfluidcmp must be zero
+ * (MMH_ERR_UNSUPPORTED otherwise); cmax is unused, as in the reference. */
+int mmh_relaxing(mmh_ctx* ctx, float* u, const float* def, const float* defp, float cmax, float dt, int nfluidcmp);
+int mmh_relaxing_f64(mmh_ctx* ctx, double* u, const double* def, const double* defp, double cmax, double dt,
+                     int nfluidcmp);
+
+/* scalar2gradient(indata,outdata,nn)                         mmh/gradient.f90:1
+ * outdata(n,n,n,3) = F^-1[i k_a F[indata]] with the reference's FFT sign
+ * convention (= minus the spectral gradient). */
+int mmh_scalar2gradient(mmh_ctx* ctx, const float* indata, float* outdata, const int* nn);
+int mmh_scalar2gradient_f64(mmh_ctx* ctx, const double* indata, double* outdata, const int* nn);
+
+/* defp2delta(indata,outdata,nn)                              mmh/reconstruct.f90:1
+ * outdata = F^-1[|k|^2 F[indata]] (= minus the spectral Laplacian). */
+int mmh_defp2delta(mmh_ctx* ctx, const float* indata, float* outdata, const int* nn);
+int mmh_defp2delta_f64(mmh_ctx* ctx, const double* indata, double* outdata, const int* nn);
+
+/* ---- reference subroutines on the path (FP64 host arrays) ------------- */
+/* relax(arr,resid,rhs,deformpot,u,rinf,dx,n,n,n,1,nrelax,iopt)  gauss1.f90:64
+ * iopt = 8*isolver + iresidopt with isolver = 2; resid((n/2)^3) is written
+ * when iresidopt is 1 or 3. */
+int mmh_relax_f64(mmh_ctx* ctx, double* arr, double* resid, const double* rhs, const double* deformpot,
+                  const double* rho, double* rinf, double dx, int n, int nrelax, int iopt);
+/* cbajraw for every plane: coef(n,n,n,6) = rho_bar*cof(A)/det    gauss1.f90:1027 */
+int mmh_metric_f64(mmh_ctx* ctx, const double* deformpot, const double* rho, double dx, int n, double* coef);
+int mmh_restrict_f64(mmh_ctx* ctx, const double* u, int n, double* uhalf);       /* mgutil.f90:74 */
+int mmh_inject_f64(mmh_ctx* ctx, double* u, const double* uhalf, int n);         /* mgutil.f90:38 */
+int mmh_zerosum_f64(mmh_ctx* ctx, double* arr, int n);                           /* gauss1.f90:1420 */
+int mmh_rgzerosum_f64(mmh_ctx* ctx, double* arr, const double* def, double dx, int n); /* gauss1.f90:1219 */
+int mmh_nsmooth_f64(mmh_ctx* ctx, double* a, int n);                             /* limiter.f90:677 */
+/* pass-1 flux limiter on tmp (in place), density-only state: limiter.f90:175-381.
+ * maskx / maskc (nullable, n^3 bytes) receive the expansion and compression masks. */
+int mmh_limiter_pass1_f64(mmh_ctx* ctx, double* tmp, const double* def, const double* rho, int n, double dtold,
+                          double dtaumesh, unsigned char* maskx, unsigned char* maskc, mmh_diag* diag);
+/* compression test: defplim = tlim where tlim > 0 else 0: limiter.f90:425-533 */
+int mmh_limiter_mask_f64(mmh_ctx* ctx, double* defplim, const double* def, const double* defp, int n, double dtold,
+                         unsigned char* mask, mmh_diag* diag);
+/* FFT Poisson correction defp += solve(defplim): limiter.f90:535-597 */
+int mmh_limiter_poisson_f64(mmh_ctx* ctx, double* defp, const double* defplim, int n);
+
+/* ---- device-resident reconstruction (mmh/main.f90:83-179) -------------- */
+/* Load the state (host arrays): def(n,n,n) (NULL: zero) and u(nfluid,n,n,n). */
+int mmh_load_f64(mmh_ctx* ctx, const double* def, const double* u, int nfluid);
+/* Same from device memory: def (NULL: zero) and the density u(1,:,:,:) as n^3. */
+int mmh_load_dev(mmh_ctx* ctx, const double* d_def, const double* d_rho);
+/* niter deformation iterations: calcdefp, def = def + defp, relaxing. */
+int mmh_iterate(mmh_ctx* ctx, int niter, mmh_diag* diag);
+/* Copy the state back to the host (either pointer may be NULL). */
+int mmh_store_f64(mmh_ctx* ctx, double* def, double* u, int nfluid);
+/* Spectral outputs of the current def to the host: grad(n,n,n,3), delta(n,n,n)
+ * (either may be NULL).  mmh/main.f90:131-179 */
+int mmh_outputs_f64(mmh_ctx* ctx, double* grad, double* delta);
+/* Device pointers of the resident state (n^3 doubles each). */
+int mmh_state_dev(mmh_ctx* ctx, double** d_def, double** d_rho, double** d_defp);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MMH_H */

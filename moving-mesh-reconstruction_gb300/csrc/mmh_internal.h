@@ -1,0 +1,66 @@
+// Internal declarations shared by the MMH CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mmh {
+
+typedef long long i64;
+
+// Count of kernel launches issued by this library (reported by bench.py).
+void count_launch(int k = 1);
+unsigned long long launch_count();
+
+// Launchers, instantiated for double (mmh_kernels_f64.cu, no FMA contraction)
+// and float (mmh_kernels_f32.cu).
+template <class T> void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_t s);
+template <class T> void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, cudaStream_t s);
+template <class T>
+void launch_residual(const T* phi, const T* rhs, const T* coef, int n, T dx, T* r, float* r32,
+                     unsigned long long* maxbits, cudaStream_t s);
+template <class T> void launch_restrict_resid(const T* r, int n, int special, T* coarse, cudaStream_t s);
+template <class T> void launch_restrict27(const T* fine, int n, T* coarse, cudaStream_t s);
+template <class T> void launch_smooth27(const T* in, int n, T* out, cudaStream_t s);
+template <class T> void launch_prolong_add(T* u, const T* uh, int n, cudaStream_t s);
+template <class T> void launch_fxsum(const T* a, i64 count, unsigned long long* acc, int* flag, cudaStream_t s);
+template <class T> void launch_det(const T* def, int n, T dx, T* det, cudaStream_t s);
+template <class T> void launch_sub_mean(T* a, i64 count, const double* mean, cudaStream_t s);
+template <class T> void launch_sub_dfact(T* a, const T* det, i64 count, const double* ratio, cudaStream_t s);
+template <class T> void launch_fill(T* a, i64 count, T v, cudaStream_t s);
+template <class T> void launch_absmax(const T* a, i64 count, unsigned long long* maxbits, cudaStream_t s);
+// divergence guard: flag = relaxerr > r1*margin && r1 > floor (bits are maxbits words)
+void launch_guard(const unsigned long long* r1bits, const unsigned long long* errbits, double margin, double floor_,
+                  int* flag, int* guards, cudaStream_t s);
+template <class T> void launch_zero_if(T* a, i64 count, const int* flag, cudaStream_t s);
+template <class T> void launch_sub_mean_unless(T* a, i64 count, const double* mean, const int* flag, cudaStream_t s);
+// zerosum helpers: mean = fx(acc)/count ; usum flag = (T)fx(acc) > 1e-2
+void launch_fx_mean(const unsigned long long* acc, double count, double* out, cudaStream_t s);
+void launch_fx_ratio(const unsigned long long* num, const unsigned long long* den, double* out, cudaStream_t s);
+template <class T> void launch_usum_flag(const unsigned long long* acc, int* flag, cudaStream_t s);
+
+// precision conversion and updates
+void launch_d2f(const double* a, float* b, i64 count, cudaStream_t s);
+void launch_f2d(const float* a, double* b, i64 count, cudaStream_t s);
+void launch_add_f2d(double* a, const float* b, i64 count, cudaStream_t s);
+void launch_add(double* a, const double* b, i64 count, cudaStream_t s);  // a = a + b
+
+// limiter / spectral / relaxing (FP64)
+struct LimDev;
+void launch_calcdefp_rhs(double* tmp, const double* rho, int n, double dtold, cudaStream_t s);
+void launch_limiter_pass1(double* tmp, const double* def, const double* rho, int n, double dtold, double dtaumesh,
+                          LimDev* st, uint8_t* maskx, uint8_t* maskc, cudaStream_t s);
+void launch_limiter_mask(double* defplim, const double* def, const double* defp, int n, double dtold, LimDev* st,
+                         uint8_t* mask, cudaStream_t s);
+void launch_lim_reset(LimDev* st, cudaStream_t s);
+void launch_spec_pack(const void* Xc, int n, int mode, void* Z, const LimDev* st, cudaStream_t s);
+void launch_spec_unpack(const void* z, int n, double* out, int stride_out, int add, const LimDev* st, cudaStream_t s);
+void launch_relax_stage1(const double* rho, const double* def, const double* defp, int n, double* baj, double* cc,
+                         double* vt, cudaStream_t s);
+void launch_relax_flux(const double* u1, const double* defp, const double* baj, int n, double* vt, cudaStream_t s);
+void launch_relax_dpv(const double* u, const double* vt, const double* cc, int n, const double* ubase, double dt,
+                      double* out, cudaStream_t s);
+// u(nf,n^3) (float or double) <-> density; flag |= 1 when a component 2..nf is not zero
+void launch_extract_density_f(const float* u, int nf, i64 n3, double* rho, int* flag, cudaStream_t s);
+void launch_extract_density_d(const double* u, int nf, i64 n3, double* rho, int* flag, cudaStream_t s);
+
+}  // namespace mmh

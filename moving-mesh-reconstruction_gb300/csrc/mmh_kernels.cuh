@@ -1,0 +1,415 @@
+// MMH reconstruction hot path -- CUDA kernels for sm_103a (GB300).
+//
+// Every kernel restates one routine of pandaPQY/Moving-Mesh-reconstruction
+// (mmh/*.f90) with the reference's operand order.  The FP64 translation unit is
+// compiled with --fmad=false, so the FP64 kernels round exactly like the CPU
+// restatement and reproduce it bit for bit; the FP32 unit (mixed-precision
+// inner V-cycle) keeps FMA contraction.
+//
+// Layout: a(i,j,k) of the Fortran arrays is a[i + n*(j + n*k)] (0-based),
+// periodic in all three directions.  Metric coefficients are 6 planes of n^3
+// (structure of arrays).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mmh_internal.h"
+
+namespace mmh {
+
+typedef long long i64;
+
+__device__ __forceinline__ int wp(int i, int n) { return i + 1 == n ? 0 : i + 1; }
+__device__ __forceinline__ int wm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
+__device__ __forceinline__ i64 IDX(int i, int j, int k, int n) { return (i64)i + (i64)n * ((i64)j + (i64)n * (i64)k); }
+
+__device__ __forceinline__ void cell_of(i64 t, int n, int& i, int& j, int& k) {
+  i = (int)(t % n);
+  i64 r = t / n;
+  j = (int)(r % n);
+  k = (int)(r / n);
+}
+
+// ---------------------------------------------------------------------------
+// Reductions
+// ---------------------------------------------------------------------------
+// Exact 128-bit fixed-point sum (2^-64 resolution, |term| < 2^32), matching the
+// oracle: sums do not depend on launch shape or order.
+__device__ __forceinline__ __int128 fx_of(double x) {
+  double a = fabs(x) * 18446744073709551616.0;
+  double q = floor(a * 5.42101086242752217e-20);
+  double rem = a - q * 18446744073709551616.0;
+  unsigned __int128 v = ((unsigned __int128)__double2ull_rz(q) << 64) | (unsigned __int128)__double2ull_rz(rem);
+  return x < 0 ? -(__int128)v : (__int128)v;
+}
+__device__ __forceinline__ double fx_to(unsigned long long lo, unsigned long long hi) {
+  __int128 s = (__int128)(((unsigned __int128)hi << 64) | (unsigned __int128)lo);
+  bool neg = s < 0;
+  unsigned __int128 a = neg ? (unsigned __int128)(-s) : (unsigned __int128)s;
+  unsigned long long h = (unsigned long long)(a >> 64), l = (unsigned long long)a;
+  double r = __dadd_rn(__ull2double_rn(h), __dmul_rn(__ull2double_rn(l), 5.42101086242752217e-20));
+  return neg ? -r : r;
+}
+
+__device__ __forceinline__ unsigned long long shfl_down_u64(unsigned long long v, int d) {
+  return __shfl_down_sync(0xffffffffu, v, d);
+}
+
+// Block-wide reduction of a 128-bit accumulator, then two 64-bit atomics
+// (two's-complement addition is order independent).  acc[0]=lo, acc[1]=hi.
+__device__ __forceinline__ void fx_block_commit(__int128 v, unsigned long long* acc) {
+  __shared__ unsigned long long s_lo[32], s_hi[32];
+  unsigned long long lo = (unsigned long long)v, hi = (unsigned long long)((unsigned __int128)v >> 64);
+  for (int d = 16; d > 0; d >>= 1) {
+    unsigned long long olo = shfl_down_u64(lo, d), ohi = shfl_down_u64(hi, d);
+    unsigned long long nlo = lo + olo;
+    hi = hi + ohi + (nlo < lo ? 1ull : 0ull);
+    lo = nlo;
+  }
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) { s_lo[w] = lo; s_hi[w] = hi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long tl = 0, th = 0;
+    int nw = (blockDim.x + 31) >> 5;
+    for (int q = 0; q < nw; ++q) {
+      unsigned long long nl = tl + s_lo[q];
+      th = th + s_hi[q] + (nl < tl ? 1ull : 0ull);
+      tl = nl;
+    }
+    unsigned long long old = atomicAdd(&acc[0], tl);
+    unsigned long long carry = (old + tl < old) ? 1ull : 0ull;
+    atomicAdd(&acc[1], th + carry);
+  }
+}
+
+// order-preserving map of a double onto uint64 (for atomic min/max)
+__device__ __forceinline__ unsigned long long ord_of(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+  for (int d = 16; d > 0; d >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, d));
+  return v;
+}
+
+// max of non-negative values (NaN wins: its bit pattern is above +inf)
+__device__ __forceinline__ void block_max_commit(double v, unsigned long long* out) {
+  __shared__ unsigned long long s_m[32];
+  unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  for (int d = 16; d > 0; d >>= 1) {
+    unsigned long long o = shfl_down_u64(b, d);
+    b = o > b ? o : b;
+  }
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) s_m[w] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long m = 0;
+    int nw = (blockDim.x + 31) >> 5;
+    for (int q = 0; q < nw; ++q) m = s_m[q] > m ? s_m[q] : m;
+    atomicMax(out, m);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Curvilinear metric (cbajraw, mmh/gauss1.f90:1107-1210, non-lsquare branch)
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_metric(const T* __restrict__ def, const T* __restrict__ rho, int n, T di2, T* __restrict__ coef) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  int i, j, k;
+  cell_of(t, n, i, j, k);
+  int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
+  T c = def[t];
+  T phixx = (def[IDX(ip, j, k, n)] - T(2) * c + def[IDX(im, j, k, n)]) * di2;
+  T phiyy = (def[IDX(i, jp, k, n)] - T(2) * c + def[IDX(i, jm, k, n)]) * di2;
+  T phizz = (def[IDX(i, j, kp, n)] - T(2) * c + def[IDX(i, j, km, n)]) * di2;
+  T phixy = (def[IDX(ip, jp, k, n)] - def[IDX(im, jp, k, n)] - def[IDX(ip, jm, k, n)] + def[IDX(im, jm, k, n)]) * di2 / T(4);
+  T phiyz = (def[IDX(i, jp, kp, n)] - def[IDX(i, jp, km, n)] - def[IDX(i, jm, kp, n)] + def[IDX(i, jm, km, n)]) * di2 / T(4);
+  T phixz = (def[IDX(ip, j, kp, n)] - def[IDX(im, j, kp, n)] - def[IDX(ip, j, km, n)] + def[IDX(im, j, km, n)]) * di2 / T(4);
+  T a11 = T(1) + phixx, a12 = phixy, a13 = phixz, a22 = T(1) + phiyy, a23 = phiyz, a33 = T(1) + phizz;
+  T det = a11 * a22 * a33 + T(2) * a12 * a13 * a23 - a13 * a13 * a22 - a11 * (a23 * a23) - a12 * a12 * a33;
+  T b11 = (a22 * a33 - a23 * a23);
+  T b12 = (a13 * a23 - a12 * a33);
+  T b13 = (a12 * a23 - a13 * a22);
+  T b22 = (a11 * a33 - a13 * a13);
+  T b23 = (a12 * a13 - a11 * a23);
+  T b33 = (a11 * a22 - a12 * a12);
+  if (det <= T(1.e-5)) {
+    b11 = T(1); b12 = T(0); b13 = T(0); b22 = T(1); b23 = T(0); b33 = T(1); det = T(1);
+  }
+  const int is[3] = {im, i, ip}, js[3] = {jm, j, jp}, ks[3] = {km, k, kp};
+  T urg = rho[IDX(im, jm, km, n)];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        if (a == 0 && b == 0 && d == 0) continue;
+        urg = urg + rho[IDX(is[a], js[b], ks[d], n)];
+      }
+  urg = urg / T(27);
+  coef[0 * n3 + t] = urg * b11 / det;
+  coef[1 * n3 + t] = urg * b12 / det;
+  coef[2 * n3 + t] = urg * b13 / det;
+  coef[3 * n3 + t] = urg * b22 / det;
+  coef[4 * n3 + t] = urg * b23 / det;
+  coef[5 * n3 + t] = urg * b33 / det;
+}
+
+// ---------------------------------------------------------------------------
+// 19-point operator pieces (relaxplane gauss1.f90:950-980, calcresid :683-709)
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ void op_terms(const T* __restrict__ phi, const T* __restrict__ coef, int n, i64 n3, int i,
+                                         int j, int k, T& tdiag, T& t1, T& t2) {
+  int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
+  const T* f1 = coef;
+  const T* f2 = coef + n3;
+  const T* f3 = coef + 2 * n3;
+  const T* f4 = coef + 3 * n3;
+  const T* f5 = coef + 4 * n3;
+  const T* f6 = coef + 5 * n3;
+  i64 c = IDX(i, j, k, n);
+  i64 cip = IDX(ip, j, k, n), cim = IDX(im, j, k, n), cjp = IDX(i, jp, k, n), cjm = IDX(i, jm, k, n);
+  i64 ckp = IDX(i, j, kp, n), ckm = IDX(i, j, km, n);
+  T b11p = (f1[cip] + f1[c]) / T(2);
+  T b11m = (f1[cim] + f1[c]) / T(2);
+  T b22p = (f4[cjp] + f4[c]) / T(2);
+  T b22m = (f4[cjm] + f4[c]) / T(2);
+  T b33p = (f6[ckp] + f6[c]) / T(2);
+  T b33m = (f6[ckm] + f6[c]) / T(2);
+  tdiag = -(b11p + b11m + b22p + b22m + b33p + b33m);
+  t1 = (b11p * phi[cip] + b11m * phi[cim] + b22p * phi[cjp] + b22m * phi[cjm] + b33p * phi[ckp] + b33m * phi[ckm]);
+  T ppk = phi[IDX(ip, jp, k, n)], mpk = phi[IDX(im, jp, k, n)], pmk = phi[IDX(ip, jm, k, n)], mmk = phi[IDX(im, jm, k, n)];
+  T jpkp = phi[IDX(i, jp, kp, n)], jmkp = phi[IDX(i, jm, kp, n)], jpkm = phi[IDX(i, jp, km, n)], jmkm = phi[IDX(i, jm, km, n)];
+  T ipkp = phi[IDX(ip, j, kp, n)], imkp = phi[IDX(im, j, kp, n)], ipkm = phi[IDX(ip, j, km, n)], imkm = phi[IDX(im, j, km, n)];
+  t2 = ((ppk - mpk) * f2[cjp]
+        - (pmk - mmk) * f2[cjm]
+        + (ppk - pmk) * f2[cip]
+        - (mpk - mmk) * f2[cim]
+        + (jpkp - jmkp) * f5[ckp]
+        - (jpkm - jmkm) * f5[ckm]
+        + (jpkp - jpkm) * f5[cjp]
+        - (jmkp - jmkm) * f5[cjm]
+        + (ipkp - imkp) * f3[ckp]
+        - (ipkm - imkm) * f3[ckm]
+        + (ipkp - ipkm) * f3[cip]
+        - (imkp - imkm) * f3[cim]) / T(4);
+}
+
+// One colour of the 8-colour Gauss-Seidel sweep: planes with k%2 == kpar,
+// i%2 == io, j%2 == jo (0-based).  Sweep order kpar(0,1) x io(0,1) x jo(0,1)
+// reproduces the reference's plane schedule (r1lax) exactly.
+template <class T>
+__global__ void k_gs_colour(T* __restrict__ phi, const T* __restrict__ rhs, const T* __restrict__ coef, int n, T dx2,
+                            int kpar, int io, int jo) {
+  int h = n >> 1;
+  i64 tot = (i64)h * h * h;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= tot) return;
+  int ti = (int)(t % h);
+  i64 r = t / h;
+  int tj = (int)(r % h), tk = (int)(r / h);
+  int i = 2 * ti + io, j = 2 * tj + jo, k = 2 * tk + kpar;
+  i64 n3 = (i64)n * n * n;
+  T tdiag, t1, t2;
+  op_terms(phi, coef, n, n3, i, j, k, tdiag, t1, t2);
+  i64 c = IDX(i, j, k, n);
+  phi[c] = (rhs[c] * dx2 - t1 - t2) / tdiag;
+}
+
+// Residual r = rhs - L[phi] on every cell (calcresid), max-norm into maxbits.
+// r may be null; r32 (float copy of the residual) may be null.
+template <class T>
+__global__ void k_residual(const T* __restrict__ phi, const T* __restrict__ rhs, const T* __restrict__ coef, int n,
+                           T di2, T* __restrict__ r, float* __restrict__ r32, unsigned long long* maxbits) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  double m = 0.0;
+  if (t < n3) {
+    int i, j, k;
+    cell_of(t, n, i, j, k);
+    T tdiag, t1, t2;
+    op_terms(phi, coef, n, n3, i, j, k, tdiag, t1, t2);
+    T tr = rhs[t] - (t1 + t2 + tdiag * phi[t]) * di2;
+    if (r) r[t] = tr;
+    if (r32) r32[t] = (float)tr;
+    m = fabs((double)tr);
+  }
+  if (maxbits) block_max_commit(m, maxbits);
+}
+
+// Full-weighting restriction of the residual with the reference's
+// accumulation order (calcresid gauss1.f90:819-859 as scheduled by r1lax):
+// coarse plane `special` adds its own-plane part first, all others their
+// lower-plane part first.
+template <class T>
+__global__ void k_restrict_resid(const T* __restrict__ r, int n, int special, T* __restrict__ coarse) {
+  int nh = n >> 1;
+  i64 tot = (i64)nh * nh * nh;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= tot) return;
+  int I, J, K;
+  cell_of(t, nh, I, J, K);
+  int ib = 2 * I, ibp = (ib + 1) % n, ibm = (ib + n - 1) % n;
+  int jb = 2 * J, jbp = (jb + 1) % n, jbm = (jb + n - 1) % n;
+  int kb = 2 * K, kbp = kb + 1, kl = (kb + n - 1) % n;
+#define R_(x, y, z) r[IDX(x, y, z, n)]
+  T lower_a = R_(ib, jb, kl) / T(16);
+  T lower_b = (R_(ibp, jb, kl) + R_(ibm, jb, kl) + R_(ib, jbp, kl) + R_(ib, jbm, kl)) / T(32);
+  T lower_c = (R_(ibp, jbp, kl) + R_(ibp, jbm, kl) + R_(ibm, jbp, kl) + R_(ibm, jbm, kl)) / T(64);
+  T main_a = R_(ib, jb, kb) / T(8);
+  T main_b = (R_(ibp, jb, kb) + R_(ibm, jb, kb) + R_(ib, jbp, kb) + R_(ib, jbm, kb) + R_(ib, jb, kbp)) / T(16);
+  T main_c = (R_(ibp, jbp, kb) + R_(ibp, jbm, kb) + R_(ibm, jbp, kb) + R_(ibm, jbm, kb) + R_(ibp, jb, kbp) +
+              R_(ibm, jb, kbp) + R_(ib, jbp, kbp) + R_(ib, jbm, kbp)) / T(32);
+  T main_d = (R_(ibp, jbp, kbp) + R_(ibp, jbm, kbp) + R_(ibm, jbp, kbp) + R_(ibm, jbm, kbp)) / T(64);
+#undef R_
+  T acc = T(0);
+  if (K == special) {
+    acc = acc + main_a + main_b + main_c + main_d;
+    acc = acc + lower_a + lower_b + lower_c;
+  } else {
+    acc = acc + lower_a + lower_b + lower_c;
+    acc = acc + main_a + main_b + main_c + main_d;
+  }
+  coarse[t] = acc;
+}
+
+// 27-point full weighting [1/4,1/2,1/4]^3 (restrict mgutil.f90:74-118 at the
+// odd fine points, nsmooth limiter.f90:677-781 at every point).
+template <class T>
+__device__ __forceinline__ T smooth27(const T* __restrict__ a, int n, int i, int j, int k) {
+  int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
+#define A_(x, y, z) a[IDX(x, y, z, n)]
+  return A_(i, j, k) / T(8) +
+         (A_(ip, j, k) + A_(im, j, k) + A_(i, jp, k) + A_(i, jm, k) + A_(i, j, kp) + A_(i, j, km)) / T(16) +
+         (A_(ip, jp, k) + A_(ip, jm, k) + A_(im, jp, k) + A_(im, jm, k) + A_(ip, j, kp) + A_(ip, j, km) +
+          A_(im, j, kp) + A_(im, j, km) + A_(i, jp, kp) + A_(i, jp, km) + A_(i, jm, kp) + A_(i, jm, km)) / T(32) +
+         (A_(ip, jp, kp) + A_(ip, jp, km) + A_(ip, jm, kp) + A_(ip, jm, km) + A_(im, jp, kp) + A_(im, jp, km) +
+          A_(im, jm, kp) + A_(im, jm, km)) / T(64);
+#undef A_
+}
+
+template <class T>
+__global__ void k_restrict27(const T* __restrict__ fine, int n, T* __restrict__ coarse) {
+  int nh = n >> 1;
+  i64 tot = (i64)nh * nh * nh;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= tot) return;
+  int I, J, K;
+  cell_of(t, nh, I, J, K);
+  coarse[t] = smooth27(fine, n, 2 * I, 2 * J, 2 * K);
+}
+
+template <class T>
+__global__ void k_smooth27(const T* __restrict__ in, int n, T* __restrict__ out) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  int i, j, k;
+  cell_of(t, n, i, j, k);
+  out[t] = smooth27(in, n, i, j, k);
+}
+
+// inject (mgutil.f90:38-71): u += trilinear prolongation of uh.
+template <class T>
+__global__ void k_prolong_add(T* __restrict__ u, const T* __restrict__ uh, int n) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  int i, j, k;
+  cell_of(t, n, i, j, k);
+  int nh = n >> 1;
+  int ibl = i >> 1, ibh = (i + 1) >> 1, jbl = j >> 1, jbh = (j + 1) >> 1, kbl = k >> 1, kbh = (k + 1) >> 1;
+  if (ibh >= nh) ibh = 0;
+  if (jbh >= nh) jbh = 0;
+  if (kbh >= nh) kbh = 0;
+#define H_(x, y, z) uh[IDX(x, y, z, nh)]
+  u[t] = u[t] + (H_(ibl, jbl, kbl) + H_(ibl, jbl, kbh) + H_(ibl, jbh, kbl) + H_(ibl, jbh, kbh) + H_(ibh, jbh, kbl) +
+                 H_(ibh, jbh, kbh) + H_(ibh, jbl, kbl) + H_(ibh, jbl, kbh)) / T(8);
+#undef H_
+}
+
+// Exact sum of a[0..count) into acc (lo, hi); flag |= 1 on a term out of range.
+template <class T>
+__global__ void k_fxsum(const T* __restrict__ a, i64 count, unsigned long long* acc, int* flag) {
+  __int128 s = 0;
+  bool bad = false;
+  for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (i64)gridDim.x * blockDim.x) {
+    double x = (double)a[t];
+    if (!(fabs(x) < 4294967296.0)) bad = true;
+    else s += fx_of(x);
+  }
+  if (bad) atomicOr(flag, 1);
+  fx_block_commit(s, acc);
+}
+
+// det of I + Hess(def)/dx^2 without the tangle fallback (rgzerosum gauss1.f90:1390-1402)
+template <class T>
+__global__ void k_det(const T* __restrict__ def, int n, T di2, T* __restrict__ det) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  int i, j, k;
+  cell_of(t, n, i, j, k);
+  int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
+  T c = def[t];
+  T phixx = (def[IDX(ip, j, k, n)] - T(2) * c + def[IDX(im, j, k, n)]) * di2;
+  T phiyy = (def[IDX(i, jp, k, n)] - T(2) * c + def[IDX(i, jm, k, n)]) * di2;
+  T phizz = (def[IDX(i, j, kp, n)] - T(2) * c + def[IDX(i, j, km, n)]) * di2;
+  T phixy = (def[IDX(ip, jp, k, n)] - def[IDX(im, jp, k, n)] - def[IDX(ip, jm, k, n)] + def[IDX(im, jm, k, n)]) * di2 / T(4);
+  T phiyz = (def[IDX(i, jp, kp, n)] - def[IDX(i, jp, km, n)] - def[IDX(i, jm, kp, n)] + def[IDX(i, jm, km, n)]) * di2 / T(4);
+  T phixz = (def[IDX(ip, j, kp, n)] - def[IDX(im, j, kp, n)] - def[IDX(ip, j, km, n)] + def[IDX(im, j, km, n)]) * di2 / T(4);
+  T a11 = T(1) + phixx, a12 = phixy, a13 = phixz, a22 = T(1) + phiyy, a23 = phiyz, a33 = T(1) + phizz;
+  det[t] = (a11 * a22 * a33 + T(2) * a12 * a13 * a23 - a13 * a13 * a22 - a11 * (a23 * a23) - a12 * a12 * a33);
+}
+
+// scalars: sc[0] = zerosum mean, sc[1] = rgzerosum dfact, sc[2] = usum
+__global__ void k_fx_mean(const unsigned long long* acc, double count, double* out);
+__global__ void k_fx_ratio(const unsigned long long* num, const unsigned long long* den, double* out);
+
+template <class T>
+__global__ void k_sub_mean(T* __restrict__ a, i64 count, const double* __restrict__ mean) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  a[t] = (T)((double)a[t] - *mean);
+}
+
+// rhs = rhs - dfact * det, dfact rounded to T (rgzerosum)
+template <class T>
+__global__ void k_sub_dfact(T* __restrict__ a, const T* __restrict__ det, i64 count, const double* __restrict__ ratio) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  T dfact = (T)(*ratio);
+  a[t] = a[t] - dfact * det[t];
+}
+
+template <class T>
+__global__ void k_fill(T* __restrict__ a, i64 count, T v) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < count) a[t] = v;
+}
+
+// a = v where the guard flag is set, else untouched (device-side divergence guard)
+template <class T>
+__global__ void k_zero_if(T* __restrict__ a, i64 count, const int* __restrict__ flag) {
+  if (*flag == 0) return;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < count) a[t] = T(0);
+}
+template <class T>
+__global__ void k_sub_mean_unless(T* __restrict__ a, i64 count, const double* __restrict__ mean,
+                                  const int* __restrict__ flag) {
+  if (*flag != 0) return;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  a[t] = (T)((double)a[t] - *mean);
+}
+
+}  // namespace mmh

@@ -1,0 +1,571 @@
+// FP64 kernels of the MMH hot path.  Compiled with --fmad=false: every
+// expression rounds as written, so results match the CPU restatement bit for
+// bit (except where a libm function -- acos, cos -- is involved).
+#include <atomic>
+
+#include "mmh_launch.cuh"
+#include "mmh_phys.cuh"
+
+namespace mmh {
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch(int k) { g_launches.fetch_add((unsigned long long)k, std::memory_order_relaxed); }
+unsigned long long launch_count() { return g_launches.load(); }
+
+MMH_INSTANTIATE(double)
+
+// ---------------------------------------------------------------------------
+// scalar helpers
+// ---------------------------------------------------------------------------
+__global__ void k_fx_mean(const unsigned long long* acc, double count, double* out) {
+  *out = fx_to(acc[0], acc[1]) / count;
+}
+__global__ void k_fx_ratio(const unsigned long long* num, const unsigned long long* den, double* out) {
+  *out = fx_to(num[0], num[1]) / fx_to(den[0], den[1]);
+}
+void launch_fx_mean(const unsigned long long* acc, double count, double* out, cudaStream_t s) {
+  k_fx_mean<<<1, 1, 0, s>>>(acc, count, out);
+  count_launch();
+}
+void launch_fx_ratio(const unsigned long long* num, const unsigned long long* den, double* out, cudaStream_t s) {
+  k_fx_ratio<<<1, 1, 0, s>>>(num, den, out);
+  count_launch();
+}
+
+__global__ void k_guard(const unsigned long long* r1bits, const unsigned long long* errbits, double margin,
+                        double floor_, int* flag, int* guards) {
+  double r1 = __longlong_as_double((long long)*r1bits);
+  double err = __longlong_as_double((long long)*errbits);
+  int g = (err > r1 * margin && r1 > floor_) ? 1 : 0;
+  *flag = g;
+  if (g) *guards += 1;
+}
+void launch_guard(const unsigned long long* r1bits, const unsigned long long* errbits, double margin, double floor_,
+                  int* flag, int* guards, cudaStream_t s) {
+  k_guard<<<1, 1, 0, s>>>(r1bits, errbits, margin, floor_, flag, guards);
+  count_launch();
+}
+
+__global__ void k_d2f(const double* __restrict__ a, float* __restrict__ b, i64 count) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < count) b[t] = (float)a[t];
+}
+__global__ void k_f2d(const float* __restrict__ a, double* __restrict__ b, i64 count) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < count) b[t] = (double)a[t];
+}
+__global__ void k_add_f2d(double* __restrict__ a, const float* __restrict__ b, i64 count) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < count) a[t] = a[t] + (double)b[t];
+}
+__global__ void k_add(double* __restrict__ a, const double* __restrict__ b, i64 count) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < count) a[t] = a[t] + b[t];
+}
+void launch_d2f(const double* a, float* b, i64 count, cudaStream_t s) {
+  k_d2f<<<grid_of(count, kBlock), kBlock, 0, s>>>(a, b, count);
+  count_launch();
+}
+void launch_f2d(const float* a, double* b, i64 count, cudaStream_t s) {
+  k_f2d<<<grid_of(count, kBlock), kBlock, 0, s>>>(a, b, count);
+  count_launch();
+}
+void launch_add_f2d(double* a, const float* b, i64 count, cudaStream_t s) {
+  k_add_f2d<<<grid_of(count, kBlock), kBlock, 0, s>>>(a, b, count);
+  count_launch();
+}
+void launch_add(double* a, const double* b, i64 count, cudaStream_t s) {
+  k_add<<<grid_of(count, kBlock), kBlock, 0, s>>>(a, b, count);
+  count_launch();
+}
+
+// ---------------------------------------------------------------------------
+// calcdefp right-hand side and limiter
+// ---------------------------------------------------------------------------
+__global__ void k_calcdefp_rhs(double* __restrict__ tmp, const double* __restrict__ rho, i64 n3, double dtold) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  double t1 = 1.0 - rho[t];
+  const double xhigh = 2.0;
+  if (fabs(t1) > xhigh) t1 = t1 >= 0.0 ? xhigh : -xhigh;
+  tmp[t] = t1 / 30.0 / dtold;
+}
+void launch_calcdefp_rhs(double* tmp, const double* rho, int n, double dtold, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  k_calcdefp_rhs<<<grid_of(n3, kBlock), kBlock, 0, s>>>(tmp, rho, n3, dtold);
+  count_launch();
+}
+
+// Block reduction of a uint64: op 0 = sum, 1 = max, 2 = min.  Result valid in
+// thread 0; every thread of the block must call it.
+__device__ __forceinline__ unsigned long long block_u64(unsigned long long v, unsigned long long* buf, int op) {
+  for (int d = 16; d > 0; d >>= 1) {
+    unsigned long long o = __shfl_down_sync(0xffffffffu, v, d);
+    v = op == 0 ? v + o : (op == 1 ? (o > v ? o : v) : (o < v ? o : v));
+  }
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) buf[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    v = buf[0];
+    for (int q = 1; q < nw; ++q) {
+      unsigned long long o = buf[q];
+      v = op == 0 ? v + o : (op == 1 ? (o > v ? o : v) : (o < v ? o : v));
+    }
+  }
+  return v;
+}
+
+__global__ void k_limiter_pass1(double* __restrict__ tmp, const double* __restrict__ def,
+                                const double* __restrict__ rho, int n, double dtold, double dtaumesh,
+                                double cmpmaxglobal, LimDev* st, uint8_t* __restrict__ maskx,
+                                uint8_t* __restrict__ maskc) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  __int128 r2 = 0;
+  bool bad = false;
+  unsigned long long nexp = 0;
+  double dmax = 0.0, dmin = 1.0, fmx = 0.0, fmn = 0.0;
+  if (t < n3) {
+    int i, j, km;
+    cell_of(t, n, i, j, km);
+    int k = wp(km, n);
+    LimM m = lim_metric(def, n, i, j, k);
+    double det = m.det;
+    double rl = rho[t];
+    double q = rl * rl / det;
+    if (!(fabs(q) < 4294967296.0)) bad = true;
+    else r2 = fx_of(q);
+    // momentum-flux divergence of a state at rest is zero (u(2:4) = 0)
+    double eflux = 0.0 + tmp[t];
+    uint8_t mx = 0, mc = 0;
+    const double densinit = 1.0;
+    if (det > 10.0 * densinit) {
+      eflux = -2.0 * fabs(eflux);
+      nexp = 1;
+      mx = 1;
+    }
+    double compression = compression_of(1.0 + m.phixx, m.phixy, m.phixz, 1.0 + m.phiyy, m.phiyz, 1.0 + m.phizz);
+    double cmpmax = cmpmaxglobal * 1.0;
+    double tlim = 3.0 * (1.0 / cmpmax - 1.0 / compression) / dtold;
+    if (tlim > 0.0) {
+      eflux = fmax(0.0, eflux);
+      mc = 1;
+    }
+    dmax = det;
+    dmin = det;
+    eflux = fmin(1.0 / dtaumesh, eflux);
+    eflux = fmax(-1.0 / dtaumesh, eflux);
+    tmp[t] = eflux;
+    fmx = fmax(0.0, eflux * dtold);
+    fmn = fmin(0.0, eflux * dtold);
+    if (maskx) maskx[t] = mx;
+    if (maskc) maskc[t] = mc;
+  }
+  // block reductions, one atomic per block and statistic
+  __shared__ unsigned long long s_buf[32];
+  unsigned long long v;
+  v = block_u64(nexp, s_buf, 0);
+  if (threadIdx.x == 0 && v) atomicAdd(&st->nexpand, v);
+  v = block_u64(ord_of(dmax), s_buf, 1);
+  if (threadIdx.x == 0) atomicMax(&st->detmax, v);
+  v = block_u64(ord_of(dmin), s_buf, 2);
+  if (threadIdx.x == 0) atomicMin(&st->detmin, v);
+  v = block_u64(ord_of(fmx), s_buf, 1);
+  if (threadIdx.x == 0) atomicMax(&st->fluxmax, v);
+  v = block_u64(ord_of(fmn), s_buf, 2);
+  if (threadIdx.x == 0) atomicMin(&st->fluxmin, v);
+  if (bad) atomicOr(&st->flag, 2);
+  fx_block_commit(r2, st->rho2);
+}
+
+void launch_limiter_pass1(double* tmp, const double* def, const double* rho, int n, double dtold, double dtaumesh,
+                          LimDev* st, uint8_t* maskx, uint8_t* maskc, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  k_limiter_pass1<<<grid_of(n3, kBlock), kBlock, 0, s>>>(tmp, def, rho, n, dtold, dtaumesh, 10.0, st, maskx, maskc);
+  count_launch();
+}
+
+__global__ void k_limiter_mask(double* __restrict__ defplim, const double* __restrict__ def,
+                               const double* __restrict__ defp, int n, double dtold, double cmpmaxglobal, LimDev* st,
+                               uint8_t* __restrict__ mask) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long cnt = 0, cm = ord_of(0.0);
+  if (t < n3) {
+    int i, j, k;
+    cell_of(t, n, i, j, k);
+    int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
+#define P_(x, y, z) defp[IDX(x, y, z, n)]
+#define D_(x, y, z) def[IDX(x, y, z, n)]
+    double phixx = (P_(ip, j, k) - 2.0 * P_(i, j, k) + P_(im, j, k)) * dtold;
+    double phiyy = (P_(i, jp, k) - 2.0 * P_(i, j, k) + P_(i, jm, k)) * dtold;
+    double phizz = (P_(i, j, kp) - 2.0 * P_(i, j, k) + P_(i, j, km)) * dtold;
+    double phixy = (P_(ip, jp, k) - P_(im, jp, k) - P_(ip, jm, k) + P_(im, jm, k)) / 4.0 * dtold;
+    double phiyz = (P_(i, jp, kp) - P_(i, jp, km) - P_(i, jm, kp) + P_(i, jm, km)) / 4.0 * dtold;
+    double phixz = (P_(ip, j, kp) - P_(im, j, kp) - P_(ip, j, km) + P_(im, j, km)) / 4.0 * dtold;
+    phixx = phixx + (D_(ip, j, k) - 2.0 * D_(i, j, k) + D_(im, j, k));
+    phiyy = phiyy + (D_(i, jp, k) - 2.0 * D_(i, j, k) + D_(i, jm, k));
+    phizz = phizz + (D_(i, j, kp) - 2.0 * D_(i, j, k) + D_(i, j, km));
+    phixy = phixy + (D_(ip, jp, k) - D_(im, jp, k) - D_(ip, jm, k) + D_(im, jm, k)) / 4.0;
+    phiyz = phiyz + (D_(i, jp, kp) - D_(i, jp, km) - D_(i, jm, kp) + D_(i, jm, km)) / 4.0;
+    phixz = phixz + (D_(ip, j, kp) - D_(im, j, kp) - D_(ip, j, km) + D_(im, j, km)) / 4.0;
+#undef P_
+#undef D_
+    double compression = compression_of(1.0 + phixx, phixy, phixz, 1.0 + phiyy, phiyz, 1.0 + phizz);
+    double cmpmax = cmpmaxglobal * 1.0;
+    double tlim = 3.0 * (1.0 / cmpmax - 1.0 / compression) / dtold;
+    cm = ord_of(fmax(0.0, compression));
+    double v = 0.0;
+    uint8_t mk = 0;
+    if (tlim > 0.0) {
+      cnt = 1;
+      v = tlim;
+      mk = 1;
+    }
+    defplim[t] = v;
+    if (mask) mask[t] = mk;
+  }
+  __shared__ unsigned long long s_buf[32];
+  unsigned long long r = block_u64(cnt, s_buf, 0);
+  if (threadIdx.x == 0 && r) atomicAdd(&st->ncompress, r);
+  r = block_u64(cm, s_buf, 1);
+  if (threadIdx.x == 0) atomicMax(&st->cmax, r);
+}
+
+void launch_limiter_mask(double* defplim, const double* def, const double* defp, int n, double dtold, LimDev* st,
+                         uint8_t* mask, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  k_limiter_mask<<<grid_of(n3, kBlock), kBlock, 0, s>>>(defplim, def, defp, n, dtold, 10.0, st, mask);
+  count_launch();
+}
+
+__global__ void k_lim_reset(LimDev* st) {
+  st->nexpand = 0;
+  st->ncompress = 0;
+  st->detmax = ord_of(0.0);
+  st->detmin = ord_of(1.0);
+  st->fluxmax = ord_of(0.0);
+  st->fluxmin = ord_of(0.0);
+  st->cmax = ord_of(0.0);
+  st->rho2[0] = 0;
+  st->rho2[1] = 0;
+  st->flag = 0;
+}
+void launch_lim_reset(LimDev* st, cudaStream_t s) {
+  k_lim_reset<<<1, 1, 0, s>>>(st);
+  count_launch();
+}
+
+// ---------------------------------------------------------------------------
+// Spectral kernels
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 spec_mode(double2 x, int kx, int ky, int kz, int n, int mode) {
+  const double pi = 3.14159265358979323846264338328;
+  double re = x.x, im = x.y;
+  if (mode <= 2) {
+    // cmp * cmplx(0,kk) / n * 2 * pi  (gradient.f90:21,43,65)
+    double kk;
+    if (mode == 0) kk = (double)kx;
+    else if (mode == 1) kk = (ky + 1 <= n / 2 + 1) ? (double)ky : (double)(ky - n);
+    else kk = (kz + 1 <= n / 2 + 1) ? (double)kz : (double)(kz - n);
+    double r2 = re * 0.0 - im * kk;
+    double i2 = re * kk + im * 0.0;
+    r2 = r2 / n * 2. * pi;
+    i2 = i2 / n * 2. * pi;
+    return make_double2(r2, i2);
+  } else if (mode == 3) {
+    // *(k1^2 + k2^2 + k3^2)  (reconstruct.f90:88-110)
+    double k3 = (kz + 1 <= n / 2 + 1) ? (double)kz : (double)(kz - n);
+    k3 = k3 / n * 2. * pi;
+    double k2 = (ky + 1 <= n / 2 + 1) ? (double)ky : (double)(ky - n);
+    k2 = k2 / n * 2. * pi;
+    double k1 = (double)kx;
+    k1 = k1 / n * 2. * pi;
+    double f = k1 * k1 + k2 * k2 + k3 * k3;
+    return make_double2(re * f, im * f);
+  } else {
+    // / (2cos kx + 2cos ky + 2cos kz - 6), DC real part zeroed (limiter.f90:561-576)
+    double xk = 2 * pi * kx / n;
+    double yk = 2 * pi * (ky + 1 - 1.) / n;
+    double zk = 2 * pi * (kz + 1 - 1.) / n;
+    double akernel = 2 * cos(xk) + 2 * cos(yk) + 2 * cos(zk) - 6;
+    if (fabs(akernel) < 1e-10) akernel = 1;
+    double r2 = re / akernel, i2 = im / akernel;
+    if (kx == 0 && ky == 0 && kz == 0) r2 = 0.0;
+    return make_double2(r2, i2);
+  }
+}
+
+__global__ void k_spec_pack(const double2* __restrict__ Xc, int n, int mode, double2* __restrict__ Z,
+                            const LimDev* st) {
+  if (mode == 4 && st->ncompress == 0) return;
+  int M = n / 2, H = M + 1;
+  i64 tot = (i64)M * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= tot) return;
+  int kx = (int)(t % M);
+  i64 r = t / M;
+  int ky = (int)(r % n), kz = (int)(r / n);
+  int kx2 = M - kx, ky2 = (n - ky) % n, kz2 = (n - kz) % n;
+  // X_NR(k) = conj(Xc(k)) : spectrum with exp(+2 pi i k.x / n)
+  double2 a = Xc[kx + (i64)H * (ky + (i64)n * kz)];
+  double2 b = Xc[kx2 + (i64)H * (ky2 + (i64)n * kz2)];
+  double2 A = spec_mode(make_double2(a.x, -a.y), kx, ky, kz, n, mode);
+  double2 B = spec_mode(make_double2(b.x, -b.y), kx2, ky2, kz2, n, mode);
+  B.y = -B.y;  // conj
+  const double pi = 3.14159265358979323846264338328;
+  double th = -2.0 * pi * kx / n;
+  double wr = cos(th), wi = sin(th);
+  double sr = A.x + B.x, si = A.y + B.y;
+  double dr = A.x - B.x, di = A.y - B.y;
+  double wdr = wr * dr - wi * di, wdi = wr * di + wi * dr;
+  // 0.5*(A+B) + 0.5 i w (A-B)
+  Z[t] = make_double2(0.5 * sr - 0.5 * wdi, 0.5 * si + 0.5 * wdr);
+}
+
+void launch_spec_pack(const void* Xc, int n, int mode, void* Z, const LimDev* st, cudaStream_t s) {
+  i64 tot = (i64)(n / 2) * n * n;
+  k_spec_pack<<<grid_of(tot, kBlock), kBlock, 0, s>>>((const double2*)Xc, n, mode, (double2*)Z, st);
+  count_launch();
+}
+
+__global__ void k_spec_unpack(const double2* __restrict__ z, int n, double* __restrict__ out, int stride_out, int add,
+                              const LimDev* st) {
+  if (add && st->ncompress == 0) return;
+  i64 tot = (i64)(n / 2) * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= tot) return;
+  double2 v = z[t];
+  double a = v.x * 2. / n / n / n;
+  double b = v.y * 2. / n / n / n;
+  i64 o0 = 2 * t, o1 = 2 * t + 1;
+  if (add) {
+    out[o0] = out[o0] + a;
+    out[o1] = out[o1] + b;
+  } else {
+    out[o0 * stride_out] = a;
+    out[o1 * stride_out] = b;
+  }
+}
+
+void launch_spec_unpack(const void* z, int n, double* out, int stride_out, int add, const LimDev* st, cudaStream_t s) {
+  i64 tot = (i64)(n / 2) * n * n;
+  k_spec_unpack<<<grid_of(tot, kBlock), kBlock, 0, s>>>((const double2*)z, n, out, stride_out, add, st);
+  count_launch();
+}
+
+// ---------------------------------------------------------------------------
+// relaxing-TVD, density component (relaxing.f90).  u(2:5) = 0, so the Euler
+// flux of the density is the zero momentum and the pressure vanishes; the
+// expressions below keep the reference's operations on those zero components.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double zdiv(double d) { return 0.0 / d; }
+
+// stage 1: calcbaj + cflkeuler + flux of u at every cell.
+// baj: 7 planes (b11,b12,b13,b22,b23,b33,det); vt: 3 planes (flux along x,y,z)
+__global__ void k_relax_stage1(const double* __restrict__ rho, const double* __restrict__ def,
+                               const double* __restrict__ defp, int n, double* __restrict__ baj,
+                               double* __restrict__ cc, double* __restrict__ vt) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  int i, j, k;
+  cell_of(t, n, i, j, k);
+  const double gamma = 5. / 3.;
+  LimM m = lim_metric(def, n, i, j, k);
+  baj[0 * n3 + t] = m.b11;
+  baj[1 * n3 + t] = m.b12;
+  baj[2 * n3 + t] = m.b13;
+  baj[3 * n3 + t] = m.b22;
+  baj[4 * n3 + t] = m.b23;
+  baj[5 * n3 + t] = m.b33;
+  baj[6 * n3 + t] = m.det;
+  int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
+  double dxp = defp[IDX(ip, j, k, n)], dxm = defp[IDX(im, j, k, n)];
+  double dyp = defp[IDX(i, jp, k, n)], dym = defp[IDX(i, jm, k, n)];
+  double dzp = defp[IDX(i, j, kp, n)], dzm = defp[IDX(i, j, km, n)];
+  double u0 = rho[t];
+  // cflkeuler (relaxing.f90:1097-1135)
+  {
+    double pdx = (dxp - dxm) / 2.0, pdy = (dyp - dym) / 2.0, pdz = (dzp - dzm) / 2.0;
+    double det = m.det;
+    double vx = zdiv(u0), vy = zdiv(u0), vz = zdiv(u0);
+    double rhoc = u0 / det;
+    double kin = rhoc * (vx * vx + vy * vy + vz * vz) / 2.0;
+    double ed = zdiv(det) - kin;
+    double pressure = (gamma - 1.0) * ed;
+    double cs = sqrt(gamma * fabs(pressure / rhoc));
+    double v1 = vx - pdx, v2 = vy - pdy, v3 = vz - pdz;
+    double vv1 = m.b11 * v1 + m.b12 * v2 + m.b13 * v3;
+    double vv2 = m.b12 * v1 + m.b22 * v2 + m.b23 * v3;
+    double vv3 = m.b13 * v1 + m.b23 * v2 + m.b33 * v3;
+    double blim1 = cs * sqrt(m.b11 * m.b11 + m.b12 * m.b12 + m.b13 * m.b13) + fabs(vv1);
+    double blim2 = cs * sqrt(m.b12 * m.b12 + m.b22 * m.b22 + m.b23 * m.b23) + fabs(vv2);
+    double blim3 = cs * sqrt(m.b13 * m.b13 + m.b23 * m.b23 + m.b33 * m.b33) + fabs(vv3);
+    cc[t] = fmax(fmax(blim1, blim2), blim3);
+  }
+  // flux (relaxing.f90:970-988) of the density
+  {
+    double rg = m.det;
+    double mx = zdiv(rg), my = zdiv(rg), mz = zdiv(rg);
+    double pdxg = (dxp - dxm) / 2.0 / rg;
+    double pdyg = (dyp - dym) / 2.0 / rg;
+    double pdzg = (dzp - dzm) / 2.0 / rg;
+    double b11 = m.b11 * rg, b12 = m.b12 * rg, b13 = m.b13 * rg, b22 = m.b22 * rg, b23 = m.b23 * rg, b33 = m.b33 * rg;
+    double vtt1 = mx - u0 * pdxg;
+    double vtt2 = my - u0 * pdyg;
+    double vtt3 = mz - u0 * pdzg;
+    vt[0 * n3 + t] = b11 * vtt1 + b12 * vtt2 + b13 * vtt3;
+    vt[1 * n3 + t] = b12 * vtt1 + b22 * vtt2 + b23 * vtt3;
+    vt[2 * n3 + t] = b13 * vtt1 + b23 * vtt2 + b33 * vtt3;
+  }
+}
+
+void launch_relax_stage1(const double* rho, const double* def, const double* defp, int n, double* baj, double* cc,
+                         double* vt, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  k_relax_stage1<<<grid_of(n3, kBlock), kBlock, 0, s>>>(rho, def, defp, n, baj, cc, vt);
+  count_launch();
+}
+
+__global__ void k_relax_flux(const double* __restrict__ u1, const double* __restrict__ defp,
+                             const double* __restrict__ baj, int n, double* __restrict__ vt) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  int i, j, k;
+  cell_of(t, n, i, j, k);
+  int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
+  double rg = baj[6 * n3 + t];
+  double u0 = u1[t];
+  double mx = zdiv(rg), my = zdiv(rg), mz = zdiv(rg);
+  double pdxg = (defp[IDX(ip, j, k, n)] - defp[IDX(im, j, k, n)]) / 2.0 / rg;
+  double pdyg = (defp[IDX(i, jp, k, n)] - defp[IDX(i, jm, k, n)]) / 2.0 / rg;
+  double pdzg = (defp[IDX(i, j, kp, n)] - defp[IDX(i, j, km, n)]) / 2.0 / rg;
+  double b11 = baj[0 * n3 + t] * rg, b12 = baj[1 * n3 + t] * rg, b13 = baj[2 * n3 + t] * rg;
+  double b22 = baj[3 * n3 + t] * rg, b23 = baj[4 * n3 + t] * rg, b33 = baj[5 * n3 + t] * rg;
+  double vtt1 = mx - u0 * pdxg;
+  double vtt2 = my - u0 * pdyg;
+  double vtt3 = mz - u0 * pdzg;
+  vt[0 * n3 + t] = b11 * vtt1 + b12 * vtt2 + b13 * vtt3;
+  vt[1 * n3 + t] = b12 * vtt1 + b22 * vtt2 + b23 * vtt3;
+  vt[2 * n3 + t] = b13 * vtt1 + b23 * vtt2 + b33 * vtt3;
+}
+
+void launch_relax_flux(const double* u1, const double* defp, const double* baj, int n, double* vt, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  k_relax_flux<<<grid_of(n3, kBlock), kBlock, 0, s>>>(u1, defp, baj, n, vt);
+  count_launch();
+}
+
+__device__ __forceinline__ double fsign1(double a) { return a >= 0.0 ? 1.0 : -1.0; }
+__device__ __forceinline__ double minmod(double a, double b) {
+  const double wslopelim = 1.5, wbee = 1.0;
+  double x = fabs(a), y = fabs(b);
+  double lo = fmin(x, y), hi = fmax(x, y);
+  double mm = fmin(wslopelim * lo, wbee * hi + (1.0 - wbee) * lo);
+  return (fsign1(a) + fsign1(b)) * mm / 2.0;
+}
+__device__ __forceinline__ double wphalf(double um, double vm, double u0, double v0, double up, double vp, double upp,
+                                         double vpp) {
+  double a = (u0 + v0) / 2.0;
+  double b = (up - vp) / 2.0;
+  double da = (up + vp) / 2.0 - a;
+  double dam = a - (um + vm) / 2.0;
+  double ap = a + minmod(dam, da) / 2.0;
+  double db = (upp - vpp) / 2.0 - b;
+  double dbm = b - (u0 - v0) / 2.0;
+  double bp = b - minmod(db, dbm) / 2.0;
+  return ap - bp;
+}
+
+// dpv (relaxing.f90:269-496) for the density, then out = ubase - res*dt.
+__global__ void k_relax_dpv(const double* __restrict__ u, const double* __restrict__ vt,
+                            const double* __restrict__ cc, int n, const double* __restrict__ ubase, double dt,
+                            double* __restrict__ out) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  int i, j, k;
+  cell_of(t, n, i, j, k);
+  const double* vx = vt;
+  const double* vy = vt + n3;
+  const double* vz = vt + 2 * n3;
+  double ck = cc[t];
+  double r;
+  {
+    double uz[5], wz[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      int kq = ((k + q - 2) % n + n) % n;
+      i64 cq = IDX(i, j, kq, n);
+      uz[q] = u[cq];
+      wz[q] = vz[cq] / cc[cq];
+    }
+    double flz1 = wphalf(uz[0], wz[0], uz[1], wz[1], uz[2], wz[2], uz[3], wz[3]);
+    double flz2 = wphalf(uz[1], wz[1], uz[2], wz[2], uz[3], wz[3], uz[4], wz[4]);
+    double ckp = cc[IDX(i, j, wp(k, n), n)], ckm = cc[IDX(i, j, wm(k, n), n)];
+    r = (ckp + ck) / 2.0 * flz2 - (ck + ckm) / 2.0 * flz1;
+  }
+  {
+    double ux[5], wx[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      int iq = ((i + q - 2) % n + n) % n;
+      i64 cq = IDX(iq, j, k, n);
+      ux[q] = u[cq];
+      wx[q] = vx[cq] / cc[cq];
+    }
+    double flx0 = wphalf(ux[1], wx[1], ux[2], wx[2], ux[3], wx[3], ux[4], wx[4]);
+    double flxm = wphalf(ux[0], wx[0], ux[1], wx[1], ux[2], wx[2], ux[3], wx[3]);
+    double cip = cc[IDX(wp(i, n), j, k, n)], cim = cc[IDX(wm(i, n), j, k, n)];
+    double fp = (cip + ck) / 2.0 * flx0;
+    double fm = (ck + cim) / 2.0 * flxm;
+    r = r + fp - fm;
+  }
+  {
+    double uy[5], wy[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      int jq = ((j + q - 2) % n + n) % n;
+      i64 cq = IDX(i, jq, k, n);
+      uy[q] = u[cq];
+      wy[q] = vy[cq] / cc[cq];
+    }
+    double fly0 = wphalf(uy[1], wy[1], uy[2], wy[2], uy[3], wy[3], uy[4], wy[4]);
+    double flym = wphalf(uy[0], wy[0], uy[1], wy[1], uy[2], wy[2], uy[3], wy[3]);
+    double cjp = cc[IDX(i, wp(j, n), k, n)], cjm = cc[IDX(i, wm(j, n), k, n)];
+    r = r + (cjp + ck) / 2.0 * fly0 - (ck + cjm) / 2.0 * flym;
+  }
+  out[t] = ubase[t] - r * dt;
+}
+
+void launch_relax_dpv(const double* u, const double* vt, const double* cc, int n, const double* ubase, double dt,
+                      double* out, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  k_relax_dpv<<<grid_of(n3, kBlock), kBlock, 0, s>>>(u, vt, cc, n, ubase, dt, out);
+  count_launch();
+}
+
+template <class U>
+__global__ void k_extract_density(const U* __restrict__ u, int nf, i64 n3, double* __restrict__ rho, int* flag) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  rho[t] = (double)u[(i64)nf * t];
+  bool nz = false;
+  for (int c = 1; c < nf; ++c) nz = nz || (u[(i64)nf * t + c] != U(0));
+  if (nz) atomicOr(flag, 1);
+}
+void launch_extract_density_f(const float* u, int nf, i64 n3, double* rho, int* flag, cudaStream_t s) {
+  k_extract_density<float><<<grid_of(n3, kBlock), kBlock, 0, s>>>(u, nf, n3, rho, flag);
+  count_launch();
+}
+void launch_extract_density_d(const double* u, int nf, i64 n3, double* rho, int* flag, cudaStream_t s) {
+  k_extract_density<double><<<grid_of(n3, kBlock), kBlock, 0, s>>>(u, nf, n3, rho, flag);
+  count_launch();
+}
+
+}  // namespace mmh

@@ -1,0 +1,167 @@
+// Launcher templates for the multigrid kernels; each precision's translation
+// unit includes this file and instantiates the launchers explicitly.
+#pragma once
+#include "mmh_kernels.cuh"
+
+namespace mmh {
+
+static inline unsigned grid_of(i64 count, int block) { return (unsigned)((count + block - 1) / block); }
+static const int kBlock = 256;
+
+template <class T>
+void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  T di2 = T(1) / (dx * dx);
+  k_metric<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(def, rho, n, di2, coef);
+  count_launch();
+}
+
+template <class T>
+void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, cudaStream_t s) {
+  i64 h3 = (i64)(n / 2) * (n / 2) * (n / 2);
+  T dx2 = dx * dx;
+  unsigned g = grid_of(h3, kBlock);
+  for (int sw = 0; sw < nsweeps; ++sw)
+    for (int kpar = 0; kpar < 2; ++kpar)
+      for (int io = 0; io < 2; ++io)
+        for (int jo = 0; jo < 2; ++jo) {
+          k_gs_colour<T><<<g, kBlock, 0, s>>>(phi, rhs, coef, n, dx2, kpar, io, jo);
+          count_launch();
+        }
+}
+
+template <class T>
+void launch_residual(const T* phi, const T* rhs, const T* coef, int n, T dx, T* r, float* r32,
+                     unsigned long long* maxbits, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  T di2 = T(1) / (dx * dx);
+  k_residual<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(phi, rhs, coef, n, di2, r, r32, maxbits);
+  count_launch();
+}
+
+template <class T>
+void launch_restrict_resid(const T* r, int n, int special, T* coarse, cudaStream_t s) {
+  i64 h3 = (i64)(n / 2) * (n / 2) * (n / 2);
+  k_restrict_resid<T><<<grid_of(h3, kBlock), kBlock, 0, s>>>(r, n, special, coarse);
+  count_launch();
+}
+
+template <class T>
+void launch_restrict27(const T* fine, int n, T* coarse, cudaStream_t s) {
+  i64 h3 = (i64)(n / 2) * (n / 2) * (n / 2);
+  k_restrict27<T><<<grid_of(h3, kBlock), kBlock, 0, s>>>(fine, n, coarse);
+  count_launch();
+}
+
+template <class T>
+void launch_smooth27(const T* in, int n, T* out, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  k_smooth27<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(in, n, out);
+  count_launch();
+}
+
+template <class T>
+void launch_prolong_add(T* u, const T* uh, int n, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  k_prolong_add<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(u, uh, n);
+  count_launch();
+}
+
+template <class T>
+void launch_fxsum(const T* a, i64 count, unsigned long long* acc, int* flag, cudaStream_t s) {
+  i64 blocks = (count + kBlock - 1) / kBlock;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+  k_fxsum<T><<<(unsigned)blocks, kBlock, 0, s>>>(a, count, acc, flag);
+  count_launch();
+}
+
+template <class T>
+void launch_det(const T* def, int n, T dx, T* det, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  T di2 = T(1) / (dx * dx);
+  k_det<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(def, n, di2, det);
+  count_launch();
+}
+
+template <class T>
+void launch_sub_mean(T* a, i64 count, const double* mean, cudaStream_t s) {
+  k_sub_mean<T><<<grid_of(count, kBlock), kBlock, 0, s>>>(a, count, mean);
+  count_launch();
+}
+
+template <class T>
+void launch_sub_dfact(T* a, const T* det, i64 count, const double* ratio, cudaStream_t s) {
+  k_sub_dfact<T><<<grid_of(count, kBlock), kBlock, 0, s>>>(a, det, count, ratio);
+  count_launch();
+}
+
+template <class T>
+void launch_fill(T* a, i64 count, T v, cudaStream_t s) {
+  k_fill<T><<<grid_of(count, kBlock), kBlock, 0, s>>>(a, count, v);
+  count_launch();
+}
+
+template <class T>
+__global__ void k_absmax(const T* __restrict__ a, i64 count, unsigned long long* maxbits) {
+  double m = 0.0;
+  for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (i64)gridDim.x * blockDim.x) {
+    double v = fabs((double)a[t]);
+    m = (v > m || v != v) ? v : m;
+  }
+  block_max_commit(m, maxbits);
+}
+
+template <class T>
+void launch_absmax(const T* a, i64 count, unsigned long long* maxbits, cudaStream_t s) {
+  i64 blocks = (count + kBlock - 1) / kBlock;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+  k_absmax<T><<<(unsigned)blocks, kBlock, 0, s>>>(a, count, maxbits);
+  count_launch();
+}
+
+template <class T>
+void launch_zero_if(T* a, i64 count, const int* flag, cudaStream_t s) {
+  k_zero_if<T><<<grid_of(count, kBlock), kBlock, 0, s>>>(a, count, flag);
+  count_launch();
+}
+
+template <class T>
+void launch_sub_mean_unless(T* a, i64 count, const double* mean, const int* flag, cudaStream_t s) {
+  k_sub_mean_unless<T><<<grid_of(count, kBlock), kBlock, 0, s>>>(a, count, mean, flag);
+  count_launch();
+}
+
+template <class T>
+__global__ void k_usum_flag(const unsigned long long* acc, int* flag) {
+  T s = (T)fx_to(acc[0], acc[1]);
+  *flag = (s > T(1.e-2)) ? 0 : 1;  // 0: run zerosum, 1: skip (flag semantics of k_sub_mean_unless)
+}
+
+template <class T>
+void launch_usum_flag(const unsigned long long* acc, int* flag, cudaStream_t s) {
+  k_usum_flag<T><<<1, 1, 0, s>>>(acc, flag);
+  count_launch();
+}
+
+#define MMH_INSTANTIATE(T)                                                                                          \
+  template void launch_metric<T>(const T*, const T*, int, T, T*, cudaStream_t);                                   \
+  template void launch_gs_sweeps<T>(T*, const T*, const T*, int, T, int, cudaStream_t);                           \
+  template void launch_residual<T>(const T*, const T*, const T*, int, T, T*, float*, unsigned long long*,          \
+                                   cudaStream_t);                                                                   \
+  template void launch_restrict_resid<T>(const T*, int, int, T*, cudaStream_t);                                   \
+  template void launch_restrict27<T>(const T*, int, T*, cudaStream_t);                                            \
+  template void launch_smooth27<T>(const T*, int, T*, cudaStream_t);                                              \
+  template void launch_prolong_add<T>(T*, const T*, int, cudaStream_t);                                           \
+  template void launch_fxsum<T>(const T*, i64, unsigned long long*, int*, cudaStream_t);                          \
+  template void launch_det<T>(const T*, int, T, T*, cudaStream_t);                                                \
+  template void launch_sub_mean<T>(T*, i64, const double*, cudaStream_t);                                         \
+  template void launch_sub_dfact<T>(T*, const T*, i64, const double*, cudaStream_t);                              \
+  template void launch_fill<T>(T*, i64, T, cudaStream_t);                                                         \
+  template void launch_absmax<T>(const T*, i64, unsigned long long*, cudaStream_t);                               \
+  template void launch_zero_if<T>(T*, i64, const int*, cudaStream_t);                                             \
+  template void launch_sub_mean_unless<T>(T*, i64, const double*, const int*, cudaStream_t);                      \
+  template void launch_usum_flag<T>(const unsigned long long*, int*, cudaStream_t);
+
+}  // namespace mmh

@@ -1,0 +1,973 @@
+// Host side of the MMH library: context, multigrid V-cycles (reference and
+// tolerance schedules, FP64 and mixed precision), calcdefp, relaxing, spectral
+// outputs, and the C ABI declared in include/mmh.h.
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/mmh.h"
+#include "mmh_internal.h"
+#include "mmh_phys.cuh"
+
+using namespace mmh;
+
+namespace {
+
+struct Scal {
+  unsigned long long acc[4][2];  // fixed-point accumulators
+  double mean, ratio;            // zerosum mean, rgzerosum dfact (unrounded)
+  int bad;                       // |x| >= 2^32 or NaN in a sum, or non-zero momentum components
+  int uflag;                     // usum flag (1: skip zerosum)
+  unsigned long long r1bits[16], errbits[16];
+  unsigned long long rhsbits, resbits;
+  int gflag[16];
+  int guards;
+  int pad;
+  LimDev lim;
+};
+
+struct Err {
+  int code = MMH_OK;
+};
+
+#define CK(x)                                                                   \
+  do {                                                                          \
+    cudaError_t e_ = (x);                                                       \
+    if (e_ != cudaSuccess) {                                                    \
+      fprintf(stderr, "mmh: CUDA error %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return MMH_ERR_CUDA;                                                      \
+    }                                                                           \
+  } while (0)
+
+#define CKF(x)                                                                  \
+  do {                                                                          \
+    cufftResult r_ = (x);                                                       \
+    if (r_ != CUFFT_SUCCESS) {                                                  \
+      fprintf(stderr, "mmh: cuFFT error %d at %s:%d\n", (int)r_, __FILE__, __LINE__); \
+      return MMH_ERR_CUDA;                                                      \
+    }                                                                           \
+  } while (0)
+
+#define RET(x)                         \
+  do {                                 \
+    int rc_ = (x);                     \
+    if (rc_ != MMH_OK) return rc_;     \
+  } while (0)
+
+bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+int ilog2(int n) {
+  int l = 0;
+  while ((1 << l) < n) ++l;
+  return l;
+}
+
+// Coarse plane whose own-plane residual part is accumulated first: the size of
+// the last r1lax chunk of relax() (gauss1.f90:134-157).
+int special_plane(int nrelax, int n) {
+  int nrmax = std::min(4, std::max(1, n / 4));
+  if (nrelax > nrmax) {
+    int left = nrelax % nrmax;
+    return left ? left : nrmax;
+  }
+  return nrelax;
+}
+
+template <class T>
+struct Hier {
+  std::vector<T*> u, rhs, coef, r;
+};
+
+}  // namespace
+
+struct mmh_ctx {
+  mmh_config cfg;
+  int n = 0, nlev = 0;
+  i64 n3 = 0;
+  std::vector<int> nl;
+  cudaStream_t s = nullptr;
+  bool own_stream = false;
+  // resident FP64 state
+  double *def = nullptr, *rho = nullptr, *scr = nullptr, *defplim = nullptr, *det = nullptr;
+  // FP64 hierarchy; level 0 u = defp, rhs = tmp
+  Hier<double> h64;
+  std::vector<double*> defl, rhol;
+  // FP32 hierarchy (mixed)
+  Hier<float> h32;
+  // relaxing
+  double *baj = nullptr, *cc = nullptr, *vt = nullptr, *u1 = nullptr;
+  // spectral
+  void *Xc = nullptr, *Z = nullptr;
+  cufftHandle pd2z = 0, pz2z = 0;
+  bool plans = false;
+  Scal* sc = nullptr;   // device
+  Scal* hsc = nullptr;  // pinned host mirror
+  std::vector<void*> allocs;
+  int last_status = MMH_OK;
+
+  double* defp() { return h64.u[0]; }
+  double* tmp() { return h64.rhs[0]; }
+
+  template <class T>
+  int alloc(T** p, i64 count) {
+    void* q = nullptr;
+    if (cudaMalloc(&q, sizeof(T) * (size_t)count) != cudaSuccess) return MMH_ERR_NOMEM;
+    allocs.push_back(q);
+    *p = (T*)q;
+    return MMH_OK;
+  }
+};
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// small building blocks
+// ---------------------------------------------------------------------------
+template <class T>
+int zerosum(mmh_ctx* c, T* a, i64 count) {
+  CK(cudaMemsetAsync(c->sc->acc[0], 0, 16, c->s));
+  launch_fxsum<T>(a, count, c->sc->acc[0], &c->sc->bad, c->s);
+  launch_fx_mean(c->sc->acc[0], (double)count, &c->sc->mean, c->s);
+  launch_sub_mean<T>(a, count, &c->sc->mean, c->s);
+  return MMH_OK;
+}
+
+// rgzerosum(arr, def, dx) at level l (FP64)
+int rgzerosum(mmh_ctx* c, double* arr, const double* def, int n, double dx) {
+  i64 n3 = (i64)n * n * n;
+  launch_det<double>(def, n, dx, c->det, c->s);
+  CK(cudaMemsetAsync(c->sc->acc[0], 0, 32, c->s));
+  launch_fxsum<double>(c->det, n3, c->sc->acc[0], &c->sc->bad, c->s);
+  launch_fxsum<double>(arr, n3, c->sc->acc[1], &c->sc->bad, c->s);
+  launch_fx_ratio(c->sc->acc[1], c->sc->acc[0], &c->sc->ratio, c->s);
+  launch_sub_dfact<double>(arr, c->det, n3, &c->sc->ratio, c->s);
+  return MMH_OK;
+}
+
+// usum + conditional zerosum at the multigrid entry (multigrid.f90:41-46)
+template <class T>
+int usum_zerosum(mmh_ctx* c, T* u, i64 count) {
+  CK(cudaMemsetAsync(c->sc->acc[2], 0, 16, c->s));
+  launch_fxsum<T>(u, count, c->sc->acc[2], &c->sc->bad, c->s);
+  launch_usum_flag<T>(c->sc->acc[2], &c->sc->uflag, c->s);
+  launch_fx_mean(c->sc->acc[2], (double)count, &c->sc->mean, c->s);
+  launch_sub_mean_unless<T>(u, count, &c->sc->mean, &c->sc->uflag, c->s);
+  return MMH_OK;
+}
+
+template <class T>
+Hier<T>& hier(mmh_ctx* c);
+template <>
+Hier<double>& hier<double>(mmh_ctx* c) { return c->h64; }
+template <>
+Hier<float>& hier<float>(mmh_ctx* c) { return c->h32; }
+
+// relax(): nrelax 8-colour sweeps, then residual (mode 3: full weighting into
+// rhs[l+1] and max norm; mode 2: max norm only) into *maxslot.
+template <class T>
+int relax_level(mmh_ctx* c, int l, int nrelax, int mode, unsigned long long* maxslot) {
+  Hier<T>& H = hier<T>(c);
+  int n = c->nl[l];
+  T dx = T(double(1 << l));
+  launch_gs_sweeps<T>(H.u[l], H.rhs[l], H.coef[l], n, dx, nrelax, c->s);
+  CK(cudaMemsetAsync(maxslot, 0, 8, c->s));
+  launch_residual<T>(H.u[l], H.rhs[l], H.coef[l], n, dx, mode == 3 ? H.r[l] : (T*)nullptr, nullptr, maxslot, c->s);
+  if (mode == 3) launch_restrict_resid<T>(H.r[l], n, special_plane(nrelax, n), H.rhs[l + 1], c->s);
+  return MMH_OK;
+}
+
+// post-relaxation step of a level: divergence guard or zerosum
+template <class T>
+int guard_or_zerosum(mmh_ctx* c, int l, double margin, double floor_, bool guard) {
+  Hier<T>& H = hier<T>(c);
+  int n = c->nl[l];
+  i64 n3 = (i64)n * n * n;
+  if (!guard) return zerosum<T>(c, H.u[l], n3);
+  launch_guard(&c->sc->r1bits[l], &c->sc->errbits[l], margin, floor_, &c->sc->gflag[l], &c->sc->guards, c->s);
+  CK(cudaMemsetAsync(c->sc->acc[3], 0, 16, c->s));
+  launch_fxsum<T>(H.u[l], n3, c->sc->acc[3], &c->sc->bad, c->s);
+  launch_fx_mean(c->sc->acc[3], (double)n3, &c->sc->mean, c->s);
+  launch_sub_mean_unless<T>(H.u[l], n3, &c->sc->mean, &c->sc->gflag[l], c->s);
+  launch_zero_if<T>(H.u[l], n3, &c->sc->gflag[l], c->s);
+  return MMH_OK;
+}
+
+int vcycle_fp64(mmh_ctx* c, int l);
+
+// One V-cycle at level l (mgtemplate.f90:6-84; mg4 at multigrid.f90:94-121).
+template <class T>
+int vcycle(mmh_ctx* c, int l) {
+  Hier<T>& H = hier<T>(c);
+  int n = c->nl[l];
+  bool ref = c->cfg.schedule == MMH_SCHED_REF;
+  bool at_ng = (n == c->n);
+  if (n == 4) {
+    if (std::is_same<T, float>::value) {
+      // coarsest grid solved in FP64
+      Hier<float>& F = c->h32;
+      i64 n3 = 64;
+      launch_f2d(F.rhs[l], c->h64.rhs[l], n3, c->s);
+      launch_f2d(F.u[l], c->h64.u[l], n3, c->s);
+      RET(vcycle_fp64(c, l));
+      launch_d2f(c->h64.u[l], F.u[l], n3, c->s);
+      return MMH_OK;
+    }
+    RET(relax_level<T>(c, l, 32, 2, &c->sc->r1bits[l]));
+    RET(relax_level<T>(c, l, 32, 2, &c->sc->errbits[l]));
+    return guard_or_zerosum<T>(c, l, 1.001, 1.e-5, !at_ng);
+  }
+  int nrelax = ref ? 4 * c->n / n : c->cfg.nu1;
+  int nrelax2 = ref ? 4 * c->n / n : c->cfg.nu2;
+  RET(relax_level<T>(c, l, nrelax, 3, &c->sc->r1bits[l]));
+  int nh = c->nl[l + 1];
+  launch_fill<T>(H.u[l + 1], (i64)nh * nh * nh, T(0), c->s);
+  RET(vcycle<T>(c, l + 1));
+  launch_prolong_add<T>(H.u[l], H.u[l + 1], n, c->s);
+  RET(relax_level<T>(c, l, nrelax2, 2, &c->sc->errbits[l]));
+  return guard_or_zerosum<T>(c, l, 1.0, -HUGE_VAL, !at_ng);
+}
+
+int vcycle_fp64(mmh_ctx* c, int l) { return vcycle<double>(c, l); }
+
+double bits_to_double(unsigned long long b) {
+  double d;
+  std::memcpy(&d, &b, 8);
+  return d;
+}
+
+int pull_scal(mmh_ctx* c) {
+  CK(cudaMemcpyAsync(c->hsc, c->sc, sizeof(Scal), cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  return MMH_OK;
+}
+
+// Build the coarse geometry (restricted def and density) and the metric of
+// every level from l0 down (FP64; FP32 copies for the mixed form).
+int build_levels(mmh_ctx* c, int l0) {
+  for (int l = l0 + 1; l < c->nlev; ++l) {
+    launch_restrict27<double>(c->defl[l - 1], c->nl[l - 1], c->defl[l], c->s);
+    launch_restrict27<double>(c->rhol[l - 1], c->nl[l - 1], c->rhol[l], c->s);
+  }
+  for (int l = l0; l < c->nlev; ++l) {
+    int n = c->nl[l];
+    launch_metric<double>(c->defl[l], c->rhol[l], n, double(1 << l), c->h64.coef[l], c->s);
+    if (c->cfg.precision == MMH_MIXED) launch_d2f(c->h64.coef[l], c->h32.coef[l], 6 * (i64)n * n * n, c->s);
+  }
+  return MMH_OK;
+}
+
+// multigrid(u, rhs, defpot, ubig, dx, ...) at level l0: u = h64.u[l0],
+// rhs = h64.rhs[l0], defpot = defl[l0], density = rhol[l0] already in place.
+int multigrid_level(mmh_ctx* c, int l0, double dx, mmh_diag* d) {
+  int n = c->nl[l0];
+  i64 n3 = (i64)n * n * n;
+  CK(cudaMemsetAsync(c->sc, 0, offsetof(Scal, lim), c->s));
+  RET(rgzerosum(c, c->h64.rhs[l0], c->defl[l0], n, dx));
+  RET(usum_zerosum<double>(c, c->h64.u[l0], n3));
+  launch_absmax<double>(c->h64.rhs[l0], n3, &c->sc->rhsbits, c->s);
+  RET(build_levels(c, l0));
+  int cycles = 0;
+  double rn = 0.0, rel = 0.0;
+  int status = MMH_OK;
+  if (c->cfg.schedule == MMH_SCHED_REF) {
+    RET(vcycle<double>(c, l0));
+    cycles = 1;
+    RET(pull_scal(c));
+    rn = bits_to_double(c->hsc->rhsbits);
+    rel = rn > 0 ? bits_to_double(c->hsc->errbits[l0]) / rn : 0.0;
+  } else if (c->cfg.precision == MMH_FP64) {
+    RET(pull_scal(c));
+    rn = bits_to_double(c->hsc->rhsbits);
+    if (rn > 0) {
+      for (cycles = 0; cycles < c->cfg.max_cycles;) {
+        RET(vcycle<double>(c, l0));
+        cycles++;
+        RET(pull_scal(c));
+        rel = bits_to_double(c->hsc->errbits[l0]) / rn;
+        if (!(rel == rel)) break;
+        if (rel <= c->cfg.tol) break;
+      }
+      if (rel > c->cfg.tol && rel == rel) status = MMH_ERR_DIVERGED;
+    }
+  } else {
+    // mixed: FP64 residual / FP32 V-cycle defect correction
+    RET(pull_scal(c));
+    rn = bits_to_double(c->hsc->rhsbits);
+    Hier<float>& F = c->h32;
+    if (rn > 0) {
+      for (cycles = 0;; ) {
+        CK(cudaMemsetAsync(&c->sc->resbits, 0, 8, c->s));
+        launch_residual<double>(c->h64.u[l0], c->h64.rhs[l0], c->h64.coef[l0], n, dx, nullptr, F.rhs[l0],
+                                &c->sc->resbits, c->s);
+        RET(pull_scal(c));
+        rel = bits_to_double(c->hsc->resbits) / rn;
+        if (!(rel == rel) || rel <= c->cfg.tol) break;
+        if (cycles >= c->cfg.max_cycles) {
+          status = MMH_ERR_DIVERGED;
+          break;
+        }
+        launch_fill<float>(F.u[l0], n3, 0.0f, c->s);
+        RET(vcycle<float>(c, l0));
+        launch_add_f2d(c->h64.u[l0], F.u[l0], n3, c->s);
+        RET(zerosum<double>(c, c->h64.u[l0], n3));
+        cycles++;
+      }
+    }
+  }
+  RET(pull_scal(c));
+  if (!(rel == rel)) status = MMH_ERR_NAN;
+  if (c->hsc->bad) status = MMH_ERR_RANGE;
+  if (d) {
+    d->r1 = bits_to_double(c->hsc->r1bits[l0]);
+    d->relaxerr = bits_to_double(c->hsc->errbits[l0]);
+    d->rhsnorm = rn;
+    d->resid_rel = rel;
+    d->vcycles = cycles;
+    d->guards = c->hsc->guards;
+    d->status = status;
+  }
+  return status;
+}
+
+double ord_to_double(unsigned long long u) {
+  unsigned long long b = (u >> 63) ? (u & 0x7fffffffffffffffull) : ~u;
+  return bits_to_double(b);
+}
+
+double fx_host(const unsigned long long* acc) {
+  __int128 s = (__int128)(((unsigned __int128)acc[1] << 64) | (unsigned __int128)acc[0]);
+  bool neg = s < 0;
+  unsigned __int128 a = neg ? (unsigned __int128)(-s) : (unsigned __int128)s;
+  double r = (double)(unsigned long long)(a >> 64) + (double)(unsigned long long)a * 5.42101086242752217e-20;
+  return neg ? -r : r;
+}
+
+void lim_to_diag(const LimDev& L, mmh_diag* d) {
+  if (!d) return;
+  d->nexpand = (long long)L.nexpand;
+  d->ncompress = (long long)L.ncompress;
+  d->cmax = ord_to_double(L.cmax);
+  d->detmin = ord_to_double(L.detmin);
+  d->detmax = ord_to_double(L.detmax);
+  d->fluxmax = ord_to_double(L.fluxmax);
+  d->fluxmin = ord_to_double(L.fluxmin);
+  d->rho2 = fx_host(L.rho2);
+}
+
+int make_plans(mmh_ctx* c) {
+  if (c->plans) return MMH_OK;
+  int n = c->n;
+  CKF(cufftPlan3d(&c->pd2z, n, n, n, CUFFT_D2Z));
+  CKF(cufftPlan3d(&c->pz2z, n, n, n / 2, CUFFT_Z2Z));
+  CKF(cufftSetStream(c->pd2z, c->s));
+  CKF(cufftSetStream(c->pz2z, c->s));
+  c->plans = true;
+  return MMH_OK;
+}
+
+// FFT Poisson correction: defp += F^-1[F[defplim]/akernel] * 2/n^3, skipped on
+// the device when no cell was limited (limiter.f90:535-597).
+int limiter_poisson(mmh_ctx* c, double* defp, const double* defplim) {
+  RET(make_plans(c));
+  CKF(cufftExecD2Z(c->pd2z, (cufftDoubleReal*)defplim, (cufftDoubleComplex*)c->Xc));
+  launch_spec_pack(c->Xc, c->n, 4, c->Z, &c->sc->lim, c->s);
+  CKF(cufftExecZ2Z(c->pz2z, (cufftDoubleComplex*)c->Z, (cufftDoubleComplex*)c->Z, CUFFT_FORWARD));
+  launch_spec_unpack(c->Z, c->n, defp, 1, 1, &c->sc->lim, c->s);
+  return MMH_OK;
+}
+
+// calcdefp on the resident state: defp (= h64.u[0]) from def and rho.
+int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t* mc1, uint8_t* mc2, mmh_diag* d) {
+  int n = c->n;
+  i64 n3 = c->n3;
+  if (dtold < 1.e-8) dtold = 1.0;
+  double* tmp = c->tmp();
+  double* defp = c->defp();
+  launch_calcdefp_rhs(tmp, c->rho, n, dtold, c->s);
+  launch_smooth27<double>(tmp, n, c->scr, c->s);
+  launch_smooth27<double>(c->scr, n, tmp, c->s);
+  launch_smooth27<double>(tmp, n, c->scr, c->s);
+  launch_lim_reset(&c->sc->lim, c->s);
+  launch_limiter_pass1(c->scr, c->def, c->rho, n, dtold, dtaumesh, &c->sc->lim, mx, mc1, c->s);
+  launch_smooth27<double>(c->scr, n, tmp, c->s);
+  launch_fill<double>(defp, n3, 0.0, c->s);
+  int st = multigrid_level(c, 0, 1.0, d);
+  if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
+  launch_smooth27<double>(defp, n, c->scr, c->s);
+  launch_smooth27<double>(c->scr, n, defp, c->s);
+  launch_limiter_mask(c->defplim, c->def, defp, n, dtold, &c->sc->lim, mc2, c->s);
+  RET(limiter_poisson(c, defp, c->defplim));
+  RET(pull_scal(c));
+  lim_to_diag(c->hsc->lim, d);
+  if (c->hsc->lim.flag) st = MMH_ERR_RANGE;
+  return st;
+}
+
+// relaxing(u, def, defp, cmax, dt, 5) on the resident density.
+int relaxing_dev(mmh_ctx* c, double dt) {
+  int n = c->n;
+  launch_relax_stage1(c->rho, c->def, c->defp(), n, c->baj, c->cc, c->vt, c->s);
+  launch_relax_dpv(c->rho, c->vt, c->cc, n, c->rho, dt / 2.0, c->u1, c->s);
+  launch_relax_flux(c->u1, c->defp(), c->baj, n, c->vt, c->s);
+  launch_relax_dpv(c->u1, c->vt, c->cc, n, c->rho, dt, c->rho, c->s);
+  return MMH_OK;
+}
+
+// spectral outputs of src into host/device buffers (grad: 3 planes of n^3)
+int spectral_outputs(mmh_ctx* c, const double* src, double* d_grad, double* d_delta) {
+  RET(make_plans(c));
+  CKF(cufftExecD2Z(c->pd2z, (cufftDoubleReal*)src, (cufftDoubleComplex*)c->Xc));
+  for (int ax = 0; ax < 3 && d_grad; ++ax) {
+    launch_spec_pack(c->Xc, c->n, ax, c->Z, &c->sc->lim, c->s);
+    CKF(cufftExecZ2Z(c->pz2z, (cufftDoubleComplex*)c->Z, (cufftDoubleComplex*)c->Z, CUFFT_FORWARD));
+    launch_spec_unpack(c->Z, c->n, d_grad + ax * c->n3, 1, 0, &c->sc->lim, c->s);
+  }
+  if (d_delta) {
+    launch_spec_pack(c->Xc, c->n, 3, c->Z, &c->sc->lim, c->s);
+    CKF(cufftExecZ2Z(c->pz2z, (cufftDoubleComplex*)c->Z, (cufftDoubleComplex*)c->Z, CUFFT_FORWARD));
+    launch_spec_unpack(c->Z, c->n, d_delta, 1, 0, &c->sc->lim, c->s);
+  }
+  return MMH_OK;
+}
+
+int check_cube(mmh_ctx* c, int nx, int ny, int nz) {
+  if (nx != ny || ny != nz) return MMH_ERR_SIZE;
+  if (!is_pow2(nx)) return MMH_ERR_NOTPOW2;
+  if (nx < 4 || nx > c->n) return MMH_ERR_SIZE;
+  return MMH_OK;
+}
+
+// host <-> device helpers with element conversion
+template <class H>
+int upload(mmh_ctx* c, const H* src, double* dst, i64 count) {
+  if (std::is_same<H, double>::value) {
+    CK(cudaMemcpyAsync(dst, src, sizeof(double) * count, cudaMemcpyHostToDevice, c->s));
+  } else {
+    float* tmpf = nullptr;
+    CK(cudaMallocAsync((void**)&tmpf, sizeof(float) * count, c->s));
+    CK(cudaMemcpyAsync(tmpf, src, sizeof(float) * count, cudaMemcpyHostToDevice, c->s));
+    launch_f2d(tmpf, dst, count, c->s);
+    CK(cudaFreeAsync(tmpf, c->s));
+  }
+  return MMH_OK;
+}
+template <class H>
+int download(mmh_ctx* c, const double* src, H* dst, i64 count) {
+  if (std::is_same<H, double>::value) {
+    CK(cudaMemcpyAsync(dst, src, sizeof(double) * count, cudaMemcpyDeviceToHost, c->s));
+  } else {
+    float* tmpf = nullptr;
+    CK(cudaMallocAsync((void**)&tmpf, sizeof(float) * count, c->s));
+    launch_d2f(src, tmpf, count, c->s);
+    CK(cudaMemcpyAsync(dst, tmpf, sizeof(float) * count, cudaMemcpyDeviceToHost, c->s));
+    CK(cudaFreeAsync(tmpf, c->s));
+  }
+  CK(cudaStreamSynchronize(c->s));
+  return MMH_OK;
+}
+
+// density of u(nf,n^3) into dst; MMH_ERR_UNSUPPORTED if u(2:nf) is not zero
+template <class H>
+int upload_density(mmh_ctx* c, const H* u, int nf, i64 n3, double* dst) {
+  if (nf < 1 || nf > 5) return MMH_ERR_ARG;
+  H* tmpu = nullptr;
+  CK(cudaMallocAsync((void**)&tmpu, sizeof(H) * n3 * nf, c->s));
+  CK(cudaMemcpyAsync(tmpu, u, sizeof(H) * n3 * nf, cudaMemcpyHostToDevice, c->s));
+  CK(cudaMemsetAsync(&c->sc->bad, 0, sizeof(int), c->s));
+  if (std::is_same<H, double>::value)
+    launch_extract_density_d((const double*)tmpu, nf, n3, dst, &c->sc->bad, c->s);
+  else
+    launch_extract_density_f((const float*)tmpu, nf, n3, dst, &c->sc->bad, c->s);
+  CK(cudaFreeAsync(tmpu, c->s));
+  RET(pull_scal(c));
+  if (c->hsc->bad) return MMH_ERR_UNSUPPORTED;
+  return MMH_OK;
+}
+
+// write the density back into component 1 of the host u(nf,n^3)
+template <class H>
+int download_density(mmh_ctx* c, const double* rho, H* u, int nf, i64 n3) {
+  std::vector<H> tmp(n3);
+  RET(download(c, rho, tmp.data(), n3));
+  for (i64 q = 0; q < n3; ++q) u[q * nf] = tmp[q];
+  return MMH_OK;
+}
+
+template <class H>
+int calcdefp_host(mmh_ctx* c, H* defp, H* tmp, H* tmp2, const H* def, const H* u, double dtold, double dtaumesh,
+                  int nfluid, mmh_diag* d) {
+  (void)tmp2;
+  if (!c || !defp || !def || !u) return MMH_ERR_ARG;
+  RET(upload(c, def, c->def, c->n3));
+  RET(upload_density(c, u, nfluid, c->n3, c->rho));
+  mmh_diag dd{};
+  int st = calcdefp_dev(c, dtold, dtaumesh, nullptr, nullptr, nullptr, &dd);
+  if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
+  RET(download(c, c->defp(), defp, c->n3));
+  if (tmp) {
+    // tmp is scratch in the reference; it returns rho2, xlum, temp in its first
+    // three elements and the (inert) cold-region marker 1 elsewhere.
+    for (i64 q = 0; q < c->n3; ++q) tmp[q] = H(1);
+    tmp[0] = H(dd.rho2);
+    if (c->n3 > 2) { tmp[1] = H(0); tmp[2] = H(0); }
+  }
+  dd.status = st;
+  if (d) *d = dd;
+  return st;
+}
+
+template <class H>
+int multigrid_host(mmh_ctx* c, H* u, H* rhs, const H* defpot, const H* ubig, double dx, int nx, int ny, int nz, int nu,
+                   int nred, int iopt, mmh_diag* d) {
+  if (!c || !u || !rhs || !defpot || !ubig) return MMH_ERR_ARG;
+  RET(check_cube(c, nx, ny, nz));
+  if (nred != 1 || iopt != 2) return MMH_ERR_ARG;
+  int l0 = ilog2(c->n / nx);
+  i64 n3 = (i64)nx * nx * nx;
+  RET(upload(c, u, c->h64.u[l0], n3));
+  RET(upload(c, rhs, c->h64.rhs[l0], n3));
+  RET(upload(c, defpot, c->defl[l0], n3));
+  RET(upload_density(c, ubig, nu, n3, c->rhol[l0]));
+  mmh_diag dd{};
+  int st = multigrid_level(c, l0, dx, &dd);
+  if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
+  RET(download(c, c->h64.u[l0], u, n3));
+  RET(download(c, c->h64.rhs[l0], rhs, n3));
+  if (d) *d = dd;
+  return st;
+}
+
+template <class H>
+int relaxing_host(mmh_ctx* c, H* u, const H* def, const H* defp, double dt, int nf) {
+  if (!c || !u || !def || !defp) return MMH_ERR_ARG;
+  RET(upload(c, def, c->def, c->n3));
+  RET(upload(c, defp, c->defp(), c->n3));
+  RET(upload_density(c, u, nf, c->n3, c->rho));
+  RET(relaxing_dev(c, dt));
+  RET(download_density(c, c->rho, u, nf, c->n3));
+  return MMH_OK;
+}
+
+template <class H>
+int spectral_host(mmh_ctx* c, const H* in, H* out, const int* nn, bool grad) {
+  if (!c || !in || !out || !nn) return MMH_ERR_ARG;
+  if (nn[0] != c->n || nn[1] != c->n || nn[2] != c->n) return MMH_ERR_SIZE;
+  RET(upload(c, in, c->scr, c->n3));
+  double* o = nullptr;
+  CK(cudaMallocAsync((void**)&o, sizeof(double) * c->n3 * (grad ? 3 : 1), c->s));
+  int st = spectral_outputs(c, c->scr, grad ? o : nullptr, grad ? nullptr : o);
+  if (st == MMH_OK) st = download(c, o, out, c->n3 * (grad ? 3 : 1));
+  cudaFreeAsync(o, c->s);
+  return st;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+void mmh_config_default(mmh_config* cfg, int n) {
+  if (!cfg) return;
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->n = n;
+  cfg->precision = MMH_FP64;
+  cfg->schedule = MMH_SCHED_REF;
+  cfg->nu1 = 2;
+  cfg->nu2 = 2;
+  cfg->max_cycles = 200;
+  cfg->tol = 1e-10;
+  cfg->device = 0;
+  cfg->stream = nullptr;
+}
+
+const char* mmh_strerror(int code) {
+  switch (code) {
+    case MMH_OK: return "ok";
+    case MMH_ERR_ARG: return "invalid argument";
+    case MMH_ERR_SIZE: return "grid must be a cube no larger than the context size";
+    case MMH_ERR_NOTPOW2: return "grid size must be a power of two";
+    case MMH_ERR_CUDA: return "CUDA or cuFFT failure";
+    case MMH_ERR_NAN: return "NaN or Inf in a residual";
+    case MMH_ERR_DIVERGED: return "tolerance not reached within max_cycles";
+    case MMH_ERR_UNSUPPORTED: return "unsupported input (nonzero momentum/energy components)";
+    case MMH_ERR_RANGE: return "value outside the exact-sum range";
+    case MMH_ERR_NOMEM: return "device allocation failed";
+    default: return "unknown error";
+  }
+}
+
+unsigned long long mmh_launch_count(void) { return mmh::launch_count(); }
+
+int mmh_destroy(mmh_ctx* c) {
+  if (!c) return MMH_OK;
+  if (c->s) cudaStreamSynchronize(c->s);
+  if (c->plans) {
+    cufftDestroy(c->pd2z);
+    cufftDestroy(c->pz2z);
+  }
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->hsc) cudaFreeHost(c->hsc);
+  if (c->own_stream && c->s) cudaStreamDestroy(c->s);
+  delete c;
+  return MMH_OK;
+}
+
+int mmh_create(mmh_ctx** out, const mmh_config* cfg) {
+  if (!out || !cfg) return MMH_ERR_ARG;
+  *out = nullptr;
+  int n = cfg->n;
+  if (!is_pow2(n)) return MMH_ERR_NOTPOW2;
+  if (n < 8 || n > 1024) return MMH_ERR_SIZE;
+  if (cfg->precision != MMH_FP64 && cfg->precision != MMH_MIXED) return MMH_ERR_ARG;
+  if (cfg->schedule != MMH_SCHED_REF && cfg->schedule != MMH_SCHED_TOL) return MMH_ERR_ARG;
+  if (cfg->precision == MMH_MIXED && cfg->schedule != MMH_SCHED_TOL) return MMH_ERR_ARG;
+  if (cfg->schedule == MMH_SCHED_TOL && (cfg->nu1 < 1 || cfg->nu2 < 1 || cfg->max_cycles < 1)) return MMH_ERR_ARG;
+  if (cudaSetDevice(cfg->device) != cudaSuccess) return MMH_ERR_CUDA;
+  mmh_ctx* c = new (std::nothrow) mmh_ctx();
+  if (!c) return MMH_ERR_NOMEM;
+  c->cfg = *cfg;
+  c->n = n;
+  c->n3 = (i64)n * n * n;
+  for (int m = n; m >= 4; m >>= 1) c->nl.push_back(m);
+  c->nlev = (int)c->nl.size();
+  if (cfg->stream) {
+    c->s = (cudaStream_t)cfg->stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess) {
+      delete c;
+      return MMH_ERR_CUDA;
+    }
+    c->own_stream = true;
+  }
+  int rc = MMH_OK;
+  auto A = [&](auto** p, i64 count) {
+    if (rc == MMH_OK) rc = c->alloc(p, count);
+  };
+  i64 n3 = c->n3;
+  A(&c->def, n3);
+  A(&c->rho, n3);
+  A(&c->scr, n3);
+  A(&c->defplim, n3);
+  A(&c->det, n3);
+  c->h64.u.resize(c->nlev);
+  c->h64.rhs.resize(c->nlev);
+  c->h64.coef.resize(c->nlev);
+  c->h64.r.resize(c->nlev);
+  c->defl.resize(c->nlev);
+  c->rhol.resize(c->nlev);
+  for (int l = 0; l < c->nlev; ++l) {
+    i64 m3 = (i64)c->nl[l] * c->nl[l] * c->nl[l];
+    A(&c->h64.u[l], m3);
+    A(&c->h64.rhs[l], m3);
+    A(&c->h64.coef[l], 6 * m3);
+    A(&c->h64.r[l], m3);
+    if (l == 0) {
+      c->defl[0] = c->def;
+      c->rhol[0] = c->rho;
+    } else {
+      A(&c->defl[l], m3);
+      A(&c->rhol[l], m3);
+    }
+  }
+  if (cfg->precision == MMH_MIXED) {
+    c->h32.u.resize(c->nlev);
+    c->h32.rhs.resize(c->nlev);
+    c->h32.coef.resize(c->nlev);
+    c->h32.r.resize(c->nlev);
+    for (int l = 0; l < c->nlev; ++l) {
+      i64 m3 = (i64)c->nl[l] * c->nl[l] * c->nl[l];
+      A(&c->h32.u[l], m3);
+      A(&c->h32.rhs[l], m3);
+      A(&c->h32.coef[l], 6 * m3);
+      A(&c->h32.r[l], m3);
+    }
+  }
+  A(&c->baj, 7 * n3);
+  A(&c->cc, n3);
+  A(&c->vt, 3 * n3);
+  A(&c->u1, n3);
+  A((double**)&c->Xc, 2 * (i64)(n / 2 + 1) * n * n);
+  A((double**)&c->Z, 2 * (i64)(n / 2) * n * n);
+  A(&c->sc, 1);
+  if (rc == MMH_OK && cudaMallocHost((void**)&c->hsc, sizeof(Scal)) != cudaSuccess) rc = MMH_ERR_NOMEM;
+  if (rc == MMH_OK && cudaMemsetAsync(c->sc, 0, sizeof(Scal), c->s) != cudaSuccess) rc = MMH_ERR_CUDA;
+  if (rc == MMH_OK) {
+    for (int l = 0; l < c->nlev && rc == MMH_OK; ++l) {
+      i64 m3 = (i64)c->nl[l] * c->nl[l] * c->nl[l];
+      if (cudaMemsetAsync(c->h64.u[l], 0, sizeof(double) * m3, c->s) != cudaSuccess) rc = MMH_ERR_CUDA;
+    }
+    if (cudaMemsetAsync(c->def, 0, sizeof(double) * n3, c->s) != cudaSuccess) rc = MMH_ERR_CUDA;
+  }
+  if (rc == MMH_OK && cudaStreamSynchronize(c->s) != cudaSuccess) rc = MMH_ERR_CUDA;
+  if (rc != MMH_OK) {
+    mmh_destroy(c);
+    return rc;
+  }
+  *out = c;
+  return MMH_OK;
+}
+
+int mmh_sync(mmh_ctx* c) {
+  if (!c) return MMH_ERR_ARG;
+  CK(cudaStreamSynchronize(c->s));
+  CK(cudaGetLastError());
+  return MMH_OK;
+}
+
+int mmh_calcdefp(mmh_ctx* c, float* defp, float* tmp, float* tmp2, const float* def, const float* u, float dtold1,
+                 float dtaumesh, int nfluid, mmh_diag* d) {
+  return calcdefp_host<float>(c, defp, tmp, tmp2, def, u, dtold1, dtaumesh, nfluid, d);
+}
+int mmh_calcdefp_f64(mmh_ctx* c, double* defp, double* tmp, double* tmp2, const double* def, const double* u,
+                     double dtold1, double dtaumesh, int nfluid, mmh_diag* d) {
+  return calcdefp_host<double>(c, defp, tmp, tmp2, def, u, dtold1, dtaumesh, nfluid, d);
+}
+int mmh_multigrid(mmh_ctx* c, float* u, float* rhs, const float* defpot, const float* ubig, float dx, int nx, int ny,
+                  int nz, int nu, int nred, int iopt, mmh_diag* d) {
+  return multigrid_host<float>(c, u, rhs, defpot, ubig, dx, nx, ny, nz, nu, nred, iopt, d);
+}
+int mmh_multigrid_f64(mmh_ctx* c, double* u, double* rhs, const double* defpot, const double* ubig, double dx, int nx,
+                      int ny, int nz, int nu, int nred, int iopt, mmh_diag* d) {
+  return multigrid_host<double>(c, u, rhs, defpot, ubig, dx, nx, ny, nz, nu, nred, iopt, d);
+}
+int mmh_relaxing(mmh_ctx* c, float* u, const float* def, const float* defp, float cmax, float dt, int nfluidcmp) {
+  (void)cmax;
+  return relaxing_host<float>(c, u, def, defp, dt, nfluidcmp);
+}
+int mmh_relaxing_f64(mmh_ctx* c, double* u, const double* def, const double* defp, double cmax, double dt,
+                     int nfluidcmp) {
+  (void)cmax;
+  return relaxing_host<double>(c, u, def, defp, dt, nfluidcmp);
+}
+int mmh_scalar2gradient(mmh_ctx* c, const float* in, float* out, const int* nn) {
+  return spectral_host<float>(c, in, out, nn, true);
+}
+int mmh_scalar2gradient_f64(mmh_ctx* c, const double* in, double* out, const int* nn) {
+  return spectral_host<double>(c, in, out, nn, true);
+}
+int mmh_defp2delta(mmh_ctx* c, const float* in, float* out, const int* nn) {
+  return spectral_host<float>(c, in, out, nn, false);
+}
+int mmh_defp2delta_f64(mmh_ctx* c, const double* in, double* out, const int* nn) {
+  return spectral_host<double>(c, in, out, nn, false);
+}
+
+int mmh_relax_f64(mmh_ctx* c, double* arr, double* resid, const double* rhs, const double* deformpot,
+                  const double* rho, double* rinf, double dx, int n, int nrelax, int iopt) {
+  if (!c || !arr || !rhs || !deformpot || !rho || !rinf) return MMH_ERR_ARG;
+  RET(check_cube(c, n, n, n));
+  int ir = iopt % 8;
+  if (iopt < 0 || iopt > 256 || (iopt / 8) % 8 != 2 || nrelax < 0) return MMH_ERR_ARG;
+  if ((ir == 1 || ir == 3) && (!resid || n < 8)) return MMH_ERR_ARG;
+  if (ir != 0 && ir != 2 && ir != 3) return MMH_ERR_ARG;
+  int l = ilog2(c->n / n);
+  i64 n3 = (i64)n * n * n;
+  RET(upload(c, arr, c->h64.u[l], n3));
+  RET(upload(c, rhs, c->h64.rhs[l], n3));
+  RET(upload(c, deformpot, c->defl[l], n3));
+  RET(upload(c, rho, c->rhol[l], n3));
+  launch_metric<double>(c->defl[l], c->rhol[l], n, dx, c->h64.coef[l], c->s);
+  launch_gs_sweeps<double>(c->h64.u[l], c->h64.rhs[l], c->h64.coef[l], n, dx, nrelax, c->s);
+  CK(cudaMemsetAsync(c->sc->errbits, 0, 8, c->s));
+  if (ir != 0) {
+    launch_residual<double>(c->h64.u[l], c->h64.rhs[l], c->h64.coef[l], n, dx, ir == 3 ? c->h64.r[l] : nullptr,
+                            nullptr, c->sc->errbits, c->s);
+    if (ir == 3) launch_restrict_resid<double>(c->h64.r[l], n, special_plane(nrelax, n), c->scr, c->s);
+  }
+  RET(pull_scal(c));
+  *rinf = ir >= 2 ? bits_to_double(c->hsc->errbits[0]) : 0.0;
+  RET(download(c, c->h64.u[l], arr, n3));
+  if (ir == 3) RET(download(c, c->scr, resid, n3 / 8));
+  return MMH_OK;
+}
+
+int mmh_metric_f64(mmh_ctx* c, const double* deformpot, const double* rho, double dx, int n, double* coef) {
+  if (!c || !deformpot || !rho || !coef) return MMH_ERR_ARG;
+  RET(check_cube(c, n, n, n));
+  int l = ilog2(c->n / n);
+  i64 n3 = (i64)n * n * n;
+  RET(upload(c, deformpot, c->defl[l], n3));
+  RET(upload(c, rho, c->rhol[l], n3));
+  launch_metric<double>(c->defl[l], c->rhol[l], n, dx, c->h64.coef[l], c->s);
+  return download(c, c->h64.coef[l], coef, 6 * n3);
+}
+
+int mmh_restrict_f64(mmh_ctx* c, const double* u, int n, double* uhalf) {
+  if (!c || !u || !uhalf) return MMH_ERR_ARG;
+  RET(check_cube(c, n, n, n));
+  if (n < 8) return MMH_ERR_SIZE;
+  i64 n3 = (i64)n * n * n;
+  RET(upload(c, u, c->scr, n3));
+  launch_restrict27<double>(c->scr, n, c->det, c->s);
+  return download(c, c->det, uhalf, n3 / 8);
+}
+
+int mmh_inject_f64(mmh_ctx* c, double* u, const double* uhalf, int n) {
+  if (!c || !u || !uhalf) return MMH_ERR_ARG;
+  RET(check_cube(c, n, n, n));
+  if (n < 8) return MMH_ERR_SIZE;
+  i64 n3 = (i64)n * n * n;
+  RET(upload(c, u, c->scr, n3));
+  RET(upload(c, uhalf, c->det, n3 / 8));
+  launch_prolong_add<double>(c->scr, c->det, n, c->s);
+  return download(c, c->scr, u, n3);
+}
+
+int mmh_zerosum_f64(mmh_ctx* c, double* arr, int n) {
+  if (!c || !arr) return MMH_ERR_ARG;
+  RET(check_cube(c, n, n, n));
+  i64 n3 = (i64)n * n * n;
+  RET(upload(c, arr, c->scr, n3));
+  CK(cudaMemsetAsync(&c->sc->bad, 0, sizeof(int), c->s));
+  RET(zerosum<double>(c, c->scr, n3));
+  RET(download(c, c->scr, arr, n3));
+  RET(pull_scal(c));
+  return c->hsc->bad ? MMH_ERR_RANGE : MMH_OK;
+}
+
+int mmh_rgzerosum_f64(mmh_ctx* c, double* arr, const double* def, double dx, int n) {
+  if (!c || !arr || !def) return MMH_ERR_ARG;
+  RET(check_cube(c, n, n, n));
+  i64 n3 = (i64)n * n * n;
+  int l = ilog2(c->n / n);
+  RET(upload(c, arr, c->scr, n3));
+  RET(upload(c, def, c->defl[l], n3));
+  CK(cudaMemsetAsync(&c->sc->bad, 0, sizeof(int), c->s));
+  RET(rgzerosum(c, c->scr, c->defl[l], n, dx));
+  RET(download(c, c->scr, arr, n3));
+  RET(pull_scal(c));
+  return c->hsc->bad ? MMH_ERR_RANGE : MMH_OK;
+}
+
+int mmh_nsmooth_f64(mmh_ctx* c, double* a, int n) {
+  if (!c || !a) return MMH_ERR_ARG;
+  RET(check_cube(c, n, n, n));
+  i64 n3 = (i64)n * n * n;
+  RET(upload(c, a, c->scr, n3));
+  launch_smooth27<double>(c->scr, n, c->det, c->s);
+  return download(c, c->det, a, n3);
+}
+
+int mmh_limiter_pass1_f64(mmh_ctx* c, double* tmp, const double* def, const double* rho, int n, double dtold,
+                          double dtaumesh, unsigned char* maskx, unsigned char* maskc, mmh_diag* d) {
+  if (!c || !tmp || !def || !rho) return MMH_ERR_ARG;
+  if (n != c->n) return MMH_ERR_SIZE;
+  i64 n3 = c->n3;
+  RET(upload(c, tmp, c->scr, n3));
+  RET(upload(c, def, c->def, n3));
+  RET(upload(c, rho, c->rho, n3));
+  uint8_t* dm = nullptr;
+  CK(cudaMallocAsync((void**)&dm, 2 * n3, c->s));
+  launch_lim_reset(&c->sc->lim, c->s);
+  launch_limiter_pass1(c->scr, c->def, c->rho, n, dtold, dtaumesh, &c->sc->lim, dm, dm + n3, c->s);
+  RET(download(c, c->scr, tmp, n3));
+  if (maskx) CK(cudaMemcpyAsync(maskx, dm, n3, cudaMemcpyDeviceToHost, c->s));
+  if (maskc) CK(cudaMemcpyAsync(maskc, dm + n3, n3, cudaMemcpyDeviceToHost, c->s));
+  CK(cudaFreeAsync(dm, c->s));
+  RET(pull_scal(c));
+  lim_to_diag(c->hsc->lim, d);
+  return c->hsc->lim.flag ? MMH_ERR_RANGE : MMH_OK;
+}
+
+int mmh_limiter_mask_f64(mmh_ctx* c, double* defplim, const double* def, const double* defp, int n, double dtold,
+                         unsigned char* mask, mmh_diag* d) {
+  if (!c || !defplim || !def || !defp) return MMH_ERR_ARG;
+  if (n != c->n) return MMH_ERR_SIZE;
+  i64 n3 = c->n3;
+  RET(upload(c, def, c->def, n3));
+  RET(upload(c, defp, c->scr, n3));
+  uint8_t* dm = nullptr;
+  CK(cudaMallocAsync((void**)&dm, n3, c->s));
+  launch_lim_reset(&c->sc->lim, c->s);
+  launch_limiter_mask(c->defplim, c->def, c->scr, n, dtold, &c->sc->lim, dm, c->s);
+  RET(download(c, c->defplim, defplim, n3));
+  if (mask) CK(cudaMemcpyAsync(mask, dm, n3, cudaMemcpyDeviceToHost, c->s));
+  CK(cudaFreeAsync(dm, c->s));
+  RET(pull_scal(c));
+  lim_to_diag(c->hsc->lim, d);
+  return MMH_OK;
+}
+
+int mmh_limiter_poisson_f64(mmh_ctx* c, double* defp, const double* defplim, int n) {
+  if (!c || !defp || !defplim) return MMH_ERR_ARG;
+  if (n != c->n) return MMH_ERR_SIZE;
+  i64 n3 = c->n3;
+  RET(upload(c, defp, c->scr, n3));
+  RET(upload(c, defplim, c->defplim, n3));
+  // force the correction on: the caller asks for it explicitly
+  launch_lim_reset(&c->sc->lim, c->s);
+  unsigned long long one = 1;
+  CK(cudaMemcpyAsync(&c->sc->lim.ncompress, &one, sizeof(one), cudaMemcpyHostToDevice, c->s));
+  RET(limiter_poisson(c, c->scr, c->defplim));
+  return download(c, c->scr, defp, n3);
+}
+
+int mmh_load_f64(mmh_ctx* c, const double* def, const double* u, int nfluid) {
+  if (!c || !u) return MMH_ERR_ARG;
+  if (def) RET(upload(c, def, c->def, c->n3));
+  else CK(cudaMemsetAsync(c->def, 0, sizeof(double) * c->n3, c->s));
+  return upload_density(c, u, nfluid, c->n3, c->rho);
+}
+
+int mmh_load_dev(mmh_ctx* c, const double* d_def, const double* d_rho) {
+  if (!c || !d_rho) return MMH_ERR_ARG;
+  if (d_def) CK(cudaMemcpyAsync(c->def, d_def, sizeof(double) * c->n3, cudaMemcpyDeviceToDevice, c->s));
+  else CK(cudaMemsetAsync(c->def, 0, sizeof(double) * c->n3, c->s));
+  CK(cudaMemcpyAsync(c->rho, d_rho, sizeof(double) * c->n3, cudaMemcpyDeviceToDevice, c->s));
+  return MMH_OK;
+}
+
+int mmh_iterate(mmh_ctx* c, int niter, mmh_diag* d) {
+  if (!c || niter < 0) return MMH_ERR_ARG;
+  int st = MMH_OK;
+  for (int it = 0; it < niter; ++it) {
+    mmh_diag dd{};
+    st = calcdefp_dev(c, 1.0, 1.0, nullptr, nullptr, nullptr, &dd);
+    if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
+    launch_add(c->def, c->defp(), c->n3, c->s);
+    RET(relaxing_dev(c, 1.0));
+    dd.status = st;
+    if (d) *d = dd;
+  }
+  CK(cudaStreamSynchronize(c->s));
+  CK(cudaGetLastError());
+  return st;
+}
+
+int mmh_store_f64(mmh_ctx* c, double* def, double* u, int nfluid) {
+  if (!c) return MMH_ERR_ARG;
+  if (def) RET(download(c, c->def, def, c->n3));
+  if (u) {
+    if (nfluid < 1 || nfluid > 5) return MMH_ERR_ARG;
+    RET(download_density(c, c->rho, u, nfluid, c->n3));
+  }
+  return MMH_OK;
+}
+
+int mmh_outputs_f64(mmh_ctx* c, double* grad, double* delta) {
+  if (!c) return MMH_ERR_ARG;
+  double* o = nullptr;
+  CK(cudaMallocAsync((void**)&o, sizeof(double) * c->n3 * 4, c->s));
+  int st = spectral_outputs(c, c->def, grad ? o : nullptr, delta ? o + 3 * c->n3 : nullptr);
+  if (st == MMH_OK && grad) st = download(c, o, grad, 3 * c->n3);
+  if (st == MMH_OK && delta) st = download(c, o + 3 * c->n3, delta, c->n3);
+  cudaFreeAsync(o, c->s);
+  return st;
+}
+
+int mmh_state_dev(mmh_ctx* c, double** d_def, double** d_rho, double** d_defp) {
+  if (!c) return MMH_ERR_ARG;
+  if (d_def) *d_def = c->def;
+  if (d_rho) *d_rho = c->rho;
+  if (d_defp) *d_defp = c->defp();
+  return MMH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,312 @@
+"""Python mirror of the reference's Fortran interface for the MMH hot path.
+
+Each function keeps the name, argument order and meaning of the Fortran
+subroutine it replaces (mmh/limiter.f90 calcdefp, mmh/multigrid.f90 multigrid,
+mmh/relaxing.f90 relaxing, mmh/gradient.f90 scalar2gradient,
+mmh/reconstruct.f90 defp2delta, mmh/gauss1.f90 relax/zerosum/rgzerosum,
+mmh/mgutil.f90 restrict/inject) and calls the CUDA library through its C ABI
+(include/mmh.h).  Arrays are numpy arrays in Fortran order; the Fortran
+convention of updating arguments in place is kept.  Where the Fortran stops
+the program (write + stop/pause), these functions raise MMHError.
+
+There is no CPU fallback: the library must be built (build.py) and a CUDA
+device must be present, otherwise loading fails loudly.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libmmh_gb300.so")
+
+MMH_FP64 = 0
+MMH_MIXED = 1
+MMH_SCHED_REF = 0
+MMH_SCHED_TOL = 1
+
+MMH_OK = 0
+MMH_ERR_DIVERGED = -6
+
+# every entry point of include/mmh.h
+EXPORTS = (
+    "mmh_config_default", "mmh_create", "mmh_destroy", "mmh_strerror", "mmh_sync", "mmh_launch_count",
+    "mmh_calcdefp", "mmh_calcdefp_f64", "mmh_multigrid", "mmh_multigrid_f64", "mmh_relaxing", "mmh_relaxing_f64",
+    "mmh_scalar2gradient", "mmh_scalar2gradient_f64", "mmh_defp2delta", "mmh_defp2delta_f64",
+    "mmh_relax_f64", "mmh_metric_f64", "mmh_restrict_f64", "mmh_inject_f64", "mmh_zerosum_f64",
+    "mmh_rgzerosum_f64", "mmh_nsmooth_f64", "mmh_limiter_pass1_f64", "mmh_limiter_mask_f64",
+    "mmh_limiter_poisson_f64", "mmh_load_f64", "mmh_load_dev", "mmh_iterate", "mmh_store_f64",
+    "mmh_outputs_f64", "mmh_state_dev",
+)
+
+
+class MMHError(RuntimeError):
+    def __init__(self, code, what=""):
+        self.code = code
+        super().__init__(f"{what}: {strerror(code)} ({code})" if what else f"{strerror(code)} ({code})")
+
+
+class Config(C.Structure):
+    _fields_ = [("n", C.c_int), ("precision", C.c_int), ("schedule", C.c_int), ("nu1", C.c_int), ("nu2", C.c_int),
+                ("max_cycles", C.c_int), ("tol", C.c_double), ("device", C.c_int), ("stream", C.c_void_p)]
+
+
+class Diag(C.Structure):
+    _fields_ = [
+        ("r1", C.c_double), ("relaxerr", C.c_double), ("rhsnorm", C.c_double), ("resid_rel", C.c_double),
+        ("vcycles", C.c_int), ("guards", C.c_int), ("status", C.c_int), ("pad", C.c_int),
+        ("nexpand", C.c_longlong), ("ncompress", C.c_longlong),
+        ("cmax", C.c_double), ("detmin", C.c_double), ("detmax", C.c_double),
+        ("fluxmax", C.c_double), ("fluxmin", C.c_double), ("rho2", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad"}
+
+
+_lib = None
+
+
+def lib():
+    """Load libmmh_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(f"libmmh_gb300.so not built ({LIB_PATH}); run build.py / __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        L.mmh_strerror.restype = C.c_char_p
+        L.mmh_launch_count.restype = C.c_ulonglong
+        _lib = L
+    return _lib
+
+
+def strerror(code):
+    try:
+        return lib().mmh_strerror(int(code)).decode()
+    except OSError:
+        return f"error {code}"
+
+
+def launch_count():
+    return int(lib().mmh_launch_count())
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _chk(rc, what, allow_diverged=False):
+    if rc != MMH_OK and not (allow_diverged and rc == MMH_ERR_DIVERGED):
+        raise MMHError(rc, what)
+    return rc
+
+
+def _farr(a, dtype):
+    if not (isinstance(a, np.ndarray) and a.dtype == dtype and a.flags.f_contiguous):
+        raise TypeError(f"expected a Fortran-ordered {np.dtype(dtype).name} array")
+    return a
+
+
+def _sfx(dtype):
+    return "_f64" if np.dtype(dtype) == np.float64 else ""
+
+
+def _sc(dtype, v):
+    return C.c_double(v) if np.dtype(dtype) == np.float64 else C.c_float(v)
+
+
+class Context:
+    """Device state for one grid size NG (the Fortran's compile-time NG)."""
+
+    def __init__(self, n, precision=MMH_FP64, schedule=MMH_SCHED_REF, nu1=2, nu2=2, tol=1e-10, max_cycles=200,
+                 device=0, stream=None):
+        L = lib()
+        cfg = Config()
+        L.mmh_config_default(C.byref(cfg), int(n))
+        cfg.precision, cfg.schedule = int(precision), int(schedule)
+        cfg.nu1, cfg.nu2, cfg.tol, cfg.max_cycles, cfg.device = int(nu1), int(nu2), float(tol), int(max_cycles), int(device)
+        cfg.stream = stream
+        self.cfg = cfg
+        self.n = int(n)
+        self._h = C.c_void_p()
+        _chk(L.mmh_create(C.byref(self._h), C.byref(cfg)), "mmh_create")
+
+    def close(self):
+        if self._h:
+            lib().mmh_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ---- drop-ins ---------------------------------------------------------
+    def calcdefp(self, defp, tmp, tmp2, defpot, u, dtold1=1.0, dtaumesh=1.0, nfluid=5):
+        """calcdefp(defp,tmp,tmp2,def,u,dtold1,dtaumesh,nfluid)  (mmh/limiter.f90:17)."""
+        dt = defp.dtype
+        for a in (defp, defpot, u):
+            _farr(a, dt)
+        d = Diag()
+        fn = getattr(lib(), "mmh_calcdefp" + _sfx(dt))
+        rc = fn(self._h, _p(defp), _p(tmp), _p(tmp2), _p(defpot), _p(u), _sc(dt, dtold1), _sc(dt, dtaumesh),
+                int(nfluid), C.byref(d))
+        _chk(rc, "calcdefp", allow_diverged=True)
+        return d.as_dict()
+
+    def multigrid(self, u, rhs, defpot, ubig, dx, nx, ny, nz, nu, nred=1, iopt=2):
+        """multigrid(u,rhs,defpot,ubig,dx,nx,ny,nz,nu,nred,iopt)  (mmh/multigrid.f90:16)."""
+        dt = u.dtype
+        for a in (u, rhs, defpot, ubig):
+            _farr(a, dt)
+        d = Diag()
+        fn = getattr(lib(), "mmh_multigrid" + _sfx(dt))
+        rc = fn(self._h, _p(u), _p(rhs), _p(defpot), _p(ubig), _sc(dt, dx), int(nx), int(ny), int(nz), int(nu),
+                int(nred), int(iopt), C.byref(d))
+        _chk(rc, "multigrid", allow_diverged=True)
+        return d.as_dict()
+
+    def relaxing(self, u, defpot, defp, cmax=1.0, dt=1.0, nfluidcmp=5):
+        """relaxing(u,def,defp,cmax,dt,nfluidcmp)  (mmh/relaxing.f90:21)."""
+        ty = u.dtype
+        for a in (u, defpot, defp):
+            _farr(a, ty)
+        fn = getattr(lib(), "mmh_relaxing" + _sfx(ty))
+        _chk(fn(self._h, _p(u), _p(defpot), _p(defp), _sc(ty, cmax), _sc(ty, dt), int(nfluidcmp)), "relaxing")
+
+    def scalar2gradient(self, indata, outdata, nn):
+        """scalar2gradient(indata,outdata,nn)  (mmh/gradient.f90:1)."""
+        dt = indata.dtype
+        _farr(indata, dt), _farr(outdata, dt)
+        nn = (C.c_int * 3)(*[int(x) for x in nn])
+        fn = getattr(lib(), "mmh_scalar2gradient" + _sfx(dt))
+        _chk(fn(self._h, _p(indata), _p(outdata), nn), "scalar2gradient")
+
+    def defp2delta(self, indata, outdata, nn):
+        """defp2delta(indata,outdata,nn)  (mmh/reconstruct.f90:1)."""
+        dt = indata.dtype
+        _farr(indata, dt), _farr(outdata, dt)
+        nn = (C.c_int * 3)(*[int(x) for x in nn])
+        fn = getattr(lib(), "mmh_defp2delta" + _sfx(dt))
+        _chk(fn(self._h, _p(indata), _p(outdata), nn), "defp2delta")
+
+    # ---- reference subroutines on the path (FP64) -------------------------
+    def relax(self, arr, rhs, deformpot, rho, dx, nrelax, iopt):
+        """relax(arr,resid,rhs,deformpot,u,rinf,dx,n,n,n,1,nrelax,iopt): returns (resid, rinf)."""
+        n = arr.shape[0]
+        for a in (arr, rhs, deformpot, rho):
+            _farr(a, np.float64)
+        resid = np.zeros((n // 2,) * 3, dtype=np.float64, order="F")
+        rinf = C.c_double(0)
+        _chk(lib().mmh_relax_f64(self._h, _p(arr), _p(resid), _p(rhs), _p(deformpot), _p(rho), C.byref(rinf),
+                                 C.c_double(dx), n, int(nrelax), int(iopt)), "relax")
+        return resid, rinf.value
+
+    def metric(self, deformpot, rho, dx=1.0):
+        n = deformpot.shape[0]
+        coef = np.zeros((n, n, n, 6), dtype=np.float64, order="F")
+        _chk(lib().mmh_metric_f64(self._h, _p(_farr(deformpot, np.float64)), _p(_farr(rho, np.float64)),
+                                  C.c_double(dx), n, _p(coef)), "metric")
+        return coef
+
+    def restrict(self, u):
+        n = u.shape[0]
+        uh = np.zeros((n // 2,) * 3, dtype=np.float64, order="F")
+        _chk(lib().mmh_restrict_f64(self._h, _p(_farr(u, np.float64)), n, _p(uh)), "restrict")
+        return uh
+
+    def inject(self, u, uhalf):
+        _chk(lib().mmh_inject_f64(self._h, _p(_farr(u, np.float64)), _p(_farr(uhalf, np.float64)), u.shape[0]),
+             "inject")
+
+    def zerosum(self, arr):
+        _chk(lib().mmh_zerosum_f64(self._h, _p(_farr(arr, np.float64)), arr.shape[0]), "zerosum")
+
+    def rgzerosum(self, arr, defpot, dx=1.0):
+        _chk(lib().mmh_rgzerosum_f64(self._h, _p(_farr(arr, np.float64)), _p(_farr(defpot, np.float64)),
+                                     C.c_double(dx), arr.shape[0]), "rgzerosum")
+
+    def nsmooth(self, a):
+        _chk(lib().mmh_nsmooth_f64(self._h, _p(_farr(a, np.float64)), a.shape[0]), "nsmooth")
+
+    def limiter_pass1(self, tmp, defpot, rho, dtold=1.0, dtaumesh=1.0):
+        n = tmp.shape[0]
+        mx = np.zeros((n, n, n), dtype=np.uint8, order="F")
+        mc = np.zeros((n, n, n), dtype=np.uint8, order="F")
+        d = Diag()
+        _chk(lib().mmh_limiter_pass1_f64(self._h, _p(_farr(tmp, np.float64)), _p(_farr(defpot, np.float64)),
+                                         _p(_farr(rho, np.float64)), n, C.c_double(dtold), C.c_double(dtaumesh),
+                                         _p(mx), _p(mc), C.byref(d)), "limiter_pass1")
+        return mx, mc, d.as_dict()
+
+    def limiter_mask(self, defpot, defp, dtold=1.0):
+        n = defpot.shape[0]
+        lim = np.zeros((n, n, n), dtype=np.float64, order="F")
+        m = np.zeros((n, n, n), dtype=np.uint8, order="F")
+        d = Diag()
+        _chk(lib().mmh_limiter_mask_f64(self._h, _p(lim), _p(_farr(defpot, np.float64)), _p(_farr(defp, np.float64)),
+                                        n, C.c_double(dtold), _p(m), C.byref(d)), "limiter_mask")
+        return lim, m, d.as_dict()
+
+    def limiter_poisson(self, defp, defplim):
+        _chk(lib().mmh_limiter_poisson_f64(self._h, _p(_farr(defp, np.float64)), _p(_farr(defplim, np.float64)),
+                                           defp.shape[0]), "limiter_poisson")
+
+    # ---- device-resident reconstruction ----------------------------------
+    def load(self, defpot, u):
+        u = _farr(u, np.float64)
+        _chk(lib().mmh_load_f64(self._h, _p(defpot), _p(u), u.shape[0]), "load")
+
+    def load_dev(self, d_def, d_rho):
+        _chk(lib().mmh_load_dev(self._h, C.c_void_p(d_def) if d_def else None, C.c_void_p(d_rho)), "load_dev")
+
+    def iterate(self, niter=1):
+        d = Diag()
+        _chk(lib().mmh_iterate(self._h, int(niter), C.byref(d)), "iterate", allow_diverged=True)
+        return d.as_dict()
+
+    def store(self, defpot=None, u=None):
+        nf = u.shape[0] if u is not None else 5
+        _chk(lib().mmh_store_f64(self._h, _p(defpot), _p(u), nf), "store")
+
+    def outputs(self, grad=None, delta=None):
+        _chk(lib().mmh_outputs_f64(self._h, _p(grad), _p(delta)), "outputs")
+
+    def state_dev(self):
+        a, b, c = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        _chk(lib().mmh_state_dev(self._h, C.byref(a), C.byref(b), C.byref(c)), "state_dev")
+        return a.value, b.value, c.value
+
+    def sync(self):
+        _chk(lib().mmh_sync(self._h), "sync")
+
+
+def reconstruct(rho, niter, precision=MMH_FP64, schedule=MMH_SCHED_REF, tol=1e-10, outputs=True, **kw):
+    """mmh/main.f90:83-179 on one density field: niter deformation iterations
+    from def = 0, then the spectral displacement and density outputs."""
+    n = rho.shape[0]
+    with Context(n, precision=precision, schedule=schedule, tol=tol, **kw) as ctx:
+        u = np.zeros((5, n, n, n), dtype=np.float64, order="F")
+        u[0] = rho
+        ctx.load(None, u)
+        diag = ctx.iterate(niter)
+        defpot = np.zeros((n, n, n), dtype=np.float64, order="F")
+        ctx.store(defpot, u)
+        res = {"def": defpot, "u": u, "diag": diag}
+        if outputs:
+            grad = np.zeros((n, n, n, 3), dtype=np.float64, order="F")
+            delta = np.zeros((n, n, n), dtype=np.float64, order="F")
+            ctx.outputs(grad, delta)
+            res["grad"], res["delta"] = grad, delta
+        return res
