@@ -24,7 +24,7 @@ def lognormal_density(n, sigma=1.0, ns=-1.5, smooth=2.0, seed=1000, dtype=np.flo
     k = np.sqrt(k2)
     with np.errstate(divide="ignore"):
         amp = np.where(k > 0, k ** (ns / 2.0), 0.0) * np.exp(-k2 * smooth * smooth / 2.0)
-    g = np.fft.irfftn(W * amp, s=(n, n, n))
+    g = np.fft.irfftn(W * amp, s=(n, n, n), axes=(0, 1, 2))
     g = g / g.std() * sigma
     rho = np.exp(g - sigma * sigma / 2.0)
     rho = rho / rho.mean()
