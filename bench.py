@@ -1,0 +1,405 @@
+#!/usr/bin/env python
+"""MMH reconstruction benchmark on GB300: prints ONE JSON line.
+
+Workload (the headline configuration): a 512^3 periodic lognormal density
+(sigma_lnrho = 1.5, P(k) ~ k^-1.5, Gaussian-smoothed at 2 cells, seeded),
+20 mesh-deformation iterations (calcdefp, def += defp, relaxing), every
+multigrid solve run to ||r||_inf / ||rhs||_inf <= 1e-8 with the residual in
+FP64, followed by the spectral displacement and density outputs.  One "step"
+is one such reconstruction; the metric is seconds per reconstruction.
+
+  value   : mixed form (FP32 V-cycles in an FP64 defect-correction loop), input
+            density resident in HBM, CUDA events on the library's stream.
+  e2e     : the same through the C ABI with host buffers: H2D of the density
+            from pinned memory, D2H of def, the displacement and the density
+            outputs, all inside the timed region.
+  fp64    : the plain FP64 GPU form of the same workload, for the mixed/FP64
+            ratio the metric asks for.
+  roofline: the dominant kernel timed live over the timed region with CUDA
+            events (achieved = algorithmic bytes / device time) against the
+            measured HBM copy bandwidth.
+  cpu_baseline: the CPU oracle (FP64, all host threads) on a bounded sample.
+
+Multi-GPU: independent reconstructions, one per rank (replicas; the path has
+no exchange step).  --impl reference times the CPU restatement of the
+reference (the Fortran reference has no compiler on this image).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = "moving-mesh-reconstruction_gb300"
+for p in (ROOT, os.path.join(ROOT, PKG), os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "s per 512³ reconstruction to residual 1e-8: mixed vs FP64 GPU; stencil HBM GB/s"
+UNIT = "s/reconstruction"
+# Algorithmic bytes per processed cell (per updated cell for the colour kernel):
+# Gauss-Seidel colour sweep reads phi, rhs and 6 coefficients and writes phi
+# (9 words); the residual reads phi, rhs, 6 coefficients and writes r (9 words).
+ALG_WORDS = {"gs": 9, "residual": 9}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--niter", type=int, default=20)
+    ap.add_argument("--sigma", type=float, default=1.5)
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--seed", type=int, default=1000)
+    ap.add_argument("--max-cycles", type=int, default=200)
+    ap.add_argument("--fp64-steps", type=int, default=1, help="timed FP64 reconstructions (0: skip)")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--cpu-sample", default="auto", choices=["auto", "none"])
+    ap.add_argument("--cpu-n", type=int, default=0, help="grid of the CPU sample (default: --n)")
+    ap.add_argument("--profile", default="gs32", choices=["gs32", "gs64", "res64", "res32", "none"])
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = list(self.rows)
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[0]) for r in rows if num(r[0]) is not None]
+        smax = [num(r[1]) for r in rows if num(r[1]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in rows for q in range(4) if r[4 + q].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle sample (test infrastructure timed as the baseline)
+# ---------------------------------------------------------------------------
+def cpu_sample(n, niter, sigma, seed, tol, cycles_hint=None):
+    """Time the oracle (FP64, tolerance schedule, 8-colour order, all host
+    threads) on a bounded sample of the workload and scale it to seconds per
+    reconstruction: one deformation iteration with the solve capped at one
+    V-cycle (t1) and at two V-cycles (t2); t_v = t2 - t1 is one V-cycle.
+    The V-cycles per solve C are measured by the oracle itself on a 64^3
+    instance solved to tol.  s/reconstruction = niter * (t1 + (C - 1) * t_v)."""
+    import oracle
+    import fields
+    threads = oracle.threads(0)
+    rho = fields.lognormal_density(n, sigma=sigma, seed=seed)
+    u = np.asfortranarray(rho.reshape((1,) + rho.shape))
+    d0 = np.zeros_like(rho, order="F")
+    times = []
+    for cyc in (1, 2):
+        t = time.perf_counter()
+        oracle.calcdefp(d0, u, sched=oracle.SCHED_TOL, tol=tol, maxcyc=cyc, colour8=True)
+        times.append(time.perf_counter() - t)
+    t1, t2 = times
+    tv = max(t2 - t1, 0.0)
+    if cycles_hint is None:
+        m = 64
+        r64 = fields.lognormal_density(m, sigma=sigma, seed=seed)
+        _, _, dg, _ = oracle.calcdefp(np.zeros_like(r64, order="F"), np.asfortranarray(r64.reshape((1,) + r64.shape)),
+                                      sched=oracle.SCHED_TOL, tol=tol, maxcyc=500, colour8=True)
+        cycles = float(dg["vcycles"])
+        src = f"oracle 64^3 solve to {tol:g}"
+    else:
+        cycles = float(cycles_hint)
+        src = "GPU FP64 run of the same workload"
+    value = niter * (t1 + (cycles - 1.0) * tv)
+    return {
+        "value": value, "unit": UNIT, "cores": threads, "kind": "port",
+        "sample": (f"oracle FP64 on {n}^3: one deformation iteration with the solve capped at 1 V-cycle "
+                   f"({t1:.2f} s) and at 2 ({t2:.2f} s); scaled to {niter} iterations x {cycles:.1f} V-cycles "
+                   f"per solve ({src}); {threads} threads"),
+        "sample_seconds": t1 + t2,
+    }
+
+
+def reference_arm(args):
+    """--impl reference: the CPU restatement on the host cores (rank 0 only)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    n = args.cpu_n or args.n
+    for _ in range(args.warmup):  # warm-up on a small grid (first touch, thread pool)
+        cpu_sample(64, 1, args.sigma, args.seed, args.tol, cycles_hint=1)
+    vals, last = [], None
+    t0 = time.perf_counter()
+    for _ in range(max(args.steps, 1)):
+        last = cpu_sample(n, args.niter, args.sigma, args.seed, args.tol)
+        vals.append(last["value"])
+    wall = time.perf_counter() - t0
+    v = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * wall / max(args.steps, 1), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args),
+        "cpu_baseline": {k: last[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the Fortran reference cannot be compiled here (no Fortran compiler); the CPU restatement "
+                "in oracle/ stands in for it",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def workload_config(args):
+    return {
+        "workload": f"{args.n}^3 lognormal density, sigma_lnrho={args.sigma}, P(k)~k^-1.5, smoothed at 2 cells, "
+                    f"seed {args.seed}; {args.niter} deformation iterations; multigrid V(2,2) cycles to "
+                    f"||r||inf/||rhs||inf<={args.tol:g} (FP64 residual); spectral displacement and density outputs",
+        "n": args.n, "iterations": args.niter, "tol": args.tol, "sigma_lnrho": args.sigma,
+        "precision": "mixed (FP32 V-cycle, FP64 residual/limiter/relaxing/FFT)",
+        "l2": "inputs larger than L2 (one 512^3 FP64 field is 1 GiB vs 129 MB L2)",
+        "parallelism": f"replicas x{args.gpus}",
+    }
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel):
+    """Per-cell DRAM traffic of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic_per_cell.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == kernel:
+                return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+    __import__("importlib").import_module(PKG)
+    import mmh
+    import fields
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = args.n
+    n3 = n ** 3
+    seed = args.seed + rank  # independent realisation per rank
+
+    rho_np = fields.lognormal_density(n, sigma=args.sigma, seed=seed)
+    rho_dev = torch.from_numpy(rho_np.ravel(order="F")).to(dev)
+    grad_dev = torch.empty(3 * n3, dtype=torch.float64, device=dev)
+    delta_dev = torch.empty(n3, dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+
+    def barrier():
+        if dist:
+            tdist.barrier()
+        torch.cuda.synchronize()
+
+    def make_ctx(precision):
+        return mmh.Context(n, precision=precision, schedule=mmh.MMH_SCHED_TOL, tol=args.tol,
+                           max_cycles=args.max_cycles, device=local, stream=stream.cuda_stream)
+
+    def recon(ctx):
+        ctx.load_dev(None, rho_dev.data_ptr())
+        d = ctx.iterate(args.niter)
+        ctx.outputs_dev(grad_dev.data_ptr(), delta_dev.data_ptr())
+        return d
+
+    def timed(ctx, steps, profile_kind=None):
+        barrier()
+        launches0 = mmh.launch_count()
+        if profile_kind:
+            mmh.profile_start(profile_kind)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        diags = []
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(steps):
+                diags.append(recon(ctx))
+            e1.record(stream)
+        e1.synchronize()
+        prof = mmh.profile_stop() if profile_kind else None
+        barrier()
+        ms = e0.elapsed_time(e1) / steps
+        if dist:
+            t = torch.tensor([ms], device=dev)
+            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, diags, mmh.launch_count() - launches0, prof
+
+    # ---- mixed (headline value) ----
+    ctx = make_ctx(mmh.MMH_MIXED)
+    for _ in range(args.warmup):
+        recon(ctx)
+        ctx.sync()
+    kinds = {"gs32": mmh.K_GS | mmh.K_F32, "gs64": mmh.K_GS, "res64": mmh.K_RESIDUAL,
+             "res32": mmh.K_RESIDUAL | mmh.K_F32, "none": None}
+    pk = kinds[args.profile]
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_mixed, diags, launches, prof = timed(ctx, args.steps, pk)
+    clk = clocks.stop()
+
+    # ---- e2e through the C ABI with host buffers ----
+    rho_host = torch.from_numpy(rho_np.ravel(order="F").copy()).pin_memory()
+    def_host = torch.empty(n3, dtype=torch.float64).pin_memory()
+    grad_host = torch.empty(3 * n3, dtype=torch.float64).pin_memory()
+    delta_host = torch.empty(n3, dtype=torch.float64).pin_memory()
+
+    def as_np(t, shape):  # Fortran-ordered numpy view of pinned host memory
+        return t.numpy().reshape(shape, order="F")
+
+    u1 = as_np(rho_host, (1, n, n, n))
+    defh = as_np(def_host, (n, n, n))
+    gradh = as_np(grad_host, (n, n, n, 3))
+    deltah = as_np(delta_host, (n, n, n))
+    e2e_ms = None
+    if args.e2e_steps > 0:
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(args.e2e_steps):
+                ctx.load(None, u1)
+                ctx.iterate(args.niter)
+                ctx.outputs(gradh, deltah)
+                ctx.store(defh, None)
+            e1.record(stream)
+        e1.synchronize()
+        barrier()
+        e2e_ms = e0.elapsed_time(e1) / args.e2e_steps
+    ctx.close()
+
+    # ---- FP64 form ----
+    fp64 = None
+    if args.fp64_steps > 0:
+        c64 = make_ctx(mmh.MMH_FP64)
+        recon(c64)
+        c64.sync()
+        ms64, d64, _, _ = timed(c64, args.fp64_steps)
+        c64.close()
+        fp64 = {"value": ms64 / 1000.0, "unit": UNIT, "vcycles_last_solve": d64[-1]["vcycles"],
+                "resid_rel_last_solve": d64[-1]["resid_rel"], "steps": args.fp64_steps, "warmup": 1}
+
+    if rank != 0:
+        if dist:
+            tdist.destroy_process_group()
+        return 0
+
+    # roofline of the profiled kernel
+    hbm, peak_src = peaks()
+    roofline = None
+    if prof and prof[0] > 0:
+        nl, pms, cells = prof
+        word = 4 if pk & mmh.K_F32 else 8
+        kname = args.profile
+        words = ALG_WORDS["gs" if kname.startswith("gs") else "residual"]
+        alg_bytes = cells * words * word
+        achieved = alg_bytes / (pms / 1000.0) / 1e9
+        tr = traffic_from_profiles(kname)
+        roofline = {"kernel": {"gs32": "k_gs_colour<float>", "gs64": "k_gs_colour<double>",
+                               "res64": "k_residual<double>", "res32": "k_residual<float>"}[kname],
+                    "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                    "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else peak_src,
+                    "traffic": (tr * cells / nl) if tr else None,
+                    "alg_bytes_per_launch": alg_bytes / nl, "launches": nl,
+                    "avg_launch_ms": pms / nl, "share_of_step": (pms / args.steps) / ms_mixed}
+
+    cpu = None
+    if args.cpu_sample != "none" and not dist:
+        hint = fp64["vcycles_last_solve"] if fp64 else None
+        cpu = cpu_sample(args.cpu_n or n, args.niter, args.sigma, args.seed, args.tol, cycles_hint=hint)
+        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    value = ms_mixed / 1000.0 / world  # whole-job seconds per reconstruction (replicas)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "config": workload_config(args),
+        "e2e": {"value": (e2e_ms / 1000.0 / world) if e2e_ms else None, "unit": UNIT,
+                "h2d_bytes_per_step": 8 * n3, "d2h_bytes_per_step": 8 * 5 * n3},
+        "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+        "fp64": fp64, "mixed_vs_fp64_speedup": (fp64["value"] / (ms_mixed / 1000.0)) if fp64 else None,
+        "solve": {"vcycles_last": diags[-1]["vcycles"], "resid_rel_last": diags[-1]["resid_rel"],
+                  "ncompress_last": diags[-1]["ncompress"], "guards_last": diags[-1]["guards"]},
+        "cells_per_s": n3 * args.niter * world / (ms_mixed / 1000.0),
+    }
+    print(json.dumps(line))
+    if dist:
+        tdist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

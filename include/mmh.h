@@ -42,15 +42,18 @@ extern "C" {
 #define MMH_MIXED 1 /* FP32 inner V-cycles inside an FP64 defect-correction loop */
 
 /* multigrid schedules */
-#define MMH_SCHED_REF 0 /* reference: one V-cycle, 4*NG/n sweeps per level (mgtemplate.f90) */
-#define MMH_SCHED_TOL 1 /* V(nu1,nu2) cycles until ||r||_inf <= tol*||rhs||_inf */
+#define MMH_SCHED_REF 0    /* reference: one V-cycle, 4*NG/n sweeps per level (mgtemplate.f90) */
+#define MMH_SCHED_TOL 1    /* flexible CG preconditioned by one V(nu1,nu2) cycle per iteration,
+                              until ||r||_inf <= tol*||rhs||_inf */
+#define MMH_SCHED_VCYCLE 2 /* plain V(nu1,nu2) cycles until ||r||_inf <= tol*||rhs||_inf (MMH_MIXED:
+                              FP32 cycles in an FP64 defect-correction loop) */
 
 typedef struct mmh_ctx mmh_ctx;
 
 typedef struct mmh_config {
   int n;          /* NG: top-level grid size, power of two, 8..1024 (mmh/dimen.f90:1) */
-  int precision;  /* MMH_FP64 or MMH_MIXED (MMH_MIXED requires MMH_SCHED_TOL) */
-  int schedule;   /* MMH_SCHED_REF or MMH_SCHED_TOL */
+  int precision;  /* MMH_FP64 or MMH_MIXED (MMH_MIXED needs MMH_SCHED_TOL or MMH_SCHED_VCYCLE) */
+  int schedule;   /* MMH_SCHED_REF, MMH_SCHED_TOL or MMH_SCHED_VCYCLE */
   int nu1, nu2;   /* pre/post Gauss-Seidel sweeps per level, tolerance schedule */
   int max_cycles; /* V-cycle / outer-iteration cap, tolerance schedule */
   double tol;     /* relative max-norm residual target, tolerance schedule */
@@ -65,7 +68,7 @@ typedef struct mmh_diag {
   double relaxerr;  /* top-level max-norm residual after post-smoothing (last cycle) */
   double rhsnorm;   /* max |rhs| after rgzerosum */
   double resid_rel; /* final ||r||_inf/||rhs||_inf (FP64 residual in MMH_MIXED) */
-  int vcycles;      /* V-cycles (MMH_FP64) or outer corrections (MMH_MIXED) run */
+  int vcycles;      /* V-cycles / PCG iterations / outer corrections run in the last solve */
   int guards;       /* coarse-level corrections discarded by the divergence guard */
   int status;       /* status of the call */
   int pad;
@@ -155,8 +158,26 @@ int mmh_store_f64(mmh_ctx* ctx, double* def, double* u, int nfluid);
 /* Spectral outputs of the current def to the host: grad(n,n,n,3), delta(n,n,n)
  * (either may be NULL).  mmh/main.f90:131-179 */
 int mmh_outputs_f64(mmh_ctx* ctx, double* grad, double* delta);
+/* Same to device memory: d_grad (3 n^3 doubles), d_delta (n^3 doubles). */
+int mmh_outputs_dev(mmh_ctx* ctx, double* d_grad, double* d_delta);
 /* Device pointers of the resident state (n^3 doubles each). */
 int mmh_state_dev(mmh_ctx* ctx, double** d_def, double** d_rho, double** d_defp);
+
+/* ---- kernel timing (no counterpart in the reference) -------------------- */
+/* Arm CUDA-event timing of one kernel kind (MMH_K_* | MMH_K_F32 for the FP32
+ * instantiation) on the stream it is launched on; mmh_profile_stop returns the
+ * number of launches timed, their summed device time in ms and the number of
+ * cells they processed (cells updated, for the Gauss-Seidel colour kernel). */
+#define MMH_K_GS 1
+#define MMH_K_RESIDUAL 2
+#define MMH_K_RESTRICT_RESID 3
+#define MMH_K_METRIC 4
+#define MMH_K_SMOOTH 5
+#define MMH_K_PROLONG 6
+#define MMH_K_RESTRICT 7
+#define MMH_K_F32 256
+int mmh_profile_start(int kind);
+int mmh_profile_stop(int* launches, double* ms, long long* cells);
 
 #ifdef __cplusplus
 }

@@ -11,6 +11,18 @@ typedef long long i64;
 void count_launch(int k = 1);
 unsigned long long launch_count();
 
+// Kernel timing hooks: when profiling is armed for `kind`, the launcher
+// brackets each launch of that kernel with CUDA events on its stream.
+enum KernelKind {
+  KK_GS = 1, KK_RESIDUAL = 2, KK_RESTRICT_RESID = 3, KK_METRIC = 4, KK_SMOOTH = 5, KK_PROLONG = 6,
+  KK_RESTRICT = 7, KK_LIMITER = 8, KK_RELAXING = 9, KK_SPECTRAL = 10, KK_APPLY = 11, KK_F32 = 256
+};
+void prof_begin(int kind, cudaStream_t s, i64 cells);
+void prof_end(int kind, cudaStream_t s);
+int prof_start(int kind);
+int prof_stop(int* launches, double* ms, long long* cells);
+template <class T> inline int kk(int base) { return base | (sizeof(T) == 4 ? KK_F32 : 0); }
+
 // Launchers, instantiated for double (mmh_kernels_f64.cu, no FMA contraction)
 // and float (mmh_kernels_f32.cu).
 template <class T> void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_t s);
@@ -62,5 +74,21 @@ void launch_relax_dpv(const double* u, const double* vt, const double* cc, int n
 // u(nf,n^3) (float or double) <-> density; flag |= 1 when a component 2..nf is not zero
 void launch_extract_density_f(const float* u, int nf, i64 n3, double* rho, int* flag, cudaStream_t s);
 void launch_extract_density_d(const double* u, int nf, i64 n3, double* rho, int* flag, cudaStream_t s);
+
+// flexible PCG scalars and accumulators (device)
+struct PcgDev {
+  unsigned long long acc[3][2];
+  unsigned long long rbits, zbits, pbits, qbits;
+  double rz, pq, alpha, beta;
+};
+void launch_apply(const double* p, const double* coef, int n, double dx, double* q, unsigned long long* qbits,
+                  cudaStream_t s);
+void launch_dot(const double* a, const double* b, i64 count, const unsigned long long* abits,
+                const unsigned long long* bbits, unsigned long long* acc, cudaStream_t s);
+void launch_pcg_update(double* x, double* r, const double* p, const double* q, i64 count, const double* alpha,
+                       unsigned long long* rbits, cudaStream_t s);
+void launch_pcg_pupdate(double* p, const double* z, i64 count, const double* beta, unsigned long long* pbits,
+                        cudaStream_t s);
+void launch_pcg_scalar(PcgDev* st, int stage, cudaStream_t s);
 
 }  // namespace mmh

@@ -2,6 +2,7 @@
 // expression rounds as written, so results match the CPU restatement bit for
 // bit (except where a libm function -- acos, cos -- is involved).
 #include <atomic>
+#include <vector>
 
 #include "mmh_launch.cuh"
 #include "mmh_phys.cuh"
@@ -11,6 +12,64 @@ namespace mmh {
 static std::atomic<unsigned long long> g_launches{0};
 void count_launch(int k) { g_launches.fetch_add((unsigned long long)k, std::memory_order_relaxed); }
 unsigned long long launch_count() { return g_launches.load(); }
+
+// ---------------------------------------------------------------------------
+// kernel timing hooks
+// ---------------------------------------------------------------------------
+namespace {
+struct Prof {
+  int kind = 0;
+  std::vector<cudaEvent_t> ev;
+  int used = 0, dropped = 0;
+  long long cells = 0;
+};
+Prof g_prof;
+}  // namespace
+
+int prof_start(int kind) {
+  if (g_prof.ev.empty()) {
+    g_prof.ev.resize(2 * 8192);
+    for (auto& e : g_prof.ev)
+      if (cudaEventCreate(&e) != cudaSuccess) return -1;
+  }
+  g_prof.kind = kind;
+  g_prof.used = 0;
+  g_prof.dropped = 0;
+  g_prof.cells = 0;
+  return 0;
+}
+
+void prof_begin(int kind, cudaStream_t s, i64 cells) {
+  if (g_prof.kind == 0 || kind != g_prof.kind) return;
+  if (g_prof.used >= (int)g_prof.ev.size() / 2) {
+    g_prof.dropped++;
+    return;
+  }
+  cudaEventRecord(g_prof.ev[2 * g_prof.used], s);
+  g_prof.cells += cells;
+}
+
+void prof_end(int kind, cudaStream_t s) {
+  if (g_prof.kind == 0 || kind != g_prof.kind) return;
+  if (g_prof.used >= (int)g_prof.ev.size() / 2) return;
+  cudaEventRecord(g_prof.ev[2 * g_prof.used + 1], s);
+  g_prof.used++;
+}
+
+int prof_stop(int* launches, double* ms, long long* cells) {
+  double tot = 0.0;
+  for (int q = 0; q < g_prof.used; ++q) {
+    float m = 0.f;
+    if (cudaEventSynchronize(g_prof.ev[2 * q + 1]) != cudaSuccess) return -1;
+    if (cudaEventElapsedTime(&m, g_prof.ev[2 * q], g_prof.ev[2 * q + 1]) != cudaSuccess) return -1;
+    tot += m;
+  }
+  if (launches) *launches = g_prof.used;
+  if (ms) *ms = tot;
+  if (cells) *cells = g_prof.cells;
+  g_prof.kind = 0;
+  return g_prof.dropped ? 1 : 0;
+}
 
 MMH_INSTANTIATE(double)
 
@@ -565,6 +624,148 @@ void launch_extract_density_f(const float* u, int nf, i64 n3, double* rho, int* 
 }
 void launch_extract_density_d(const double* u, int nf, i64 n3, double* rho, int* flag, cudaStream_t s) {
   k_extract_density<double><<<grid_of(n3, kBlock), kBlock, 0, s>>>(u, nf, n3, rho, flag);
+  count_launch();
+}
+
+}  // namespace mmh
+
+// ---------------------------------------------------------------------------
+// Krylov (flexible PCG) building blocks, FP64.  Dot products are exact and
+// order free: terms a_i*b_i are scaled by 2^(96-E), 2^E > max|a|*max|b|,
+// truncated to 128-bit integers and summed with two 64-bit atomics.
+// ---------------------------------------------------------------------------
+namespace mmh {
+
+__device__ __forceinline__ __int128 fx_scaled(double y) {
+  double a = fabs(y);
+  double q = floor(a * 5.42101086242752217e-20);
+  double rem = a - q * 18446744073709551616.0;
+  unsigned __int128 v = ((unsigned __int128)__double2ull_rz(q) << 64) | (unsigned __int128)__double2ull_rz(rem);
+  return y < 0 ? -(__int128)v : (__int128)v;
+}
+
+__device__ __forceinline__ double fx_unscale(const unsigned long long* acc, int E) {
+  __int128 s = (__int128)(((unsigned __int128)acc[1] << 64) | (unsigned __int128)acc[0]);
+  bool neg = s < 0;
+  unsigned __int128 a = neg ? (unsigned __int128)(-s) : (unsigned __int128)s;
+  double r = __dadd_rn(scalbn(__ull2double_rn((unsigned long long)(a >> 64)), E - 32),
+                       scalbn(__ull2double_rn((unsigned long long)a), E - 96));
+  return neg ? -r : r;
+}
+
+__device__ __forceinline__ double bits_d(const unsigned long long* b) { return __longlong_as_double((long long)*b); }
+
+// q = L[p] = (t1 + t2 + tdiag*p) * di2, max|q| into qbits
+__global__ void k_apply(const double* __restrict__ p, const double* __restrict__ coef, int n, double di2,
+                        double* __restrict__ q, unsigned long long* qbits) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  double m = 0.0;
+  if (t < n3) {
+    int i, j, k;
+    cell_of(t, n, i, j, k);
+    double tdiag, t1, t2;
+    op_terms(p, coef, n, n3, i, j, k, tdiag, t1, t2);
+    double v = (t1 + t2 + tdiag * p[t]) * di2;
+    q[t] = v;
+    m = fabs(v);
+  }
+  block_max_commit(m, qbits);
+}
+
+__global__ void k_dot(const double* __restrict__ a, const double* __restrict__ b, i64 count,
+                      const unsigned long long* abits, const unsigned long long* bbits, unsigned long long* acc) {
+  double ma = bits_d(abits), mb = bits_d(bbits);
+  __int128 s = 0;
+  if (ma > 0.0 && mb > 0.0) {
+    int E = ilogb(ma) + ilogb(mb) + 2;
+    for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (i64)gridDim.x * blockDim.x)
+      s += fx_scaled(scalbn(a[t] * b[t], 96 - E));
+  }
+  fx_block_commit(s, acc);
+}
+
+__device__ __forceinline__ double dot_value(const unsigned long long* acc, const unsigned long long* abits,
+                                            const unsigned long long* bbits) {
+  double ma = bits_d(abits), mb = bits_d(bbits);
+  if (!(ma > 0.0) || !(mb > 0.0)) return 0.0;
+  return fx_unscale(acc, ilogb(ma) + ilogb(mb) + 2);
+}
+
+// x = x + alpha*p ; r = r - alpha*q ; max|r|
+__global__ void k_pcg_update(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
+                             const double* __restrict__ q, i64 count, const double* __restrict__ alpha,
+                             unsigned long long* rbits) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  double a = *alpha;
+  double m = 0.0;
+  if (t < count) {
+    x[t] = x[t] + a * p[t];
+    double v = r[t] - a * q[t];
+    r[t] = v;
+    m = fabs(v);
+  }
+  block_max_commit(m, rbits);
+}
+
+// p = z + beta*p ; max|p|
+__global__ void k_pcg_pupdate(double* __restrict__ p, const double* __restrict__ z, i64 count,
+                              const double* __restrict__ beta, unsigned long long* pbits) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  double b = *beta;
+  double m = 0.0;
+  if (t < count) {
+    double v = z[t] + b * p[t];
+    p[t] = v;
+    m = fabs(v);
+  }
+  block_max_commit(m, pbits);
+}
+
+// scalar steps.  st: 0 rz = dot(r,z) ; 1 alpha = rz / dot(p,q) ;
+// 2 beta = -(alpha*dot(z,q))/rz, rz = dot(r,z)
+__global__ void k_pcg_scalar(PcgDev* s, int stage) {
+  if (stage == 0) {
+    s->rz = dot_value(s->acc[0], &s->rbits, &s->zbits);
+  } else if (stage == 1) {
+    s->pq = dot_value(s->acc[1], &s->pbits, &s->qbits);
+    s->alpha = s->rz / s->pq;
+  } else {
+    double zq = dot_value(s->acc[2], &s->zbits, &s->qbits);
+    double rznew = dot_value(s->acc[0], &s->rbits, &s->zbits);
+    s->beta = -(s->alpha * zq) / s->rz;
+    s->rz = rznew;
+  }
+}
+
+void launch_apply(const double* p, const double* coef, int n, double dx, double* q, unsigned long long* qbits,
+                  cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  prof_begin(KK_APPLY, s, n3);
+  k_apply<<<grid_of(n3, kBlock), kBlock, 0, s>>>(p, coef, n, 1.0 / (dx * dx), q, qbits);
+  prof_end(KK_APPLY, s);
+  count_launch();
+}
+void launch_dot(const double* a, const double* b, i64 count, const unsigned long long* abits,
+                const unsigned long long* bbits, unsigned long long* acc, cudaStream_t s) {
+  i64 blocks = (count + kBlock - 1) / kBlock;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+  k_dot<<<(unsigned)blocks, kBlock, 0, s>>>(a, b, count, abits, bbits, acc);
+  count_launch();
+}
+void launch_pcg_update(double* x, double* r, const double* p, const double* q, i64 count, const double* alpha,
+                       unsigned long long* rbits, cudaStream_t s) {
+  k_pcg_update<<<grid_of(count, kBlock), kBlock, 0, s>>>(x, r, p, q, count, alpha, rbits);
+  count_launch();
+}
+void launch_pcg_pupdate(double* p, const double* z, i64 count, const double* beta, unsigned long long* pbits,
+                        cudaStream_t s) {
+  k_pcg_pupdate<<<grid_of(count, kBlock), kBlock, 0, s>>>(p, z, count, beta, pbits);
+  count_launch();
+}
+void launch_pcg_scalar(PcgDev* st, int stage, cudaStream_t s) {
+  k_pcg_scalar<<<1, 1, 0, s>>>(st, stage);
   count_launch();
 }
 

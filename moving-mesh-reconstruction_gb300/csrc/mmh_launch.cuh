@@ -12,7 +12,9 @@ template <class T>
 void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
   T di2 = T(1) / (dx * dx);
+  prof_begin(kk<T>(KK_METRIC), s, n3);
   k_metric<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(def, rho, n, di2, coef);
+  prof_end(kk<T>(KK_METRIC), s);
   count_launch();
 }
 
@@ -25,7 +27,9 @@ void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nswe
     for (int kpar = 0; kpar < 2; ++kpar)
       for (int io = 0; io < 2; ++io)
         for (int jo = 0; jo < 2; ++jo) {
+          prof_begin(kk<T>(KK_GS), s, h3);
           k_gs_colour<T><<<g, kBlock, 0, s>>>(phi, rhs, coef, n, dx2, kpar, io, jo);
+          prof_end(kk<T>(KK_GS), s);
           count_launch();
         }
 }
@@ -35,35 +39,45 @@ void launch_residual(const T* phi, const T* rhs, const T* coef, int n, T dx, T* 
                      unsigned long long* maxbits, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
   T di2 = T(1) / (dx * dx);
+  prof_begin(kk<T>(KK_RESIDUAL), s, n3);
   k_residual<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(phi, rhs, coef, n, di2, r, r32, maxbits);
+  prof_end(kk<T>(KK_RESIDUAL), s);
   count_launch();
 }
 
 template <class T>
 void launch_restrict_resid(const T* r, int n, int special, T* coarse, cudaStream_t s) {
   i64 h3 = (i64)(n / 2) * (n / 2) * (n / 2);
+  prof_begin(kk<T>(KK_RESTRICT_RESID), s, h3);
   k_restrict_resid<T><<<grid_of(h3, kBlock), kBlock, 0, s>>>(r, n, special, coarse);
+  prof_end(kk<T>(KK_RESTRICT_RESID), s);
   count_launch();
 }
 
 template <class T>
 void launch_restrict27(const T* fine, int n, T* coarse, cudaStream_t s) {
   i64 h3 = (i64)(n / 2) * (n / 2) * (n / 2);
+  prof_begin(kk<T>(KK_RESTRICT), s, h3);
   k_restrict27<T><<<grid_of(h3, kBlock), kBlock, 0, s>>>(fine, n, coarse);
+  prof_end(kk<T>(KK_RESTRICT), s);
   count_launch();
 }
 
 template <class T>
 void launch_smooth27(const T* in, int n, T* out, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
+  prof_begin(kk<T>(KK_SMOOTH), s, n3);
   k_smooth27<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(in, n, out);
+  prof_end(kk<T>(KK_SMOOTH), s);
   count_launch();
 }
 
 template <class T>
 void launch_prolong_add(T* u, const T* uh, int n, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
+  prof_begin(kk<T>(KK_PROLONG), s, n3);
   k_prolong_add<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(u, uh, n);
+  prof_end(kk<T>(KK_PROLONG), s);
   count_launch();
 }
 

@@ -29,6 +29,7 @@ struct Scal {
   int gflag[16];
   int guards;
   int pad;
+  PcgDev pcg;
   LimDev lim;
 };
 
@@ -99,6 +100,8 @@ struct mmh_ctx {
   std::vector<double*> defl, rhol;
   // FP32 hierarchy (mixed)
   Hier<float> h32;
+  // flexible PCG vectors (solution, right-hand side, search direction, L p)
+  double *px = nullptr, *pb = nullptr, *pp = nullptr, *pq = nullptr;
   // relaxing
   double *baj = nullptr, *cc = nullptr, *vt = nullptr, *u1 = nullptr;
   // spectral
@@ -261,6 +264,88 @@ int build_levels(mmh_ctx* c, int l0) {
   return MMH_OK;
 }
 
+// One preconditioner application z = V(r): r in h64.rhs[l0], z to h64.u[l0].
+int precond(mmh_ctx* c, int l0) {
+  int n = c->nl[l0];
+  i64 n3 = (i64)n * n * n;
+  if (c->cfg.precision == MMH_MIXED) {
+    launch_d2f(c->h64.rhs[l0], c->h32.rhs[l0], n3, c->s);
+    launch_fill<float>(c->h32.u[l0], n3, 0.0f, c->s);
+    RET(vcycle<float>(c, l0));
+    launch_f2d(c->h32.u[l0], c->h64.u[l0], n3, c->s);
+  } else {
+    launch_fill<double>(c->h64.u[l0], n3, 0.0, c->s);
+    RET(vcycle<double>(c, l0));
+  }
+  CK(cudaMemsetAsync(&c->sc->pcg.zbits, 0, 8, c->s));
+  launch_absmax<double>(c->h64.u[l0], n3, &c->sc->pcg.zbits, c->s);
+  return MMH_OK;
+}
+
+// Flexible preconditioned conjugate gradients on L x = b at level l0, one
+// V-cycle per iteration as preconditioner (FP64 or FP32 cycles).  Vectors,
+// operator and dot products are FP64; dots are exact and order free.
+int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_out, double* r1_out) {
+  int n = c->nl[l0];
+  i64 n3 = (i64)n * n * n;
+  PcgDev* P = &c->sc->pcg;
+  double* r = c->h64.rhs[l0];
+  double* z = c->h64.u[l0];
+  CK(cudaMemcpyAsync(c->pb, r, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  CK(cudaMemcpyAsync(c->px, z, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  CK(cudaMemsetAsync(P, 0, sizeof(PcgDev), c->s));
+  // r = b - L x
+  launch_residual<double>(c->px, c->pb, c->h64.coef[l0], n, dx, r, nullptr, &P->rbits, c->s);
+  RET(pull_scal(c));
+  double rel = bits_to_double(c->hsc->pcg.rbits) / rn;
+  *r1_out = bits_to_double(c->hsc->pcg.rbits);
+  int it = 0;
+  int status = MMH_OK;
+  if (rel > c->cfg.tol) {
+    RET(precond(c, l0));
+    CK(cudaMemcpyAsync(c->pp, z, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+    CK(cudaMemcpyAsync(&P->pbits, &P->zbits, 8, cudaMemcpyDeviceToDevice, c->s));
+    launch_dot(r, z, n3, &P->rbits, &P->zbits, P->acc[0], c->s);
+    launch_pcg_scalar(P, 0, c->s);
+    for (it = 1;; ++it) {
+      CK(cudaMemsetAsync(&P->qbits, 0, 8, c->s));
+      launch_apply(c->pp, c->h64.coef[l0], n, dx, c->pq, &P->qbits, c->s);
+      CK(cudaMemsetAsync(P->acc[1], 0, 16, c->s));
+      launch_dot(c->pp, c->pq, n3, &P->pbits, &P->qbits, P->acc[1], c->s);
+      launch_pcg_scalar(P, 1, c->s);
+      CK(cudaMemsetAsync(&P->rbits, 0, 8, c->s));
+      launch_pcg_update(c->px, r, c->pp, c->pq, n3, &P->alpha, &P->rbits, c->s);
+      RET(pull_scal(c));
+      rel = bits_to_double(c->hsc->pcg.rbits) / rn;
+      if (!(rel == rel) || rel <= c->cfg.tol) break;
+      if (it >= c->cfg.max_cycles) {
+        status = MMH_ERR_DIVERGED;
+        break;
+      }
+      RET(precond(c, l0));
+      CK(cudaMemsetAsync(P->acc[0], 0, 16, c->s));
+      CK(cudaMemsetAsync(P->acc[2], 0, 16, c->s));
+      launch_dot(z, c->pq, n3, &P->zbits, &P->qbits, P->acc[2], c->s);
+      launch_dot(r, z, n3, &P->rbits, &P->zbits, P->acc[0], c->s);
+      launch_pcg_scalar(P, 2, c->s);
+      CK(cudaMemsetAsync(&P->pbits, 0, 8, c->s));
+      launch_pcg_pupdate(c->pp, z, n3, &P->beta, &P->pbits, c->s);
+    }
+  }
+  // zero mean, true residual, results back in place
+  RET(zerosum<double>(c, c->px, n3));
+  CK(cudaMemsetAsync(&P->rbits, 0, 8, c->s));
+  launch_residual<double>(c->px, c->pb, c->h64.coef[l0], n, dx, nullptr, nullptr, &P->rbits, c->s);
+  CK(cudaMemcpyAsync(z, c->px, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  CK(cudaMemcpyAsync(r, c->pb, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  RET(pull_scal(c));
+  double rt = bits_to_double(c->hsc->pcg.rbits);
+  *rel_out = rt / rn;
+  *iters = it;
+  if (!(rt == rt)) return MMH_ERR_NAN;
+  return status;
+}
+
 // multigrid(u, rhs, defpot, ubig, dx, ...) at level l0: u = h64.u[l0],
 // rhs = h64.rhs[l0], defpot = defl[l0], density = rhol[l0] already in place.
 int multigrid_level(mmh_ctx* c, int l0, double dx, mmh_diag* d) {
@@ -280,6 +365,26 @@ int multigrid_level(mmh_ctx* c, int l0, double dx, mmh_diag* d) {
     RET(pull_scal(c));
     rn = bits_to_double(c->hsc->rhsbits);
     rel = rn > 0 ? bits_to_double(c->hsc->errbits[l0]) / rn : 0.0;
+  } else if (c->cfg.schedule == MMH_SCHED_TOL) {
+    RET(pull_scal(c));
+    rn = bits_to_double(c->hsc->rhsbits);
+    if (rn > 0) {
+      double r1 = 0.0;
+      status = pcg_level(c, l0, dx, rn, &cycles, &rel, &r1);
+      if (status != MMH_OK && status != MMH_ERR_DIVERGED) return status;
+      if (d) d->r1 = r1;
+    }
+    RET(pull_scal(c));
+    if (c->hsc->bad) status = MMH_ERR_RANGE;
+    if (d) {
+      d->relaxerr = rel * rn;
+      d->rhsnorm = rn;
+      d->resid_rel = rel;
+      d->vcycles = cycles;
+      d->guards = c->hsc->guards;
+      d->status = status;
+    }
+    return status;
   } else if (c->cfg.precision == MMH_FP64) {
     RET(pull_scal(c));
     rn = bits_to_double(c->hsc->rhsbits);
@@ -356,7 +461,8 @@ void lim_to_diag(const LimDev& L, mmh_diag* d) {
   d->detmax = ord_to_double(L.detmax);
   d->fluxmax = ord_to_double(L.fluxmax);
   d->fluxmin = ord_to_double(L.fluxmin);
-  d->rho2 = fx_host(L.rho2);
+  // rho2 is a printed diagnostic only; terms outside the exact-sum range make it NaN
+  d->rho2 = L.flag ? NAN : fx_host(L.rho2);
 }
 
 int make_plans(mmh_ctx* c) {
@@ -404,7 +510,6 @@ int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t
   RET(limiter_poisson(c, defp, c->defplim));
   RET(pull_scal(c));
   lim_to_diag(c->hsc->lim, d);
-  if (c->hsc->lim.flag) st = MMH_ERR_RANGE;
   return st;
 }
 
@@ -605,6 +710,12 @@ const char* mmh_strerror(int code) {
 
 unsigned long long mmh_launch_count(void) { return mmh::launch_count(); }
 
+int mmh_profile_start(int kind) { return mmh::prof_start(kind) == 0 ? MMH_OK : MMH_ERR_CUDA; }
+int mmh_profile_stop(int* launches, double* ms, long long* cells) {
+  int r = mmh::prof_stop(launches, ms, cells);
+  return r < 0 ? MMH_ERR_CUDA : MMH_OK;
+}
+
 int mmh_destroy(mmh_ctx* c) {
   if (!c) return MMH_OK;
   if (c->s) cudaStreamSynchronize(c->s);
@@ -626,9 +737,10 @@ int mmh_create(mmh_ctx** out, const mmh_config* cfg) {
   if (!is_pow2(n)) return MMH_ERR_NOTPOW2;
   if (n < 8 || n > 1024) return MMH_ERR_SIZE;
   if (cfg->precision != MMH_FP64 && cfg->precision != MMH_MIXED) return MMH_ERR_ARG;
-  if (cfg->schedule != MMH_SCHED_REF && cfg->schedule != MMH_SCHED_TOL) return MMH_ERR_ARG;
-  if (cfg->precision == MMH_MIXED && cfg->schedule != MMH_SCHED_TOL) return MMH_ERR_ARG;
-  if (cfg->schedule == MMH_SCHED_TOL && (cfg->nu1 < 1 || cfg->nu2 < 1 || cfg->max_cycles < 1)) return MMH_ERR_ARG;
+  if (cfg->schedule != MMH_SCHED_REF && cfg->schedule != MMH_SCHED_TOL && cfg->schedule != MMH_SCHED_VCYCLE)
+    return MMH_ERR_ARG;
+  if (cfg->precision == MMH_MIXED && cfg->schedule == MMH_SCHED_REF) return MMH_ERR_ARG;
+  if (cfg->schedule != MMH_SCHED_REF && (cfg->nu1 < 1 || cfg->nu2 < 1 || cfg->max_cycles < 1)) return MMH_ERR_ARG;
   if (cudaSetDevice(cfg->device) != cudaSuccess) return MMH_ERR_CUDA;
   mmh_ctx* c = new (std::nothrow) mmh_ctx();
   if (!c) return MMH_ERR_NOMEM;
@@ -688,6 +800,12 @@ int mmh_create(mmh_ctx** out, const mmh_config* cfg) {
       A(&c->h32.coef[l], 6 * m3);
       A(&c->h32.r[l], m3);
     }
+  }
+  if (cfg->schedule == MMH_SCHED_TOL) {
+    A(&c->px, n3);
+    A(&c->pb, n3);
+    A(&c->pp, n3);
+    A(&c->pq, n3);
   }
   A(&c->baj, 7 * n3);
   A(&c->cc, n3);
@@ -873,7 +991,7 @@ int mmh_limiter_pass1_f64(mmh_ctx* c, double* tmp, const double* def, const doub
   CK(cudaFreeAsync(dm, c->s));
   RET(pull_scal(c));
   lim_to_diag(c->hsc->lim, d);
-  return c->hsc->lim.flag ? MMH_ERR_RANGE : MMH_OK;
+  return MMH_OK;
 }
 
 int mmh_limiter_mask_f64(mmh_ctx* c, double* defplim, const double* def, const double* defp, int n, double dtold,
@@ -960,6 +1078,12 @@ int mmh_outputs_f64(mmh_ctx* c, double* grad, double* delta) {
   if (st == MMH_OK && delta) st = download(c, o + 3 * c->n3, delta, c->n3);
   cudaFreeAsync(o, c->s);
   return st;
+}
+
+int mmh_outputs_dev(mmh_ctx* c, double* d_grad, double* d_delta) {
+  if (!c) return MMH_ERR_ARG;
+  RET(spectral_outputs(c, c->def, d_grad, d_delta));
+  return MMH_OK;
 }
 
 int mmh_state_dev(mmh_ctx* c, double** d_def, double** d_rho, double** d_defp) {

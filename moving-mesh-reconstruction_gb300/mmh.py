@@ -23,7 +23,8 @@ LIB_PATH = os.path.join(_HERE, "_build", "libmmh_gb300.so")
 MMH_FP64 = 0
 MMH_MIXED = 1
 MMH_SCHED_REF = 0
-MMH_SCHED_TOL = 1
+MMH_SCHED_TOL = 1      # flexible CG, one V-cycle per iteration as preconditioner
+MMH_SCHED_VCYCLE = 2   # plain repeated V-cycles
 
 MMH_OK = 0
 MMH_ERR_DIVERGED = -6
@@ -36,8 +37,12 @@ EXPORTS = (
     "mmh_relax_f64", "mmh_metric_f64", "mmh_restrict_f64", "mmh_inject_f64", "mmh_zerosum_f64",
     "mmh_rgzerosum_f64", "mmh_nsmooth_f64", "mmh_limiter_pass1_f64", "mmh_limiter_mask_f64",
     "mmh_limiter_poisson_f64", "mmh_load_f64", "mmh_load_dev", "mmh_iterate", "mmh_store_f64",
-    "mmh_outputs_f64", "mmh_state_dev",
+    "mmh_outputs_f64", "mmh_outputs_dev", "mmh_state_dev", "mmh_profile_start", "mmh_profile_stop",
 )
+
+# kernel kinds for the timing hooks
+K_GS, K_RESIDUAL, K_RESTRICT_RESID, K_METRIC, K_SMOOTH, K_PROLONG, K_RESTRICT = 1, 2, 3, 4, 5, 6, 7
+K_F32 = 256
 
 
 class MMHError(RuntimeError):
@@ -89,6 +94,18 @@ def strerror(code):
 
 def launch_count():
     return int(lib().mmh_launch_count())
+
+
+def profile_start(kind):
+    """Arm CUDA-event timing of every launch of one kernel kind."""
+    _chk(lib().mmh_profile_start(int(kind)), "profile_start")
+
+
+def profile_stop():
+    """Returns (launches, total device ms, cells processed) since profile_start."""
+    n, ms, cells = C.c_int(), C.c_double(), C.c_longlong()
+    _chk(lib().mmh_profile_stop(C.byref(n), C.byref(ms), C.byref(cells)), "profile_stop")
+    return n.value, ms.value, cells.value
 
 
 def _p(a):
@@ -282,6 +299,11 @@ class Context:
 
     def outputs(self, grad=None, delta=None):
         _chk(lib().mmh_outputs_f64(self._h, _p(grad), _p(delta)), "outputs")
+
+    def outputs_dev(self, d_grad, d_delta):
+        """Spectral outputs into device buffers (integer device addresses)."""
+        _chk(lib().mmh_outputs_dev(self._h, C.c_void_p(d_grad) if d_grad else None,
+                                   C.c_void_p(d_delta) if d_delta else None), "outputs_dev")
 
     def state_dev(self):
         a, b, c = C.c_void_p(), C.c_void_p(), C.c_void_p()

@@ -538,7 +538,7 @@ void rgzerosum(T* arr, const T* def, int n, T dx, bool* bad) {
 // ---------------------------------------------------------------------------
 struct MgCfg {
   int ng;          // NG: the top-level size (nrelax = 4*NG/n)
-  int sched;       // 0 = reference schedule, 1 = tolerance schedule
+  int sched;       // 0 = reference schedule, 1 = PCG to tolerance, 2 = repeated V-cycles to tolerance
   int nu1, nu2;    // sweeps per level in the tolerance schedule
   double tol;      // relative max-norm residual target (tolerance schedule)
   int maxcyc;      // V-cycle cap (tolerance schedule)
@@ -592,6 +592,129 @@ void mg_level(T* u, T* rhs, const T* def, const T* rho, int n, T dx, const MgCfg
   if (top) { st.r1 = r1; st.relaxerr = relaxerr; }
 }
 
+// ---------------------------------------------------------------------------
+// Exact, order-free dot product for the Krylov solver: each product a_i*b_i
+// (rounded to double) is scaled by 2^(96-E) with 2^E > max|a| * max|b|,
+// truncated to a 128-bit integer and summed exactly; the GPU does the same.
+// ---------------------------------------------------------------------------
+inline int dot_exp(double ma, double mb) { return std::ilogb(ma) + std::ilogb(mb) + 2; }
+inline i128 fx_scaled(double y) {
+  double a = std::fabs(y);
+  double q = std::floor(a * 5.42101086242752217e-20);
+  double rem = a - q * 18446744073709551616.0;
+  u128 v = ((u128)(uint64_t)q << 64) | (u128)(uint64_t)rem;
+  return y < 0 ? -(i128)v : (i128)v;
+}
+inline double fx_unscale(i128 s, int E) {
+  bool neg = s < 0;
+  u128 a = neg ? (u128)(-s) : (u128)s;
+  double r = std::ldexp((double)(uint64_t)(a >> 64), E - 32) + std::ldexp((double)(uint64_t)a, E - 96);
+  return neg ? -r : r;
+}
+template <class T>
+double dot_exact(const T* a, const T* b, i64 n, double ma, double mb) {
+  if (!(ma > 0) || !(mb > 0)) return 0.0;
+  int E = dot_exp(ma, mb);
+  i128 tot = 0;
+#pragma omp parallel
+  {
+    i128 loc = 0;
+#pragma omp for nowait
+    for (i64 i = 0; i < n; ++i) loc += fx_scaled(std::ldexp((double)a[i] * (double)b[i], 96 - E));
+#pragma omp critical
+    tot += loc;
+  }
+  return fx_unscale(tot, E);
+}
+template <class T>
+double absmax(const T* a, i64 n) {
+  double m = 0.0;
+#pragma omp parallel for reduction(max : m)
+  for (i64 i = 0; i < n; ++i) m = std::max(m, (double)std::fabs(a[i]));
+  return m;
+}
+
+// Flexible preconditioned conjugate gradients on L x = b, preconditioned by
+// one V-cycle (mg_level from a zero guess).  L is symmetric and, for a regular
+// mesh, negative definite on zero-mean fields; the Polak-Ribiere form of beta
+// keeps the iteration stable when the preconditioner is not exactly linear
+// (divergence guard, FP32 inner cycles on the GPU).
+template <class T>
+void pcg(T* x, const T* b, const T* def, const T* rho, int n, T dx, const MgCfg& cfg, MgStats& st, double rn) {
+  i64 n3 = (i64)n * n * n;
+  std::vector<T> coef(6 * n3), r(n3), z(n3), p(n3), q(n3);
+  metric(def, rho, n, dx, coef.data());
+  Op<T> op(coef.data(), n);
+  T di2 = T(1) / (dx * dx);
+  auto apply = [&](const T* v, T* out) {
+#pragma omp parallel for collapse(2)
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          T tdiag, t1, t2;
+          op.terms(v, i, j, k, tdiag, t1, t2);
+          i64 c = ID(i, j, k, n);
+          out[c] = (t1 + t2 + tdiag * v[c]) * di2;
+        }
+  };
+  auto precond = [&]() {
+    std::fill(z.begin(), z.end(), T(0));
+    MgStats sv;
+    mg_level(z.data(), r.data(), def, rho, n, dx, cfg, sv, true);
+    st.guards += sv.guards;
+    st.bad = st.bad || sv.bad;
+  };
+#pragma omp parallel for collapse(2)
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) r[ID(i, j, k, n)] = resid_cell(x, op, b, di2, i, j, k);
+  double rmax = absmax(r.data(), n3);
+  st.r1 = rmax;
+  if (!(rmax / rn > cfg.tol)) {
+    st.relaxerr = rmax;
+    st.resid_rel = rmax / rn;
+    return;
+  }
+  precond();
+  double zmax = absmax(z.data(), n3);
+  p = z;
+  double pmax = zmax;
+  double rz = dot_exact(r.data(), z.data(), n3, rmax, zmax);
+  for (int it = 1; it <= cfg.maxcyc; ++it) {
+    apply(p.data(), q.data());
+    double qmax = absmax(q.data(), n3);
+    double pq = dot_exact(p.data(), q.data(), n3, pmax, qmax);
+    double alpha = rz / pq;
+    T ta = (T)alpha;
+#pragma omp parallel for
+    for (i64 c = 0; c < n3; ++c) {
+      x[c] = x[c] + ta * p[c];
+      r[c] = r[c] - ta * q[c];
+    }
+    rmax = absmax(r.data(), n3);
+    st.vcycles = it;
+    if (!(rmax / rn > cfg.tol)) break;
+    precond();
+    zmax = absmax(z.data(), n3);
+    double zq = dot_exact(z.data(), q.data(), n3, zmax, qmax);
+    double rznew = dot_exact(r.data(), z.data(), n3, rmax, zmax);
+    double beta = -(alpha * zq) / rz;
+    rz = rznew;
+    T tb = (T)beta;
+#pragma omp parallel for
+    for (i64 c = 0; c < n3; ++c) p[c] = z[c] + tb * p[c];
+    pmax = absmax(p.data(), n3);
+  }
+  zerosum(x, n, &st.bad);
+#pragma omp parallel for collapse(2)
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) r[ID(i, j, k, n)] = resid_cell(x, op, b, di2, i, j, k);
+  rmax = absmax(r.data(), n3);
+  st.relaxerr = rmax;
+  st.resid_rel = rmax / rn;
+}
+
 // multigrid(u,rhs,defpot,ubig,dx,...) with iopt=2 (potential-flow solver).
 // rho is ubig(1,:,:,:).  rhs is modified in place (rgzerosum), as in the reference.
 template <class T>
@@ -609,10 +732,14 @@ void multigrid(T* u, T* rhs, const T* def, const T* rho, int n, T dx, const MgCf
     st.resid_rel = rn > 0 ? st.relaxerr / rn : 0;
     return;
   }
-  // Tolerance schedule: repeat V-cycles until the post-smoothing max-norm
-  // residual on the finest grid is below tol * max|rhs|.
   st.vcycles = 0;
   if (rn == T(0)) return;
+  if (cfg.sched == 1) {
+    pcg(u, rhs, def, rho, n, dx, cfg, st, (double)rn);
+    return;
+  }
+  // Repeated V-cycles until the post-smoothing max-norm residual on the
+  // finest grid is below tol * max|rhs|.
   for (int c = 0; c < cfg.maxcyc; ++c) {
     mg_level(u, rhs, def, rho, n, dx, cfg, st, true);
     st.vcycles++;

@@ -20,9 +20,10 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libmmh_oracle.so")
 _lib = None
 
-# reference schedule / tolerance schedule
+# reference schedule / PCG to tolerance / repeated V-cycles to tolerance
 SCHED_REF = 0
 SCHED_TOL = 1
+SCHED_VCYCLE = 2
 
 
 class Diag(C.Structure):

@@ -120,35 +120,38 @@ def test_multigrid_subgrid_entry(mmh, oracle, fields):
     assert np.array_equal(exp_u, ug)
 
 
-@pytest.mark.parametrize("n", [16, 32])
-def test_multigrid_tol_fp64_bitexact(mmh, oracle, fields, n):
+@pytest.mark.parametrize("n,sched", [(16, 1), (32, 1), (64, 1), (16, 2), (32, 2)])
+def test_multigrid_tol_fp64_bitexact(mmh, oracle, fields, n, sched):
+    """Tolerance schedules in FP64: flexible PCG (sched 1) and repeated V-cycles
+    (sched 2) reproduce the oracle bit for bit, iteration count included."""
     defpot, u = case(fields, n, 31, sigma=1.5)
     rho = np.asfortranarray(u[0])
     rng = np.random.default_rng(n + 1)
     rhs0 = np.asfortranarray(rng.standard_normal((n, n, n)) * 0.01)
     uo = np.zeros((n, n, n), order="F"); ro = rhs0.copy(order="F")
-    rc, do = oracle.multigrid(uo, ro, defpot, rho, 1.0, sched=oracle.SCHED_TOL, tol=1e-10, maxcyc=100,
-                              colour8=True)
+    rc, do = oracle.multigrid(uo, ro, defpot, rho, 1.0, sched=sched, tol=1e-10, maxcyc=200, colour8=True)
     ug = np.zeros((n, n, n), order="F"); rg = rhs0.copy(order="F")
-    with mmh.Context(n, schedule=mmh.MMH_SCHED_TOL, tol=1e-10, max_cycles=100) as ctx:
+    with mmh.Context(n, schedule=sched, tol=1e-10, max_cycles=200) as ctx:
         dg = ctx.multigrid(ug, rg, defpot, u, 1.0, n, n, n, 5)
     assert do["resid_rel"] <= 1e-10 and dg["resid_rel"] <= 1e-10
     assert do["vcycles"] == dg["vcycles"]
     assert np.array_equal(uo, ug)
+    assert do["resid_rel"] == dg["resid_rel"]
 
 
-@pytest.mark.parametrize("n", [16, 32, 64])
-def test_multigrid_mixed_converges(mmh, oracle, fields, n):
-    """Mixed form: FP32 V-cycles in an FP64 defect-correction loop reach the FP64
-    tolerance, and its potential agrees with the converged FP64 oracle."""
+@pytest.mark.parametrize("n,sched", [(16, 1), (32, 1), (64, 1), (32, 2)])
+def test_multigrid_mixed_converges(mmh, oracle, fields, n, sched):
+    """Mixed form: FP32 V-cycles inside FP64 PCG (sched 1) or an FP64
+    defect-correction loop (sched 2) reach the FP64 tolerance, and the
+    potential agrees with the converged FP64 oracle."""
     defpot, u = case(fields, n, 41, sigma=1.5)
     rho = np.asfortranarray(u[0])
     rng = np.random.default_rng(n + 2)
     rhs0 = np.asfortranarray(rng.standard_normal((n, n, n)) * 0.01)
     uo = np.zeros((n, n, n), order="F"); ro = rhs0.copy(order="F")
-    oracle.multigrid(uo, ro, defpot, rho, 1.0, sched=oracle.SCHED_TOL, tol=1e-12, maxcyc=200, colour8=True)
+    oracle.multigrid(uo, ro, defpot, rho, 1.0, sched=1, tol=1e-12, maxcyc=300, colour8=True)
     ug = np.zeros((n, n, n), order="F"); rg = rhs0.copy(order="F")
-    with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL, tol=1e-12, max_cycles=200) as ctx:
+    with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=sched, tol=1e-12, max_cycles=300) as ctx:
         dg = ctx.multigrid(ug, rg, defpot, u, 1.0, n, n, n, 5)
     assert dg["resid_rel"] <= 1e-12
     assert rel(ug, uo) <= 1e-9
