@@ -165,6 +165,42 @@ __global__ void k_metric(const T* __restrict__ def, const T* __restrict__ rho, i
 // ---------------------------------------------------------------------------
 // 19-point operator pieces (relaxplane gauss1.f90:950-980, calcresid :683-709)
 // ---------------------------------------------------------------------------
+// The 19 values of phi and 21 coefficient values one update reads.
+template <class T>
+struct Stencil {
+  T c, ip, im, jp, jm, kp, km;                      // phi: centre and faces
+  T ppk, mpk, pmk, mmk;                             // phi: in-plane edges (i+-1, j+-1, k)
+  T jpkp, jmkp, jpkm, jmkm, ipkp, imkp, ipkm, imkm;  // phi: edges through k+-1
+  T f1c, f1ip, f1im, f4c, f4jp, f4jm, f6c, f6kp, f6km;
+  T f2jp, f2jm, f2ip, f2im, f5kp, f5km, f5jp, f5jm, f3kp, f3km, f3ip, f3im;
+};
+
+// tdiag, t1 (face terms) and t2 (cross terms) in the reference's operand order.
+template <class T>
+__device__ __forceinline__ void op_eval(const Stencil<T>& s, T& tdiag, T& t1, T& t2) {
+  T b11p = (s.f1ip + s.f1c) / T(2);
+  T b11m = (s.f1im + s.f1c) / T(2);
+  T b22p = (s.f4jp + s.f4c) / T(2);
+  T b22m = (s.f4jm + s.f4c) / T(2);
+  T b33p = (s.f6kp + s.f6c) / T(2);
+  T b33m = (s.f6km + s.f6c) / T(2);
+  tdiag = -(b11p + b11m + b22p + b22m + b33p + b33m);
+  t1 = (b11p * s.ip + b11m * s.im + b22p * s.jp + b22m * s.jm + b33p * s.kp + b33m * s.km);
+  t2 = ((s.ppk - s.mpk) * s.f2jp
+        - (s.pmk - s.mmk) * s.f2jm
+        + (s.ppk - s.pmk) * s.f2ip
+        - (s.mpk - s.mmk) * s.f2im
+        + (s.jpkp - s.jmkp) * s.f5kp
+        - (s.jpkm - s.jmkm) * s.f5km
+        + (s.jpkp - s.jpkm) * s.f5jp
+        - (s.jmkp - s.jmkm) * s.f5jm
+        + (s.ipkp - s.imkp) * s.f3kp
+        - (s.ipkm - s.imkm) * s.f3km
+        + (s.ipkp - s.ipkm) * s.f3ip
+        - (s.imkp - s.imkm) * s.f3im) / T(4);
+}
+
+// Gather the stencil of cell (i,j,k) from global memory.
 template <class T>
 __device__ __forceinline__ void op_terms(const T* __restrict__ phi, const T* __restrict__ coef, int n, i64 n3, int i,
                                          int j, int k, T& tdiag, T& t1, T& t2) {
@@ -178,29 +214,21 @@ __device__ __forceinline__ void op_terms(const T* __restrict__ phi, const T* __r
   i64 c = IDX(i, j, k, n);
   i64 cip = IDX(ip, j, k, n), cim = IDX(im, j, k, n), cjp = IDX(i, jp, k, n), cjm = IDX(i, jm, k, n);
   i64 ckp = IDX(i, j, kp, n), ckm = IDX(i, j, km, n);
-  T b11p = (f1[cip] + f1[c]) / T(2);
-  T b11m = (f1[cim] + f1[c]) / T(2);
-  T b22p = (f4[cjp] + f4[c]) / T(2);
-  T b22m = (f4[cjm] + f4[c]) / T(2);
-  T b33p = (f6[ckp] + f6[c]) / T(2);
-  T b33m = (f6[ckm] + f6[c]) / T(2);
-  tdiag = -(b11p + b11m + b22p + b22m + b33p + b33m);
-  t1 = (b11p * phi[cip] + b11m * phi[cim] + b22p * phi[cjp] + b22m * phi[cjm] + b33p * phi[ckp] + b33m * phi[ckm]);
-  T ppk = phi[IDX(ip, jp, k, n)], mpk = phi[IDX(im, jp, k, n)], pmk = phi[IDX(ip, jm, k, n)], mmk = phi[IDX(im, jm, k, n)];
-  T jpkp = phi[IDX(i, jp, kp, n)], jmkp = phi[IDX(i, jm, kp, n)], jpkm = phi[IDX(i, jp, km, n)], jmkm = phi[IDX(i, jm, km, n)];
-  T ipkp = phi[IDX(ip, j, kp, n)], imkp = phi[IDX(im, j, kp, n)], ipkm = phi[IDX(ip, j, km, n)], imkm = phi[IDX(im, j, km, n)];
-  t2 = ((ppk - mpk) * f2[cjp]
-        - (pmk - mmk) * f2[cjm]
-        + (ppk - pmk) * f2[cip]
-        - (mpk - mmk) * f2[cim]
-        + (jpkp - jmkp) * f5[ckp]
-        - (jpkm - jmkm) * f5[ckm]
-        + (jpkp - jpkm) * f5[cjp]
-        - (jmkp - jmkm) * f5[cjm]
-        + (ipkp - imkp) * f3[ckp]
-        - (ipkm - imkm) * f3[ckm]
-        + (ipkp - ipkm) * f3[cip]
-        - (imkp - imkm) * f3[cim]) / T(4);
+  Stencil<T> s;
+  s.c = phi[c]; s.ip = phi[cip]; s.im = phi[cim]; s.jp = phi[cjp]; s.jm = phi[cjm]; s.kp = phi[ckp]; s.km = phi[ckm];
+  s.ppk = phi[IDX(ip, jp, k, n)]; s.mpk = phi[IDX(im, jp, k, n)]; s.pmk = phi[IDX(ip, jm, k, n)];
+  s.mmk = phi[IDX(im, jm, k, n)];
+  s.jpkp = phi[IDX(i, jp, kp, n)]; s.jmkp = phi[IDX(i, jm, kp, n)]; s.jpkm = phi[IDX(i, jp, km, n)];
+  s.jmkm = phi[IDX(i, jm, km, n)];
+  s.ipkp = phi[IDX(ip, j, kp, n)]; s.imkp = phi[IDX(im, j, kp, n)]; s.ipkm = phi[IDX(ip, j, km, n)];
+  s.imkm = phi[IDX(im, j, km, n)];
+  s.f1c = f1[c]; s.f1ip = f1[cip]; s.f1im = f1[cim];
+  s.f4c = f4[c]; s.f4jp = f4[cjp]; s.f4jm = f4[cjm];
+  s.f6c = f6[c]; s.f6kp = f6[ckp]; s.f6km = f6[ckm];
+  s.f2jp = f2[cjp]; s.f2jm = f2[cjm]; s.f2ip = f2[cip]; s.f2im = f2[cim];
+  s.f5kp = f5[ckp]; s.f5km = f5[ckm]; s.f5jp = f5[cjp]; s.f5jm = f5[cjm];
+  s.f3kp = f3[ckp]; s.f3km = f3[ckm]; s.f3ip = f3[cip]; s.f3im = f3[cim];
+  op_eval(s, tdiag, t1, t2);
 }
 
 // One colour of the 8-colour Gauss-Seidel sweep: planes with k%2 == kpar,
@@ -222,6 +250,86 @@ __global__ void k_gs_colour(T* __restrict__ phi, const T* __restrict__ rhs, cons
   op_terms(phi, coef, n, n3, i, j, k, tdiag, t1, t2);
   i64 c = IDX(i, j, k, n);
   phi[c] = (rhs[c] * dx2 - t1 - t2) / tdiag;
+}
+
+// All four in-plane colours of one plane P (k%2 == kpar) for a TX x TY tile,
+// staged in shared memory with a 4-cell halo; colour q = 2*io + jo is applied
+// on the tile grown by 3-q cells, so the interior ends exactly as after the
+// four global colour phases (cells of one colour never read each other).
+// Neighbour planes P+-1 are not written during a half sweep.  Needs n >= TX+8
+// and n >= TY+8.  Shared-memory slots: 0 phi(P), 1 rhs(P), 2-7 f1..f6(P),
+// 8/9 phi(P-1)/phi(P+1), 10-12 f3,f5,f6(P-1), 13-15 f3,f5,f6(P+1).
+template <class T, int TX, int TY>
+__global__ void __launch_bounds__(256) k_gs_plane(T* __restrict__ phi, const T* __restrict__ rhs,
+                                                  const T* __restrict__ coef, int n, T dx2, int kpar) {
+  constexpr int HB = 4, W = TX + 2 * HB, HT = TY + 2 * HB, S = W * HT;
+  extern __shared__ unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  const i64 n2 = (i64)n * n, n3 = n2 * n;
+  const int i0 = blockIdx.x * TX - HB, j0 = blockIdx.y * TY - HB, k = 2 * blockIdx.z + kpar;
+  const int kmn = wm(k, n), kpn = wp(k, n);
+  for (int e = threadIdx.x; e < S; e += blockDim.x) {
+    int x = e % W, y = e / W;
+    int gi = i0 + x, gj = j0 + y;
+    gi += (gi < 0) ? n : ((gi >= n) ? -n : 0);
+    gj += (gj < 0) ? n : ((gj >= n) ? -n : 0);
+    i64 b = (i64)gi + (i64)n * gj;
+    i64 cP = b + n2 * k, cm = b + n2 * kmn, cp = b + n2 * kpn;
+    sm[0 * S + e] = phi[cP];
+    sm[1 * S + e] = rhs[cP];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) sm[(2 + f) * S + e] = coef[f * n3 + cP];
+    sm[8 * S + e] = phi[cm];
+    sm[9 * S + e] = phi[cp];
+    sm[10 * S + e] = coef[2 * n3 + cm];
+    sm[11 * S + e] = coef[4 * n3 + cm];
+    sm[12 * S + e] = coef[5 * n3 + cm];
+    sm[13 * S + e] = coef[2 * n3 + cp];
+    sm[14 * S + e] = coef[4 * n3 + cp];
+    sm[15 * S + e] = coef[5 * n3 + cp];
+  }
+  __syncthreads();
+  const T* sP = sm;
+  const T* sR = sm + S;
+  const T* F1 = sm + 2 * S;
+  const T* F2 = sm + 3 * S;
+  const T* F3 = sm + 4 * S;
+  const T* F4 = sm + 5 * S;
+  const T* F5 = sm + 6 * S;
+  const T* F6 = sm + 7 * S;
+  const T* sKm = sm + 8 * S;
+  const T* sKp = sm + 9 * S;
+#pragma unroll 1
+  for (int q = 0; q < 4; ++q) {
+    const int io = q >> 1, jo = q & 1, r = 3 - q;
+    const int xs = HB - r + ((HB - r) & 1 ? (io ? 0 : 1) : io);
+    const int ys = HB - r + ((HB - r) & 1 ? (jo ? 0 : 1) : jo);
+    const int nx = (HB + TX + r - xs + 1) / 2, ny = (HB + TY + r - ys + 1) / 2;
+    for (int e = threadIdx.x; e < nx * ny; e += blockDim.x) {
+      const int x = xs + 2 * (e % nx), y = ys + 2 * (e / nx);
+      const int c = y * W + x;
+      Stencil<T> st;
+      st.c = sP[c]; st.ip = sP[c + 1]; st.im = sP[c - 1]; st.jp = sP[c + W]; st.jm = sP[c - W];
+      st.kp = sKp[c]; st.km = sKm[c];
+      st.ppk = sP[c + W + 1]; st.mpk = sP[c + W - 1]; st.pmk = sP[c - W + 1]; st.mmk = sP[c - W - 1];
+      st.jpkp = sKp[c + W]; st.jmkp = sKp[c - W]; st.jpkm = sKm[c + W]; st.jmkm = sKm[c - W];
+      st.ipkp = sKp[c + 1]; st.imkp = sKp[c - 1]; st.ipkm = sKm[c + 1]; st.imkm = sKm[c - 1];
+      st.f1c = F1[c]; st.f1ip = F1[c + 1]; st.f1im = F1[c - 1];
+      st.f4c = F4[c]; st.f4jp = F4[c + W]; st.f4jm = F4[c - W];
+      st.f6c = F6[c]; st.f6kp = sm[15 * S + c]; st.f6km = sm[12 * S + c];
+      st.f2jp = F2[c + W]; st.f2jm = F2[c - W]; st.f2ip = F2[c + 1]; st.f2im = F2[c - 1];
+      st.f5kp = sm[14 * S + c]; st.f5km = sm[11 * S + c]; st.f5jp = F5[c + W]; st.f5jm = F5[c - W];
+      st.f3kp = sm[13 * S + c]; st.f3km = sm[10 * S + c]; st.f3ip = F3[c + 1]; st.f3im = F3[c - 1];
+      T tdiag, t1, t2;
+      op_eval(st, tdiag, t1, t2);
+      sm[c] = (sR[c] * dx2 - t1 - t2) / tdiag;
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
+    int x = HB + e % TX, y = HB + e / TX;
+    phi[(i64)(i0 + x) + (i64)n * (j0 + y) + n2 * k] = sm[y * W + x];
+  }
 }
 
 // Residual r = rhs - L[phi] on every cell (calcresid), max-norm into maxbits.

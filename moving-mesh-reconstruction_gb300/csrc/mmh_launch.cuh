@@ -18,10 +18,35 @@ void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_
   count_launch();
 }
 
+template <class T> struct GsTile;
+template <> struct GsTile<float> { static const int TX = 32, TY = 16; };
+template <> struct GsTile<double> { static const int TX = 32, TY = 8; };
+
+// nsweeps 8-colour Gauss-Seidel sweeps.  Grids of 64^3 and up run one fused
+// launch per half sweep (all in-plane colours of every plane of one parity);
+// smaller grids run one launch per colour.
 template <class T>
 void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, cudaStream_t s) {
   i64 h3 = (i64)(n / 2) * (n / 2) * (n / 2);
   T dx2 = dx * dx;
+  if (n >= 64) {
+    constexpr int TX = GsTile<T>::TX, TY = GsTile<T>::TY;
+    const size_t smem = sizeof(T) * 16 * (TX + 8) * (TY + 8);
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_gs_plane<T, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      attr = true;
+    }
+    dim3 grid(n / TX, n / TY, n / 2);
+    for (int sw = 0; sw < nsweeps; ++sw)
+      for (int kpar = 0; kpar < 2; ++kpar) {
+        prof_begin(kk<T>(KK_GS), s, 4 * h3);
+        k_gs_plane<T, TX, TY><<<grid, 256, smem, s>>>(phi, rhs, coef, n, dx2, kpar);
+        prof_end(kk<T>(KK_GS), s);
+        count_launch();
+      }
+    return;
+  }
   unsigned g = grid_of(h3, kBlock);
   for (int sw = 0; sw < nsweeps; ++sw)
     for (int kpar = 0; kpar < 2; ++kpar)

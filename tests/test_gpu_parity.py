@@ -41,7 +41,8 @@ def test_metric_bitexact(mmh, oracle, fields, n):
 
 
 @pytest.mark.parametrize("n,nrelax,iopt", [(8, 2, 19), (16, 4, 19), (32, 4, 19), (32, 8, 19), (16, 3, 18),
-                                           (32, 1, 19), (16, 16, 19), (4, 32, 18), (16, 0, 19)])
+                                           (32, 1, 19), (16, 16, 19), (4, 32, 18), (16, 0, 19), (64, 4, 19),
+                                           (64, 2, 18), (128, 4, 19)])
 def test_relax_bitexact(mmh, oracle, fields, n, nrelax, iopt):
     """relax(): the literal r1lax plane schedule of the oracle vs the GPU's 8-colour sweeps."""
     defpot, u = case(fields, n, 5 + n)
@@ -83,7 +84,7 @@ def test_small_ops_bitexact(mmh, oracle, fields, n):
         assert np.array_equal(x, y)
 
 
-@pytest.mark.parametrize("n", [8, 16, 32, 64])
+@pytest.mark.parametrize("n", [8, 16, 32, 64, 128])
 def test_multigrid_ref_bitexact(mmh, oracle, fields, n):
     """multigrid(...) with the reference schedule (one V-cycle, 4*NG/n sweeps)."""
     defpot, u = case(fields, n, 21, sigma=1.5)
@@ -235,9 +236,11 @@ def test_calcdefp_ref(mmh, oracle, fields, n, sigma, amp):
         assert rel(dg, do_) <= TOL_SPECTRAL
 
 
-@pytest.mark.parametrize("n,niter", [(16, 3), (32, 2)])
+@pytest.mark.parametrize("n,niter", [(16, 3), (32, 3), (64, 2)])
 def test_iterations_ref(mmh, oracle, fields, n, niter):
-    defpot, u = fields.initial_state(n, sigma=1.5, seed=61)
+    """Whole deformation iterations (calcdefp, def += defp, relaxing) on a
+    field the reference algorithm handles stably (sigma_lnrho = 1)."""
+    defpot, u = fields.initial_state(n, sigma=1.0, seed=61)
     do_, uo = defpot, u
     for _ in range(niter):
         do_, uo, _, _, _ = oracle.iteration(do_, uo, sched=oracle.SCHED_REF)
