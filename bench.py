@@ -193,6 +193,22 @@ def reference_arm(args):
     return 0
 
 
+def replica_seed(base, rank):
+    """Each rank reconstructs its own realisation (replicas; no data exchange)."""
+    return base + rank
+
+
+def max_over_ranks(value, device=None):
+    """Max of a per-rank number over all ranks (the job's time is the slowest rank's)."""
+    import torch
+    import torch.distributed as tdist
+    if not (tdist.is_available() and tdist.is_initialized()) or tdist.get_world_size() == 1:
+        return value
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def workload_config(args):
     return {
         "workload": f"{args.n}^3 lognormal density, sigma_lnrho={args.sigma}, P(k)~k^-1.5, smoothed at 2 cells, "
@@ -251,7 +267,7 @@ def main():
     dev = torch.device("cuda", local)
     n = args.n
     n3 = n ** 3
-    seed = args.seed + rank  # independent realisation per rank
+    seed = replica_seed(args.seed, rank)
 
     rho_np = fields.lognormal_density(n, sigma=args.sigma, seed=seed)
     rho_dev = torch.from_numpy(rho_np.ravel(order="F")).to(dev)
@@ -290,11 +306,7 @@ def main():
         e1.synchronize()
         prof = mmh.profile_stop() if profile_kind else None
         barrier()
-        ms = e0.elapsed_time(e1) / steps
-        if dist:
-            t = torch.tensor([ms], device=dev)
-            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(e0.elapsed_time(e1) / steps, dev)
         return ms, diags, mmh.launch_count() - launches0, prof
 
     # ---- mixed (headline value) ----
@@ -338,7 +350,7 @@ def main():
             e1.record(stream)
         e1.synchronize()
         barrier()
-        e2e_ms = e0.elapsed_time(e1) / args.e2e_steps
+        e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.e2e_steps, dev)
     ctx.close()
 
     # ---- FP64 form ----

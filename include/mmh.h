@@ -59,6 +59,8 @@ typedef struct mmh_config {
   double tol;     /* relative max-norm residual target, tolerance schedule */
   int device;     /* CUDA device ordinal */
   void* stream;   /* cudaStream_t to run on; NULL: the context creates its own */
+  int precond_guards; /* MMH_SCHED_TOL: apply the coarse-level divergence guards inside the
+                         preconditioner V-cycle (default 0: the preconditioner stays linear) */
 } mmh_config;
 
 /* Diagnostics: the quantities the Fortran prints (mg64.f90:43-45,

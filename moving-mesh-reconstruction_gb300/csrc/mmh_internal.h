@@ -26,7 +26,7 @@ template <class T> inline int kk(int base) { return base | (sizeof(T) == 4 ? KK_
 // Launchers, instantiated for double (mmh_kernels_f64.cu, no FMA contraction)
 // and float (mmh_kernels_f32.cu).
 template <class T> void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_t s);
-template <class T> void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, cudaStream_t s);
+template <class T> void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, T* scratch, cudaStream_t s);
 template <class T>
 void launch_residual(const T* phi, const T* rhs, const T* coef, int n, T dx, T* r, float* r32,
                      unsigned long long* maxbits, cudaStream_t s);

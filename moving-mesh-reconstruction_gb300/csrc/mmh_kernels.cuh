@@ -256,11 +256,14 @@ __global__ void k_gs_colour(T* __restrict__ phi, const T* __restrict__ rhs, cons
 // staged in shared memory with a 4-cell halo; colour q = 2*io + jo is applied
 // on the tile grown by 3-q cells, so the interior ends exactly as after the
 // four global colour phases (cells of one colour never read each other).
-// Neighbour planes P+-1 are not written during a half sweep.  Needs n >= TX+8
+// The half sweep reads its own planes from src, the neighbour planes P+-1
+// (not written during the half sweep) from nbr, and writes dst != src, so no
+// tile can read a halo that another tile has already updated.  Needs n >= TX+8
 // and n >= TY+8.  Shared-memory slots: 0 phi(P), 1 rhs(P), 2-7 f1..f6(P),
 // 8/9 phi(P-1)/phi(P+1), 10-12 f3,f5,f6(P-1), 13-15 f3,f5,f6(P+1).
 template <class T, int TX, int TY>
-__global__ void __launch_bounds__(256) k_gs_plane(T* __restrict__ phi, const T* __restrict__ rhs,
+__global__ void __launch_bounds__(256) k_gs_plane(const T* __restrict__ src, const T* __restrict__ nbr,
+                                                  T* __restrict__ dst, const T* __restrict__ rhs,
                                                   const T* __restrict__ coef, int n, T dx2, int kpar) {
   constexpr int HB = 4, W = TX + 2 * HB, HT = TY + 2 * HB, S = W * HT;
   extern __shared__ unsigned char smem_raw[];
@@ -275,12 +278,12 @@ __global__ void __launch_bounds__(256) k_gs_plane(T* __restrict__ phi, const T* 
     gj += (gj < 0) ? n : ((gj >= n) ? -n : 0);
     i64 b = (i64)gi + (i64)n * gj;
     i64 cP = b + n2 * k, cm = b + n2 * kmn, cp = b + n2 * kpn;
-    sm[0 * S + e] = phi[cP];
+    sm[0 * S + e] = src[cP];
     sm[1 * S + e] = rhs[cP];
 #pragma unroll
     for (int f = 0; f < 6; ++f) sm[(2 + f) * S + e] = coef[f * n3 + cP];
-    sm[8 * S + e] = phi[cm];
-    sm[9 * S + e] = phi[cp];
+    sm[8 * S + e] = nbr[cm];
+    sm[9 * S + e] = nbr[cp];
     sm[10 * S + e] = coef[2 * n3 + cm];
     sm[11 * S + e] = coef[4 * n3 + cm];
     sm[12 * S + e] = coef[5 * n3 + cm];
@@ -328,7 +331,7 @@ __global__ void __launch_bounds__(256) k_gs_plane(T* __restrict__ phi, const T* 
   }
   for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
     int x = HB + e % TX, y = HB + e / TX;
-    phi[(i64)(i0 + x) + (i64)n * (j0 + y) + n2 * k] = sm[y * W + x];
+    dst[(i64)(i0 + x) + (i64)n * (j0 + y) + n2 * k] = sm[y * W + x];
   }
 }
 

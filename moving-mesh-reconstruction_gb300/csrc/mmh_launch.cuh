@@ -26,7 +26,7 @@ template <> struct GsTile<double> { static const int TX = 32, TY = 8; };
 // launch per half sweep (all in-plane colours of every plane of one parity);
 // smaller grids run one launch per colour.
 template <class T>
-void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, cudaStream_t s) {
+void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, T* scratch, cudaStream_t s) {
   i64 h3 = (i64)(n / 2) * (n / 2) * (n / 2);
   T dx2 = dx * dx;
   if (n >= 64) {
@@ -38,13 +38,21 @@ void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nswe
       attr = true;
     }
     dim3 grid(n / TX, n / TY, n / 2);
-    for (int sw = 0; sw < nsweeps; ++sw)
+    // double buffer: a sweep reads a and leaves the swept field in b
+    T* a = phi;
+    T* b = scratch;
+    for (int sw = 0; sw < nsweeps; ++sw) {
       for (int kpar = 0; kpar < 2; ++kpar) {
         prof_begin(kk<T>(KK_GS), s, 4 * h3);
-        k_gs_plane<T, TX, TY><<<grid, 256, smem, s>>>(phi, rhs, coef, n, dx2, kpar);
+        k_gs_plane<T, TX, TY><<<grid, 256, smem, s>>>(a, kpar == 0 ? a : b, b, rhs, coef, n, dx2, kpar);
         prof_end(kk<T>(KK_GS), s);
         count_launch();
       }
+      T* t = a;
+      a = b;
+      b = t;
+    }
+    if (a != phi) cudaMemcpyAsync(phi, a, sizeof(T) * (size_t)n * n * n, cudaMemcpyDeviceToDevice, s);
     return;
   }
   unsigned g = grid_of(h3, kBlock);
@@ -186,7 +194,7 @@ void launch_usum_flag(const unsigned long long* acc, int* flag, cudaStream_t s) 
 
 #define MMH_INSTANTIATE(T)                                                                                          \
   template void launch_metric<T>(const T*, const T*, int, T, T*, cudaStream_t);                                   \
-  template void launch_gs_sweeps<T>(T*, const T*, const T*, int, T, int, cudaStream_t);                           \
+  template void launch_gs_sweeps<T>(T*, const T*, const T*, int, T, int, T*, cudaStream_t);                         \
   template void launch_residual<T>(const T*, const T*, const T*, int, T, T*, float*, unsigned long long*,          \
                                    cudaStream_t);                                                                   \
   template void launch_restrict_resid<T>(const T*, int, int, T*, cudaStream_t);                                   \

@@ -177,7 +177,7 @@ int relax_level(mmh_ctx* c, int l, int nrelax, int mode, unsigned long long* max
   Hier<T>& H = hier<T>(c);
   int n = c->nl[l];
   T dx = T(double(1 << l));
-  launch_gs_sweeps<T>(H.u[l], H.rhs[l], H.coef[l], n, dx, nrelax, c->s);
+  launch_gs_sweeps<T>(H.u[l], H.rhs[l], H.coef[l], n, dx, nrelax, H.r[l], c->s);
   CK(cudaMemsetAsync(maxslot, 0, 8, c->s));
   launch_residual<T>(H.u[l], H.rhs[l], H.coef[l], n, dx, mode == 3 ? H.r[l] : (T*)nullptr, nullptr, maxslot, c->s);
   if (mode == 3) launch_restrict_resid<T>(H.r[l], n, special_plane(nrelax, n), H.rhs[l + 1], c->s);
@@ -209,6 +209,7 @@ int vcycle(mmh_ctx* c, int l) {
   int n = c->nl[l];
   bool ref = c->cfg.schedule == MMH_SCHED_REF;
   bool at_ng = (n == c->n);
+  bool guard = !at_ng && (c->cfg.schedule != MMH_SCHED_TOL || c->cfg.precond_guards);
   if (n == 4) {
     if (std::is_same<T, float>::value) {
       // coarsest grid solved in FP64
@@ -222,7 +223,7 @@ int vcycle(mmh_ctx* c, int l) {
     }
     RET(relax_level<T>(c, l, 32, 2, &c->sc->r1bits[l]));
     RET(relax_level<T>(c, l, 32, 2, &c->sc->errbits[l]));
-    return guard_or_zerosum<T>(c, l, 1.001, 1.e-5, !at_ng);
+    return guard_or_zerosum<T>(c, l, 1.001, 1.e-5, guard);
   }
   int nrelax = ref ? 4 * c->n / n : c->cfg.nu1;
   int nrelax2 = ref ? 4 * c->n / n : c->cfg.nu2;
@@ -232,7 +233,7 @@ int vcycle(mmh_ctx* c, int l) {
   RET(vcycle<T>(c, l + 1));
   launch_prolong_add<T>(H.u[l], H.u[l + 1], n, c->s);
   RET(relax_level<T>(c, l, nrelax2, 2, &c->sc->errbits[l]));
-  return guard_or_zerosum<T>(c, l, 1.0, -HUGE_VAL, !at_ng);
+  return guard_or_zerosum<T>(c, l, 1.0, -HUGE_VAL, guard);
 }
 
 int vcycle_fp64(mmh_ctx* c, int l) { return vcycle<double>(c, l); }
@@ -690,6 +691,7 @@ void mmh_config_default(mmh_config* cfg, int n) {
   cfg->tol = 1e-10;
   cfg->device = 0;
   cfg->stream = nullptr;
+  cfg->precond_guards = 0;
 }
 
 const char* mmh_strerror(int code) {
@@ -892,7 +894,7 @@ int mmh_relax_f64(mmh_ctx* c, double* arr, double* resid, const double* rhs, con
   RET(upload(c, deformpot, c->defl[l], n3));
   RET(upload(c, rho, c->rhol[l], n3));
   launch_metric<double>(c->defl[l], c->rhol[l], n, dx, c->h64.coef[l], c->s);
-  launch_gs_sweeps<double>(c->h64.u[l], c->h64.rhs[l], c->h64.coef[l], n, dx, nrelax, c->s);
+  launch_gs_sweeps<double>(c->h64.u[l], c->h64.rhs[l], c->h64.coef[l], n, dx, nrelax, c->h64.r[l], c->s);
   CK(cudaMemsetAsync(c->sc->errbits, 0, 8, c->s));
   if (ir != 0) {
     launch_residual<double>(c->h64.u[l], c->h64.rhs[l], c->h64.coef[l], n, dx, ir == 3 ? c->h64.r[l] : nullptr,

@@ -53,7 +53,8 @@ class MMHError(RuntimeError):
 
 class Config(C.Structure):
     _fields_ = [("n", C.c_int), ("precision", C.c_int), ("schedule", C.c_int), ("nu1", C.c_int), ("nu2", C.c_int),
-                ("max_cycles", C.c_int), ("tol", C.c_double), ("device", C.c_int), ("stream", C.c_void_p)]
+                ("max_cycles", C.c_int), ("tol", C.c_double), ("device", C.c_int), ("stream", C.c_void_p),
+                ("precond_guards", C.c_int)]
 
 
 class Diag(C.Structure):
@@ -136,13 +137,14 @@ class Context:
     """Device state for one grid size NG (the Fortran's compile-time NG)."""
 
     def __init__(self, n, precision=MMH_FP64, schedule=MMH_SCHED_REF, nu1=2, nu2=2, tol=1e-10, max_cycles=200,
-                 device=0, stream=None):
+                 device=0, stream=None, precond_guards=False):
         L = lib()
         cfg = Config()
         L.mmh_config_default(C.byref(cfg), int(n))
         cfg.precision, cfg.schedule = int(precision), int(schedule)
         cfg.nu1, cfg.nu2, cfg.tol, cfg.max_cycles, cfg.device = int(nu1), int(nu2), float(tol), int(max_cycles), int(device)
         cfg.stream = stream
+        cfg.precond_guards = int(bool(precond_guards))
         self.cfg = cfg
         self.n = int(n)
         self._h = C.c_void_p()

@@ -543,6 +543,7 @@ struct MgCfg {
   double tol;      // relative max-norm residual target (tolerance schedule)
   int maxcyc;      // V-cycle cap (tolerance schedule)
   bool colour8;    // execute sweeps in 8-colour order instead of the literal schedule
+  bool guards = true;  // divergence guards of the coarse levels (mgtemplate.f90:46-55)
 };
 
 struct MgStats {
@@ -563,7 +564,7 @@ void mg_level(T* u, T* rhs, const T* def, const T* rho, int n, T dx, const MgCfg
     std::vector<T> dummy(8);
     relax(u, dummy.data(), rhs, op, r1, dx, 32, 2 * 8 + 2, cfg.colour8);
     relax(u, dummy.data(), rhs, op, relaxerr, dx, 32, 2 * 8 + 2, cfg.colour8);
-    if (n != cfg.ng && relaxerr > r1 * T(1.001) && r1 > T(1.E-5)) {
+    if (cfg.guards && n != cfg.ng && relaxerr > r1 * T(1.001) && r1 > T(1.E-5)) {
       std::fill(u, u + n3, T(0));
       st.guards++;
     } else {
@@ -583,7 +584,7 @@ void mg_level(T* u, T* rhs, const T* def, const T* rho, int n, T dx, const MgCfg
   mg_level(uhalf.data(), rhshalf.data(), defhalf.data(), rhohalf.data(), nh, dx * T(2), cfg, st, false);
   prolong_add(u, uhalf.data(), n);
   relax(u, rhshalf.data(), rhs, op, relaxerr, dx, nrelax2, 2 * 8 + 2, cfg.colour8);
-  if (n != cfg.ng && relaxerr > r1) {
+  if (cfg.guards && n != cfg.ng && relaxerr > r1) {
     std::fill(u, u + n3, T(0));
     st.guards++;
   } else {
@@ -1329,7 +1330,8 @@ MgCfg make_cfg(int n, int sched, int nu1, int nu2, double tol, int maxcyc, int c
   c.nu2 = nu2;
   c.tol = tol;
   c.maxcyc = maxcyc;
-  c.colour8 = colour8 != 0;
+  c.colour8 = (colour8 & 1) != 0;
+  c.guards = (colour8 & 2) == 0;  // bit 1 of the flags word switches the guards off
   return c;
 }
 

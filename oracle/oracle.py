@@ -146,14 +146,23 @@ def fxsum(a):
     return fn(_p(a), C.c_longlong(a.size))
 
 
-def multigrid(u, rhs, defpot, rho, dx=1.0, sched=SCHED_REF, nu1=2, nu2=2, tol=1e-10, maxcyc=50, colour8=False):
+def _flags(sched, colour8, precond_guards):
+    """bit 0: 8-colour order; bit 1: no divergence guards (the PCG preconditioner's default)."""
+    f = 1 if colour8 else 0
+    if sched == SCHED_TOL and not precond_guards:
+        f |= 2
+    return f
+
+
+def multigrid(u, rhs, defpot, rho, dx=1.0, sched=SCHED_REF, nu1=2, nu2=2, tol=1e-10, maxcyc=50, colour8=False,
+              precond_guards=False):
     """multigrid(u, rhs, defpot, ubig, dx, ...) with iopt=2; u and rhs updated in place."""
     dt = u.dtype
     assert u.flags.f_contiguous and rhs.flags.f_contiguous and rhs.dtype == dt
     d = Diag()
     rc = getattr(lib(), "orc_multigrid_" + _sfx(dt))(
         _p(u), _p(rhs), _p(_f(defpot, dt)), _p(_f(rho, dt)), u.shape[0], _scalar(dt, dx), int(sched), int(nu1),
-        int(nu2), C.c_double(tol), int(maxcyc), int(colour8), C.byref(d))
+        int(nu2), C.c_double(tol), int(maxcyc), _flags(sched, colour8, precond_guards), C.byref(d))
     return rc, d.as_dict()
 
 
@@ -217,7 +226,7 @@ def relaxing(u, defpot, defp, dt_=1.0):
 
 
 def calcdefp(defpot, u, dtold=1.0, dtaumesh=1.0, sched=SCHED_REF, nu1=2, nu2=2, tol=1e-10, maxcyc=50,
-             colour8=False):
+             colour8=False, precond_guards=False):
     """calcdefp(defp, tmp, tmp2, def, u, dtold, dtaumesh, nfluid): returns (defp, masks, diag)."""
     dt = defpot.dtype
     n = defpot.shape[0]
@@ -227,7 +236,8 @@ def calcdefp(defpot, u, dtold=1.0, dtaumesh=1.0, sched=SCHED_REF, nu1=2, nu2=2, 
     d = Diag()
     rc = getattr(lib(), "orc_calcdefp_" + _sfx(dt))(
         _p(defp), _p(_f(defpot, dt)), _p(u), u.shape[0], n, _scalar(dt, dtold), _scalar(dt, dtaumesh), int(sched),
-        int(nu1), int(nu2), C.c_double(tol), int(maxcyc), int(colour8), _p(m[0]), _p(m[1]), _p(m[2]), C.byref(d))
+        int(nu1), int(nu2), C.c_double(tol), int(maxcyc), _flags(sched, colour8, precond_guards), _p(m[0]),
+        _p(m[1]), _p(m[2]), C.byref(d))
     return defp, {"expand": m[0], "compress1": m[1], "compress2": m[2]}, d.as_dict(), rc
 
 
