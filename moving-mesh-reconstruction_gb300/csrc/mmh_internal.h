@@ -81,14 +81,16 @@ struct PcgDev {
   unsigned long long rbits, zbits, pbits, qbits;
   double rz, pq, alpha, beta;
 };
-void launch_apply(const double* p, const double* coef, int n, double dx, double* q, unsigned long long* qbits,
-                  cudaStream_t s);
-void launch_dot(const double* a, const double* b, i64 count, const unsigned long long* abits,
-                const unsigned long long* bbits, unsigned long long* acc, cudaStream_t s);
-void launch_pcg_update(double* x, double* r, const double* p, const double* q, i64 count, const double* alpha,
-                       unsigned long long* rbits, cudaStream_t s);
-void launch_pcg_pupdate(double* p, const double* z, i64 count, const double* beta, unsigned long long* pbits,
-                        cudaStream_t s);
+template <class T>
+void launch_apply(const T* p, const T* coef, int n, T dx, T* q, unsigned long long* qbits, cudaStream_t s);
+template <class T>
+void launch_dot(const T* a, const T* b, i64 count, const unsigned long long* abits, const unsigned long long* bbits,
+                unsigned long long* acc, cudaStream_t s);
+template <class T>
+void launch_pcg_update(T* x, T* r, const T* p, const T* q, i64 count, const double* alpha, unsigned long long* rbits,
+                       cudaStream_t s);
+template <class T>
+void launch_pcg_pupdate(T* p, const T* z, i64 count, const double* beta, unsigned long long* pbits, cudaStream_t s);
 void launch_pcg_scalar(PcgDev* st, int stage, cudaStream_t s);
 
 }  // namespace mmh

@@ -35,13 +35,26 @@ __device__ __forceinline__ void cell_of(i64 t, int n, int& i, int& j, int& k) {
 // ---------------------------------------------------------------------------
 // Exact 128-bit fixed-point sum (2^-64 resolution, |term| < 2^32), matching the
 // oracle: sums do not depend on launch shape or order.
-__device__ __forceinline__ __int128 fx_of(double x) {
-  double a = fabs(x) * 18446744073709551616.0;
-  double q = floor(a * 5.42101086242752217e-20);
-  double rem = a - q * 18446744073709551616.0;
-  unsigned __int128 v = ((unsigned __int128)__double2ull_rz(q) << 64) | (unsigned __int128)__double2ull_rz(rem);
-  return x < 0 ? -(__int128)v : (__int128)v;
+// trunc(x * 2^sh) as a 128-bit integer from the bits of x (integer operations
+// only; valid for finite x with |x * 2^sh| < 2^126).
+__device__ __forceinline__ __int128 fx_bits(double x, int sh) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  int ex = (int)((b >> 52) & 0x7FF);
+  unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  if (ex == 0) {
+    if (m == 0) return 0;
+    ex = 1;
+  } else {
+    m |= (1ull << 52);
+  }
+  int s = ex - 1075 + sh;
+  unsigned __int128 v;
+  if (s >= 0) v = (unsigned __int128)m << s;
+  else if (s > -64) v = (unsigned __int128)(m >> (-s));
+  else v = 0;
+  return (b >> 63) ? -(__int128)v : (__int128)v;
 }
+__device__ __forceinline__ __int128 fx_of(double x) { return fx_bits(x, 64); }
 __device__ __forceinline__ double fx_to(unsigned long long lo, unsigned long long hi) {
   __int128 s = (__int128)(((unsigned __int128)hi << 64) | (unsigned __int128)lo);
   bool neg = s < 0;
@@ -250,6 +263,29 @@ __global__ void k_gs_colour(T* __restrict__ phi, const T* __restrict__ rhs, cons
   op_terms(phi, coef, n, n3, i, j, k, tdiag, t1, t2);
   i64 c = IDX(i, j, k, n);
   phi[c] = (rhs[c] * dx2 - t1 - t2) / tdiag;
+}
+
+// nsweeps full 8-colour sweeps of a small grid (n <= 16) by one CTA: the
+// colour phases are separated by block barriers instead of kernel launches.
+template <class T>
+__global__ void __launch_bounds__(512) k_gs_small(T* __restrict__ phi, const T* __restrict__ rhs,
+                                                   const T* __restrict__ coef, int n, T dx2, int nsweeps) {
+  const int h = n >> 1;
+  const int tot = h * h * h;
+  const i64 n3 = (i64)n * n * n;
+  for (int sw = 0; sw < nsweeps; ++sw)
+    for (int q = 0; q < 8; ++q) {
+      const int kpar = q >> 2, io = (q >> 1) & 1, jo = q & 1;
+      for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+        int ti = t % h, tj = (t / h) % h, tk = t / (h * h);
+        int i = 2 * ti + io, j = 2 * tj + jo, k = 2 * tk + kpar;
+        T tdiag, t1, t2;
+        op_terms(phi, coef, n, n3, i, j, k, tdiag, t1, t2);
+        i64 c = IDX(i, j, k, n);
+        phi[c] = (rhs[c] * dx2 - t1 - t2) / tdiag;
+      }
+      __syncthreads();
+    }
 }
 
 // All four in-plane colours of one plane P (k%2 == kpar) for a TX x TY tile,

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "mmh_launch.cuh"
+#include "mmh_pcg.cuh"
 #include "mmh_phys.cuh"
 
 namespace mmh {
@@ -629,20 +630,13 @@ void launch_extract_density_d(const double* u, int nf, i64 n3, double* rho, int*
 
 }  // namespace mmh
 
+
 // ---------------------------------------------------------------------------
-// Krylov (flexible PCG) building blocks, FP64.  Dot products are exact and
-// order free: terms a_i*b_i are scaled by 2^(96-E), 2^E > max|a|*max|b|,
-// truncated to 128-bit integers and summed with two 64-bit atomics.
+// Krylov scalars (flexible PCG): dot products from the exact accumulators.
 // ---------------------------------------------------------------------------
 namespace mmh {
 
-__device__ __forceinline__ __int128 fx_scaled(double y) {
-  double a = fabs(y);
-  double q = floor(a * 5.42101086242752217e-20);
-  double rem = a - q * 18446744073709551616.0;
-  unsigned __int128 v = ((unsigned __int128)__double2ull_rz(q) << 64) | (unsigned __int128)__double2ull_rz(rem);
-  return y < 0 ? -(__int128)v : (__int128)v;
-}
+MMH_INSTANTIATE_PCG(double)
 
 __device__ __forceinline__ double fx_unscale(const unsigned long long* acc, int E) {
   __int128 s = (__int128)(((unsigned __int128)acc[1] << 64) | (unsigned __int128)acc[0]);
@@ -653,38 +647,6 @@ __device__ __forceinline__ double fx_unscale(const unsigned long long* acc, int 
   return neg ? -r : r;
 }
 
-__device__ __forceinline__ double bits_d(const unsigned long long* b) { return __longlong_as_double((long long)*b); }
-
-// q = L[p] = (t1 + t2 + tdiag*p) * di2, max|q| into qbits
-__global__ void k_apply(const double* __restrict__ p, const double* __restrict__ coef, int n, double di2,
-                        double* __restrict__ q, unsigned long long* qbits) {
-  i64 n3 = (i64)n * n * n;
-  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  double m = 0.0;
-  if (t < n3) {
-    int i, j, k;
-    cell_of(t, n, i, j, k);
-    double tdiag, t1, t2;
-    op_terms(p, coef, n, n3, i, j, k, tdiag, t1, t2);
-    double v = (t1 + t2 + tdiag * p[t]) * di2;
-    q[t] = v;
-    m = fabs(v);
-  }
-  block_max_commit(m, qbits);
-}
-
-__global__ void k_dot(const double* __restrict__ a, const double* __restrict__ b, i64 count,
-                      const unsigned long long* abits, const unsigned long long* bbits, unsigned long long* acc) {
-  double ma = bits_d(abits), mb = bits_d(bbits);
-  __int128 s = 0;
-  if (ma > 0.0 && mb > 0.0) {
-    int E = ilogb(ma) + ilogb(mb) + 2;
-    for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (i64)gridDim.x * blockDim.x)
-      s += fx_scaled(scalbn(a[t] * b[t], 96 - E));
-  }
-  fx_block_commit(s, acc);
-}
-
 __device__ __forceinline__ double dot_value(const unsigned long long* acc, const unsigned long long* abits,
                                             const unsigned long long* bbits) {
   double ma = bits_d(abits), mb = bits_d(bbits);
@@ -692,38 +654,8 @@ __device__ __forceinline__ double dot_value(const unsigned long long* acc, const
   return fx_unscale(acc, ilogb(ma) + ilogb(mb) + 2);
 }
 
-// x = x + alpha*p ; r = r - alpha*q ; max|r|
-__global__ void k_pcg_update(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
-                             const double* __restrict__ q, i64 count, const double* __restrict__ alpha,
-                             unsigned long long* rbits) {
-  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  double a = *alpha;
-  double m = 0.0;
-  if (t < count) {
-    x[t] = x[t] + a * p[t];
-    double v = r[t] - a * q[t];
-    r[t] = v;
-    m = fabs(v);
-  }
-  block_max_commit(m, rbits);
-}
-
-// p = z + beta*p ; max|p|
-__global__ void k_pcg_pupdate(double* __restrict__ p, const double* __restrict__ z, i64 count,
-                              const double* __restrict__ beta, unsigned long long* pbits) {
-  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  double b = *beta;
-  double m = 0.0;
-  if (t < count) {
-    double v = z[t] + b * p[t];
-    p[t] = v;
-    m = fabs(v);
-  }
-  block_max_commit(m, pbits);
-}
-
-// scalar steps.  st: 0 rz = dot(r,z) ; 1 alpha = rz / dot(p,q) ;
-// 2 beta = -(alpha*dot(z,q))/rz, rz = dot(r,z)
+// stage 0: rz = dot(r,z) ; 1: alpha = rz / dot(p,q) ;
+// 2: beta = -(alpha*dot(z,q))/rz, rz = dot(r,z)
 __global__ void k_pcg_scalar(PcgDev* s, int stage) {
   if (stage == 0) {
     s->rz = dot_value(s->acc[0], &s->rbits, &s->zbits);
@@ -738,32 +670,6 @@ __global__ void k_pcg_scalar(PcgDev* s, int stage) {
   }
 }
 
-void launch_apply(const double* p, const double* coef, int n, double dx, double* q, unsigned long long* qbits,
-                  cudaStream_t s) {
-  i64 n3 = (i64)n * n * n;
-  prof_begin(KK_APPLY, s, n3);
-  k_apply<<<grid_of(n3, kBlock), kBlock, 0, s>>>(p, coef, n, 1.0 / (dx * dx), q, qbits);
-  prof_end(KK_APPLY, s);
-  count_launch();
-}
-void launch_dot(const double* a, const double* b, i64 count, const unsigned long long* abits,
-                const unsigned long long* bbits, unsigned long long* acc, cudaStream_t s) {
-  i64 blocks = (count + kBlock - 1) / kBlock;
-  if (blocks > 152 * 16) blocks = 152 * 16;
-  if (blocks < 1) blocks = 1;
-  k_dot<<<(unsigned)blocks, kBlock, 0, s>>>(a, b, count, abits, bbits, acc);
-  count_launch();
-}
-void launch_pcg_update(double* x, double* r, const double* p, const double* q, i64 count, const double* alpha,
-                       unsigned long long* rbits, cudaStream_t s) {
-  k_pcg_update<<<grid_of(count, kBlock), kBlock, 0, s>>>(x, r, p, q, count, alpha, rbits);
-  count_launch();
-}
-void launch_pcg_pupdate(double* p, const double* z, i64 count, const double* beta, unsigned long long* pbits,
-                        cudaStream_t s) {
-  k_pcg_pupdate<<<grid_of(count, kBlock), kBlock, 0, s>>>(p, z, count, beta, pbits);
-  count_launch();
-}
 void launch_pcg_scalar(PcgDev* st, int stage, cudaStream_t s) {
   k_pcg_scalar<<<1, 1, 0, s>>>(st, stage);
   count_launch();

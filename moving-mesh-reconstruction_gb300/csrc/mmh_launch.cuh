@@ -55,6 +55,15 @@ void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nswe
     if (a != phi) cudaMemcpyAsync(phi, a, sizeof(T) * (size_t)n * n * n, cudaMemcpyDeviceToDevice, s);
     return;
   }
+  if (n <= 16) {
+    if (nsweeps > 0) {
+      prof_begin(kk<T>(KK_GS), s, h3 * 8 * nsweeps);
+      k_gs_small<T><<<1, 512, 0, s>>>(phi, rhs, coef, n, dx2, nsweeps);
+      prof_end(kk<T>(KK_GS), s);
+      count_launch();
+    }
+    return;
+  }
   unsigned g = grid_of(h3, kBlock);
   for (int sw = 0; sw < nsweeps; ++sw)
     for (int kpar = 0; kpar < 2; ++kpar)

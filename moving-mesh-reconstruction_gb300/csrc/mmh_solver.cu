@@ -100,8 +100,10 @@ struct mmh_ctx {
   std::vector<double*> defl, rhol;
   // FP32 hierarchy (mixed)
   Hier<float> h32;
-  // flexible PCG vectors (solution, right-hand side, search direction, L p)
+  // flexible PCG vectors (solution, right-hand side, search direction, L p);
+  // FP32 correction, right-hand side and directions of the mixed inner solve
   double *px = nullptr, *pb = nullptr, *pp = nullptr, *pq = nullptr;
+  float *pe32 = nullptr, *pb32 = nullptr, *pp32 = nullptr, *pq32 = nullptr;
   // relaxing
   double *baj = nullptr, *cc = nullptr, *vt = nullptr, *u1 = nullptr;
   // spectral
@@ -265,85 +267,145 @@ int build_levels(mmh_ctx* c, int l0) {
   return MMH_OK;
 }
 
-// One preconditioner application z = V(r): r in h64.rhs[l0], z to h64.u[l0].
-int precond(mmh_ctx* c, int l0) {
+// One preconditioner application z = V(r) on the precision-T hierarchy:
+// r in H.rhs[l0], z to H.u[l0], max|z| into zbits.
+template <class T>
+int precond(mmh_ctx* c, int l0, unsigned long long* zbits) {
+  Hier<T>& H = hier<T>(c);
   int n = c->nl[l0];
   i64 n3 = (i64)n * n * n;
-  if (c->cfg.precision == MMH_MIXED) {
-    launch_d2f(c->h64.rhs[l0], c->h32.rhs[l0], n3, c->s);
-    launch_fill<float>(c->h32.u[l0], n3, 0.0f, c->s);
-    RET(vcycle<float>(c, l0));
-    launch_f2d(c->h32.u[l0], c->h64.u[l0], n3, c->s);
-  } else {
-    launch_fill<double>(c->h64.u[l0], n3, 0.0, c->s);
-    RET(vcycle<double>(c, l0));
-  }
-  CK(cudaMemsetAsync(&c->sc->pcg.zbits, 0, 8, c->s));
-  launch_absmax<double>(c->h64.u[l0], n3, &c->sc->pcg.zbits, c->s);
+  launch_fill<T>(H.u[l0], n3, T(0), c->s);
+  RET(vcycle<T>(c, l0));
+  CK(cudaMemsetAsync(zbits, 0, 8, c->s));
+  launch_absmax<T>(H.u[l0], n3, zbits, c->s);
   return MMH_OK;
 }
 
-// Flexible preconditioned conjugate gradients on L x = b at level l0, one
-// V-cycle per iteration as preconditioner (FP64 or FP32 cycles).  Vectors,
-// operator and dot products are FP64; dots are exact and order free.
-int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_out, double* r1_out) {
+// Flexible preconditioned conjugate gradients on L x = b at level l0 in
+// precision T, one V-cycle per iteration as preconditioner, until
+// max|r| <= tol * bn (recurrence residual) or maxit iterations.  The
+// residual lives in H.rhs[l0] (the preconditioner's right-hand side) and the
+// preconditioned residual in H.u[l0].  Dot products are exact (FP64 scalars).
+template <class T>
+int pcg_core(mmh_ctx* c, int l0, double dx, T* x, const T* b, T* p, T* q, double bn, double tol, int maxit,
+             int* iters, double* rel_out, double* r0_out) {
+  Hier<T>& H = hier<T>(c);
   int n = c->nl[l0];
   i64 n3 = (i64)n * n * n;
   PcgDev* P = &c->sc->pcg;
-  double* r = c->h64.rhs[l0];
-  double* z = c->h64.u[l0];
-  CK(cudaMemcpyAsync(c->pb, r, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
-  CK(cudaMemcpyAsync(c->px, z, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  T* r = H.rhs[l0];
+  T* z = H.u[l0];
   CK(cudaMemsetAsync(P, 0, sizeof(PcgDev), c->s));
-  // r = b - L x
-  launch_residual<double>(c->px, c->pb, c->h64.coef[l0], n, dx, r, nullptr, &P->rbits, c->s);
+  launch_residual<T>(x, b, H.coef[l0], n, (T)dx, r, nullptr, &P->rbits, c->s);
   RET(pull_scal(c));
-  double rel = bits_to_double(c->hsc->pcg.rbits) / rn;
-  *r1_out = bits_to_double(c->hsc->pcg.rbits);
+  double rel = bits_to_double(c->hsc->pcg.rbits) / bn;
+  *r0_out = bits_to_double(c->hsc->pcg.rbits);
   int it = 0;
   int status = MMH_OK;
-  if (rel > c->cfg.tol) {
-    RET(precond(c, l0));
-    CK(cudaMemcpyAsync(c->pp, z, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  if (rel > tol) {
+    RET(precond<T>(c, l0, &P->zbits));
+    CK(cudaMemcpyAsync(p, z, sizeof(T) * n3, cudaMemcpyDeviceToDevice, c->s));
     CK(cudaMemcpyAsync(&P->pbits, &P->zbits, 8, cudaMemcpyDeviceToDevice, c->s));
-    launch_dot(r, z, n3, &P->rbits, &P->zbits, P->acc[0], c->s);
+    launch_dot<T>(r, z, n3, &P->rbits, &P->zbits, P->acc[0], c->s);
     launch_pcg_scalar(P, 0, c->s);
     for (it = 1;; ++it) {
       CK(cudaMemsetAsync(&P->qbits, 0, 8, c->s));
-      launch_apply(c->pp, c->h64.coef[l0], n, dx, c->pq, &P->qbits, c->s);
+      launch_apply<T>(p, H.coef[l0], n, (T)dx, q, &P->qbits, c->s);
       CK(cudaMemsetAsync(P->acc[1], 0, 16, c->s));
-      launch_dot(c->pp, c->pq, n3, &P->pbits, &P->qbits, P->acc[1], c->s);
+      launch_dot<T>(p, q, n3, &P->pbits, &P->qbits, P->acc[1], c->s);
       launch_pcg_scalar(P, 1, c->s);
       CK(cudaMemsetAsync(&P->rbits, 0, 8, c->s));
-      launch_pcg_update(c->px, r, c->pp, c->pq, n3, &P->alpha, &P->rbits, c->s);
+      launch_pcg_update<T>(x, r, p, q, n3, &P->alpha, &P->rbits, c->s);
       RET(pull_scal(c));
-      rel = bits_to_double(c->hsc->pcg.rbits) / rn;
-      if (!(rel == rel) || rel <= c->cfg.tol) break;
-      if (it >= c->cfg.max_cycles) {
+      rel = bits_to_double(c->hsc->pcg.rbits) / bn;
+      if (!(rel == rel) || rel <= tol) break;
+      if (it >= maxit) {
         status = MMH_ERR_DIVERGED;
         break;
       }
-      RET(precond(c, l0));
+      RET(precond<T>(c, l0, &P->zbits));
       CK(cudaMemsetAsync(P->acc[0], 0, 16, c->s));
       CK(cudaMemsetAsync(P->acc[2], 0, 16, c->s));
-      launch_dot(z, c->pq, n3, &P->zbits, &P->qbits, P->acc[2], c->s);
-      launch_dot(r, z, n3, &P->rbits, &P->zbits, P->acc[0], c->s);
+      launch_dot<T>(z, q, n3, &P->zbits, &P->qbits, P->acc[2], c->s);
+      launch_dot<T>(r, z, n3, &P->rbits, &P->zbits, P->acc[0], c->s);
       launch_pcg_scalar(P, 2, c->s);
       CK(cudaMemsetAsync(&P->pbits, 0, 8, c->s));
-      launch_pcg_pupdate(c->pp, z, n3, &P->beta, &P->pbits, c->s);
+      launch_pcg_pupdate<T>(p, z, n3, &P->beta, &P->pbits, c->s);
+    }
+  }
+  *iters = it;
+  *rel_out = rel;
+  if (!(rel == rel)) return MMH_ERR_NAN;
+  return status;
+}
+
+// FP64 true residual of x against b at level l0: max|b - L x| (also copied
+// to FP32 in r32 when given).
+int true_residual(mmh_ctx* c, int l0, double dx, const double* x, const double* b, float* r32, double* rmax) {
+  int n = c->nl[l0];
+  CK(cudaMemsetAsync(&c->sc->resbits, 0, 8, c->s));
+  launch_residual<double>(x, b, c->h64.coef[l0], n, dx, nullptr, r32, &c->sc->resbits, c->s);
+  RET(pull_scal(c));
+  *rmax = bits_to_double(c->hsc->resbits);
+  return MMH_OK;
+}
+
+// Solve L x = b to tol (MMH_SCHED_TOL).  MMH_FP64: flexible PCG in FP64.
+// MMH_MIXED: FP64 defect correction -- FP64 residual, inner FP32 flexible PCG
+// (FP32 V-cycle preconditioner) on the correction to a relative 1e-3, FP64
+// update -- until the FP64 residual meets tol.
+const double kInnerTol = 1e-3;
+const int kInnerMax = 60;
+
+int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_out, double* r1_out) {
+  int n = c->nl[l0];
+  i64 n3 = (i64)n * n * n;
+  double* u = c->h64.u[l0];
+  double* rhs = c->h64.rhs[l0];
+  CK(cudaMemcpyAsync(c->pb, rhs, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  CK(cudaMemcpyAsync(c->px, u, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  int status = MMH_OK, total = 0;
+  double rel = 0.0;
+  if (c->cfg.precision == MMH_FP64) {
+    int it = 0;
+    double r0 = 0.0;
+    status = pcg_core<double>(c, l0, dx, c->px, c->pb, c->pp, c->pq, rn, c->cfg.tol, c->cfg.max_cycles, &it, &rel,
+                              &r0);
+    if (status != MMH_OK && status != MMH_ERR_DIVERGED) return status;
+    total = it;
+    *r1_out = r0;
+  } else {
+    double rmax = 0.0;
+    for (int outer = 0;; ++outer) {
+      RET(true_residual(c, l0, dx, c->px, c->pb, c->pb32, &rmax));
+      rel = rmax / rn;
+      if (outer == 0) *r1_out = rmax;
+      if (!(rel == rel)) return MMH_ERR_NAN;
+      if (rel <= c->cfg.tol) break;
+      if (total >= c->cfg.max_cycles) {
+        status = MMH_ERR_DIVERGED;
+        break;
+      }
+      launch_fill<float>(c->pe32, n3, 0.0f, c->s);
+      int it = 0;
+      double rin = 0.0, r0 = 0.0;
+      int st = pcg_core<float>(c, l0, dx, c->pe32, c->pb32, c->pp32, c->pq32, rmax, kInnerTol, kInnerMax, &it, &rin,
+                               &r0);
+      if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
+      total += it;
+      launch_add_f2d(c->px, c->pe32, n3, c->s);
     }
   }
   // zero mean, true residual, results back in place
   RET(zerosum<double>(c, c->px, n3));
-  CK(cudaMemsetAsync(&P->rbits, 0, 8, c->s));
-  launch_residual<double>(c->px, c->pb, c->h64.coef[l0], n, dx, nullptr, nullptr, &P->rbits, c->s);
-  CK(cudaMemcpyAsync(z, c->px, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
-  CK(cudaMemcpyAsync(r, c->pb, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
-  RET(pull_scal(c));
-  double rt = bits_to_double(c->hsc->pcg.rbits);
+  double rt = 0.0;
+  RET(true_residual(c, l0, dx, c->px, c->pb, nullptr, &rt));
+  CK(cudaMemcpyAsync(u, c->px, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  CK(cudaMemcpyAsync(rhs, c->pb, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
   *rel_out = rt / rn;
-  *iters = it;
+  *iters = total;
   if (!(rt == rt)) return MMH_ERR_NAN;
+  if (status == MMH_ERR_DIVERGED && *rel_out <= c->cfg.tol) status = MMH_OK;
   return status;
 }
 
@@ -806,8 +868,15 @@ int mmh_create(mmh_ctx** out, const mmh_config* cfg) {
   if (cfg->schedule == MMH_SCHED_TOL) {
     A(&c->px, n3);
     A(&c->pb, n3);
-    A(&c->pp, n3);
-    A(&c->pq, n3);
+    if (cfg->precision == MMH_FP64) {
+      A(&c->pp, n3);
+      A(&c->pq, n3);
+    } else {
+      A(&c->pe32, n3);
+      A(&c->pb32, n3);
+      A(&c->pp32, n3);
+      A(&c->pq32, n3);
+    }
   }
   A(&c->baj, 7 * n3);
   A(&c->cc, n3);

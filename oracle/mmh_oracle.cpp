@@ -53,13 +53,27 @@ inline i64 ID(int i, int j, int k, int n) { return (i64)i + (i64)n * ((i64)j + (
 // Exact fixed-point summation (stand-in for the real(8) accumulators).
 // A term x (|x| < 2^32) maps to trunc(x * 2^64) as a signed 128-bit integer.
 // ---------------------------------------------------------------------------
-inline i128 fx_of(double x) {
-  double a = std::fabs(x) * 18446744073709551616.0;  // * 2^64, exact
-  double q = std::floor(a * 5.42101086242752217e-20);  // * 2^-64, exact
-  double rem = a - q * 18446744073709551616.0;         // exact
-  u128 v = ((u128)(uint64_t)q << 64) | (u128)(uint64_t)rem;
-  return x < 0 ? -(i128)v : (i128)v;
+// trunc(x * 2^sh) as a 128-bit integer, from the bits of x (finite x,
+// |x * 2^sh| < 2^126).
+inline i128 fx_bits(double x, int sh) {
+  uint64_t b;
+  std::memcpy(&b, &x, 8);
+  int ex = (int)((b >> 52) & 0x7FF);
+  uint64_t m = b & 0xFFFFFFFFFFFFFull;
+  if (ex == 0) {
+    if (m == 0) return 0;
+    ex = 1;
+  } else {
+    m |= (1ull << 52);
+  }
+  int s = ex - 1075 + sh;
+  u128 v;
+  if (s >= 0) v = (u128)m << s;
+  else if (s > -64) v = (u128)(m >> (-s));
+  else v = 0;
+  return (b >> 63) ? -(i128)v : (i128)v;
 }
+inline i128 fx_of(double x) { return fx_bits(x, 64); }
 inline double fx_to(i128 s) {
   bool neg = s < 0;
   u128 a = neg ? (u128)(-s) : (u128)s;
@@ -599,13 +613,6 @@ void mg_level(T* u, T* rhs, const T* def, const T* rho, int n, T dx, const MgCfg
 // truncated to a 128-bit integer and summed exactly; the GPU does the same.
 // ---------------------------------------------------------------------------
 inline int dot_exp(double ma, double mb) { return std::ilogb(ma) + std::ilogb(mb) + 2; }
-inline i128 fx_scaled(double y) {
-  double a = std::fabs(y);
-  double q = std::floor(a * 5.42101086242752217e-20);
-  double rem = a - q * 18446744073709551616.0;
-  u128 v = ((u128)(uint64_t)q << 64) | (u128)(uint64_t)rem;
-  return y < 0 ? -(i128)v : (i128)v;
-}
 inline double fx_unscale(i128 s, int E) {
   bool neg = s < 0;
   u128 a = neg ? (u128)(-s) : (u128)s;
@@ -621,7 +628,7 @@ double dot_exact(const T* a, const T* b, i64 n, double ma, double mb) {
   {
     i128 loc = 0;
 #pragma omp for nowait
-    for (i64 i = 0; i < n; ++i) loc += fx_scaled(std::ldexp((double)a[i] * (double)b[i], 96 - E));
+    for (i64 i = 0; i < n; ++i) loc += fx_bits((double)a[i] * (double)b[i], 96 - E);
 #pragma omp critical
     tot += loc;
   }
