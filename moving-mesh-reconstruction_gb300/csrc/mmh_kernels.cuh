@@ -23,6 +23,10 @@ __device__ __forceinline__ int wp(int i, int n) { return i + 1 == n ? 0 : i + 1;
 __device__ __forceinline__ int wm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
 __device__ __forceinline__ i64 IDX(int i, int j, int k, int n) { return (i64)i + (i64)n * ((i64)j + (i64)n * (i64)k); }
 
+template <class T> struct Vec16;
+template <> struct Vec16<float> { typedef float4 type; };
+template <> struct Vec16<double> { typedef double2 type; };
+
 __device__ __forceinline__ void cell_of(i64 t, int n, int& i, int& j, int& k) {
   i = (int)(t % n);
   i64 r = t / n;
@@ -302,30 +306,41 @@ __global__ void __launch_bounds__(256) k_gs_plane(const T* __restrict__ src, con
                                                   T* __restrict__ dst, const T* __restrict__ rhs,
                                                   const T* __restrict__ coef, int n, T dx2, int kpar) {
   constexpr int HB = 4, W = TX + 2 * HB, HT = TY + 2 * HB, S = W * HT;
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   const i64 n2 = (i64)n * n, n3 = n2 * n;
   const int i0 = blockIdx.x * TX - HB, j0 = blockIdx.y * TY - HB, k = 2 * blockIdx.z + kpar;
   const int kmn = wm(k, n), kpn = wp(k, n);
-  for (int e = threadIdx.x; e < S; e += blockDim.x) {
-    int x = e % W, y = e / W;
-    int gi = i0 + x, gj = j0 + y;
+  // 16-byte loads: a row segment of the tile starts 16-byte aligned (i0 is a
+  // multiple of 4 elements) and a 16-byte group never straddles the periodic
+  // wrap (n is a multiple of the group), so each group is one aligned load.
+  typedef typename Vec16<T>::type V;
+  constexpr int VW = 16 / (int)sizeof(T), NV = W / VW, NVT = NV * HT;
+  V* vs = reinterpret_cast<V*>(sm);
+  for (int e = threadIdx.x; e < NVT; e += blockDim.x) {
+    int xv = e % NV, y = e / NV;
+    int gi = i0 + xv * VW, gj = j0 + y;
     gi += (gi < 0) ? n : ((gi >= n) ? -n : 0);
     gj += (gj < 0) ? n : ((gj >= n) ? -n : 0);
     i64 b = (i64)gi + (i64)n * gj;
-    i64 cP = b + n2 * k, cm = b + n2 * kmn, cp = b + n2 * kpn;
-    sm[0 * S + e] = src[cP];
-    sm[1 * S + e] = rhs[cP];
+    i64 cP = (b + n2 * k) / VW, cm = (b + n2 * kmn) / VW, cp = (b + n2 * kpn) / VW, nv3 = n3 / VW;
+    const V* vsrc = reinterpret_cast<const V*>(src);
+    const V* vnbr = reinterpret_cast<const V*>(nbr);
+    const V* vrhs = reinterpret_cast<const V*>(rhs);
+    const V* vcoef = reinterpret_cast<const V*>(coef);
+    constexpr int SV = S / VW;
+    vs[0 * SV + e] = vsrc[cP];
+    vs[1 * SV + e] = vrhs[cP];
 #pragma unroll
-    for (int f = 0; f < 6; ++f) sm[(2 + f) * S + e] = coef[f * n3 + cP];
-    sm[8 * S + e] = nbr[cm];
-    sm[9 * S + e] = nbr[cp];
-    sm[10 * S + e] = coef[2 * n3 + cm];
-    sm[11 * S + e] = coef[4 * n3 + cm];
-    sm[12 * S + e] = coef[5 * n3 + cm];
-    sm[13 * S + e] = coef[2 * n3 + cp];
-    sm[14 * S + e] = coef[4 * n3 + cp];
-    sm[15 * S + e] = coef[5 * n3 + cp];
+    for (int f = 0; f < 6; ++f) vs[(2 + f) * SV + e] = vcoef[f * nv3 + cP];
+    vs[8 * SV + e] = vnbr[cm];
+    vs[9 * SV + e] = vnbr[cp];
+    vs[10 * SV + e] = vcoef[2 * nv3 + cm];
+    vs[11 * SV + e] = vcoef[4 * nv3 + cm];
+    vs[12 * SV + e] = vcoef[5 * nv3 + cm];
+    vs[13 * SV + e] = vcoef[2 * nv3 + cp];
+    vs[14 * SV + e] = vcoef[4 * nv3 + cp];
+    vs[15 * SV + e] = vcoef[5 * nv3 + cp];
   }
   __syncthreads();
   const T* sP = sm;

@@ -207,12 +207,20 @@ __global__ void k_limiter_pass1(double* __restrict__ tmp, const double* __restri
       nexp = 1;
       mx = 1;
     }
-    double compression = compression_of(1.0 + m.phixx, m.phixy, m.phixz, 1.0 + m.phiyy, m.phiyz, 1.0 + m.phizz);
+    // Only the sign of tlim is used here.  When the Gershgorin lower bound of
+    // the smallest eigenvalue of C = I + Hess(def) exceeds 1/cmpmax by a wide
+    // margin, tlim < 0 for certain and the trigonometric evaluation is skipped.
+    double c11 = 1.0 + m.phixx, c22 = 1.0 + m.phiyy, c33 = 1.0 + m.phizz;
+    double g = fmin(fmin(c11 - fabs(m.phixy) - fabs(m.phixz), c22 - fabs(m.phixy) - fabs(m.phiyz)),
+                    c33 - fabs(m.phixz) - fabs(m.phiyz));
     double cmpmax = cmpmaxglobal * 1.0;
-    double tlim = 3.0 * (1.0 / cmpmax - 1.0 / compression) / dtold;
-    if (tlim > 0.0) {
-      eflux = fmax(0.0, eflux);
-      mc = 1;
+    if (!(g > 1.0 / cmpmax + 1e-6)) {
+      double compression = compression_of(c11, m.phixy, m.phixz, c22, m.phiyz, c33);
+      double tlim = 3.0 * (1.0 / cmpmax - 1.0 / compression) / dtold;
+      if (tlim > 0.0) {
+        eflux = fmax(0.0, eflux);
+        mc = 1;
+      }
     }
     dmax = det;
     dmin = det;
