@@ -36,6 +36,7 @@ extern "C" {
 #define MMH_ERR_UNSUPPORTED (-7) /* e.g. relaxing with nonzero momentum/energy components */
 #define MMH_ERR_RANGE (-8)       /* a summed value is outside the exact-sum range |x| < 2^32 */
 #define MMH_ERR_NOMEM (-9)       /* device allocation failed */
+#define MMH_ERR_TOO_LARGE (-10)  /* grid larger than an allocation-free entry point's fixed scratch */
 
 /* precision forms */
 #define MMH_FP64 0  /* everything in FP64 (bit-identical to the CPU restatement) */
@@ -164,6 +165,24 @@ int mmh_outputs_f64(mmh_ctx* ctx, double* grad, double* delta);
 int mmh_outputs_dev(mmh_ctx* ctx, double* d_grad, double* d_delta);
 /* Device pointers of the resident state (n^3 doubles each). */
 int mmh_state_dev(mmh_ctx* ctx, double** d_def, double** d_rho, double** d_defp);
+
+/* ---- allocation-free relax (no counterpart in the reference) ----------- */
+/* For callers that cannot let a library allocate device memory (a driver that
+ * hands out every buffer from its own pool, or one that must not allocate in a
+ * time-critical loop).  Same work as mmh_relax_f64 with iresidopt 0 or 2 --
+ * metric, nrelax Gauss-Seidel sweeps, max-norm residual into *rinf -- on
+ * device pointers, with no context and no allocation: the scratch (metric,
+ * sweep buffer, reduction word) is a fixed device array of the library sized
+ * for n <= MMH_NOALLOC_MAX_N (7*64^3+2 doubles, about 14.7 MB, held on every
+ * GPU that loads the library until the process exits).  Larger grids return
+ * MMH_ERR_TOO_LARGE.  The first call on a device looks up the array's device
+ * address; make that first call before any stream capture.  All calls share
+ * the array, so calls that overlap on the GPU (concurrent streams, devices
+ * sharing nothing else) race and must be serialised by the caller.  The call
+ * synchronises `stream` (a cudaStream_t, NULL for the default stream). */
+#define MMH_NOALLOC_MAX_N 64
+int mmh_relax_noalloc_f64(const double* d_deformpot, const double* d_rho, double* d_arr, const double* d_rhs,
+                          double dx, int n, int nrelax, int iopt, double* rinf, void* stream);
 
 /* ---- kernel timing (no counterpart in the reference) -------------------- */
 /* Arm CUDA-event timing of one kernel kind (MMH_K_* | MMH_K_F32 for the FP32

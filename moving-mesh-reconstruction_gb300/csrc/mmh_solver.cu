@@ -768,6 +768,7 @@ const char* mmh_strerror(int code) {
     case MMH_ERR_UNSUPPORTED: return "unsupported input (nonzero momentum/energy components)";
     case MMH_ERR_RANGE: return "value outside the exact-sum range";
     case MMH_ERR_NOMEM: return "device allocation failed";
+    case MMH_ERR_TOO_LARGE: return "grid larger than the fixed scratch of the allocation-free entry point (n <= 64)";
     default: return "unknown error";
   }
 }
