@@ -27,6 +27,31 @@ template <class T> struct Vec16;
 template <> struct Vec16<float> { typedef float4 type; };
 template <> struct Vec16<double> { typedef double2 type; };
 
+// A 16-byte group of a tile row (elements x0..x0+VW-1, x0 a multiple of 4
+// for float, of 2 for double) stored into / loaded from a parity-split row:
+// even x at [x/2], odd x at [H2 + x/2].
+template <class T> struct SplitRow;
+template <> struct SplitRow<float> {
+  static __device__ __forceinline__ void store(float* row, int H2, int x0, float4 v) {
+    *reinterpret_cast<float2*>(row + (x0 >> 1)) = make_float2(v.x, v.z);
+    *reinterpret_cast<float2*>(row + H2 + (x0 >> 1)) = make_float2(v.y, v.w);
+  }
+  static __device__ __forceinline__ float4 load(const float* row, int H2, int x0) {
+    float2 e = *reinterpret_cast<const float2*>(row + (x0 >> 1));
+    float2 o = *reinterpret_cast<const float2*>(row + H2 + (x0 >> 1));
+    return make_float4(e.x, o.x, e.y, o.y);
+  }
+};
+template <> struct SplitRow<double> {
+  static __device__ __forceinline__ void store(double* row, int H2, int x0, double2 v) {
+    row[x0 >> 1] = v.x;
+    row[H2 + (x0 >> 1)] = v.y;
+  }
+  static __device__ __forceinline__ double2 load(const double* row, int H2, int x0) {
+    return make_double2(row[x0 >> 1], row[H2 + (x0 >> 1)]);
+  }
+};
+
 __device__ __forceinline__ void cell_of(i64 t, int n, int& i, int& j, int& k) {
   i = (int)(t % n);
   i64 r = t / n;
@@ -314,33 +339,36 @@ __global__ void __launch_bounds__(256) k_gs_plane(const T* __restrict__ src, con
   // 16-byte loads: a row segment of the tile starts 16-byte aligned (i0 is a
   // multiple of 4 elements) and a 16-byte group never straddles the periodic
   // wrap (n is a multiple of the group), so each group is one aligned load.
+  // Each tile row is stored parity-split (even x first, then odd x), so the
+  // cells of one colour and each of their x-neighbours are contiguous in
+  // shared memory and a colour phase reads it without bank conflicts.
   typedef typename Vec16<T>::type V;
-  constexpr int VW = 16 / (int)sizeof(T), NV = W / VW, NVT = NV * HT;
-  V* vs = reinterpret_cast<V*>(sm);
+  constexpr int VW = 16 / (int)sizeof(T), NV = W / VW, NVT = NV * HT, H2 = W / 2;
+  const V* vsrc = reinterpret_cast<const V*>(src);
+  const V* vnbr = reinterpret_cast<const V*>(nbr);
+  const V* vrhs = reinterpret_cast<const V*>(rhs);
+  const V* vcoef = reinterpret_cast<const V*>(coef);
+  const i64 nv3 = n3 / VW;
   for (int e = threadIdx.x; e < NVT; e += blockDim.x) {
-    int xv = e % NV, y = e / NV;
-    int gi = i0 + xv * VW, gj = j0 + y;
+    const int xv = e % NV, y = e / NV, x0 = xv * VW;
+    int gi = i0 + x0, gj = j0 + y;
     gi += (gi < 0) ? n : ((gi >= n) ? -n : 0);
     gj += (gj < 0) ? n : ((gj >= n) ? -n : 0);
-    i64 b = (i64)gi + (i64)n * gj;
-    i64 cP = (b + n2 * k) / VW, cm = (b + n2 * kmn) / VW, cp = (b + n2 * kpn) / VW, nv3 = n3 / VW;
-    const V* vsrc = reinterpret_cast<const V*>(src);
-    const V* vnbr = reinterpret_cast<const V*>(nbr);
-    const V* vrhs = reinterpret_cast<const V*>(rhs);
-    const V* vcoef = reinterpret_cast<const V*>(coef);
-    constexpr int SV = S / VW;
-    vs[0 * SV + e] = vsrc[cP];
-    vs[1 * SV + e] = vrhs[cP];
+    const i64 b = (i64)gi + (i64)n * gj;
+    const i64 cP = (b + n2 * k) / VW, cm = (b + n2 * kmn) / VW, cp = (b + n2 * kpn) / VW;
+    T* row = sm + y * W;
+    SplitRow<T>::store(row + 0 * S, H2, x0, vsrc[cP]);
+    SplitRow<T>::store(row + 1 * S, H2, x0, vrhs[cP]);
 #pragma unroll
-    for (int f = 0; f < 6; ++f) vs[(2 + f) * SV + e] = vcoef[f * nv3 + cP];
-    vs[8 * SV + e] = vnbr[cm];
-    vs[9 * SV + e] = vnbr[cp];
-    vs[10 * SV + e] = vcoef[2 * nv3 + cm];
-    vs[11 * SV + e] = vcoef[4 * nv3 + cm];
-    vs[12 * SV + e] = vcoef[5 * nv3 + cm];
-    vs[13 * SV + e] = vcoef[2 * nv3 + cp];
-    vs[14 * SV + e] = vcoef[4 * nv3 + cp];
-    vs[15 * SV + e] = vcoef[5 * nv3 + cp];
+    for (int f = 0; f < 6; ++f) SplitRow<T>::store(row + (2 + f) * S, H2, x0, vcoef[f * nv3 + cP]);
+    SplitRow<T>::store(row + 8 * S, H2, x0, vnbr[cm]);
+    SplitRow<T>::store(row + 9 * S, H2, x0, vnbr[cp]);
+    SplitRow<T>::store(row + 10 * S, H2, x0, vcoef[2 * nv3 + cm]);
+    SplitRow<T>::store(row + 11 * S, H2, x0, vcoef[4 * nv3 + cm]);
+    SplitRow<T>::store(row + 12 * S, H2, x0, vcoef[5 * nv3 + cm]);
+    SplitRow<T>::store(row + 13 * S, H2, x0, vcoef[2 * nv3 + cp]);
+    SplitRow<T>::store(row + 14 * S, H2, x0, vcoef[4 * nv3 + cp]);
+    SplitRow<T>::store(row + 15 * S, H2, x0, vcoef[5 * nv3 + cp]);
   }
   __syncthreads();
   const T* sP = sm;
@@ -359,30 +387,35 @@ __global__ void __launch_bounds__(256) k_gs_plane(const T* __restrict__ src, con
     const int xs = HB - r + ((HB - r) & 1 ? (io ? 0 : 1) : io);
     const int ys = HB - r + ((HB - r) & 1 ? (jo ? 0 : 1) : jo);
     const int nx = (HB + TX + r - xs + 1) / 2, ny = (HB + TY + r - ys + 1) / 2;
+    // offsets from (row + x/2) of the cell and of its x+1 / x-1 neighbours
+    const int oc = io * H2, oxp = (1 - io) * H2 + io, oxm = (1 - io) * H2 + io - 1;
     for (int e = threadIdx.x; e < nx * ny; e += blockDim.x) {
       const int x = xs + 2 * (e % nx), y = ys + 2 * (e / nx);
-      const int c = y * W + x;
+      const int base = y * W + (x >> 1);
+      const int c = base + oc, cxp = base + oxp, cxm = base + oxm;
       Stencil<T> st;
-      st.c = sP[c]; st.ip = sP[c + 1]; st.im = sP[c - 1]; st.jp = sP[c + W]; st.jm = sP[c - W];
+      st.c = sP[c]; st.ip = sP[cxp]; st.im = sP[cxm]; st.jp = sP[c + W]; st.jm = sP[c - W];
       st.kp = sKp[c]; st.km = sKm[c];
-      st.ppk = sP[c + W + 1]; st.mpk = sP[c + W - 1]; st.pmk = sP[c - W + 1]; st.mmk = sP[c - W - 1];
+      st.ppk = sP[cxp + W]; st.mpk = sP[cxm + W]; st.pmk = sP[cxp - W]; st.mmk = sP[cxm - W];
       st.jpkp = sKp[c + W]; st.jmkp = sKp[c - W]; st.jpkm = sKm[c + W]; st.jmkm = sKm[c - W];
-      st.ipkp = sKp[c + 1]; st.imkp = sKp[c - 1]; st.ipkm = sKm[c + 1]; st.imkm = sKm[c - 1];
-      st.f1c = F1[c]; st.f1ip = F1[c + 1]; st.f1im = F1[c - 1];
+      st.ipkp = sKp[cxp]; st.imkp = sKp[cxm]; st.ipkm = sKm[cxp]; st.imkm = sKm[cxm];
+      st.f1c = F1[c]; st.f1ip = F1[cxp]; st.f1im = F1[cxm];
       st.f4c = F4[c]; st.f4jp = F4[c + W]; st.f4jm = F4[c - W];
       st.f6c = F6[c]; st.f6kp = sm[15 * S + c]; st.f6km = sm[12 * S + c];
-      st.f2jp = F2[c + W]; st.f2jm = F2[c - W]; st.f2ip = F2[c + 1]; st.f2im = F2[c - 1];
+      st.f2jp = F2[c + W]; st.f2jm = F2[c - W]; st.f2ip = F2[cxp]; st.f2im = F2[cxm];
       st.f5kp = sm[14 * S + c]; st.f5km = sm[11 * S + c]; st.f5jp = F5[c + W]; st.f5jm = F5[c - W];
-      st.f3kp = sm[13 * S + c]; st.f3km = sm[10 * S + c]; st.f3ip = F3[c + 1]; st.f3im = F3[c - 1];
+      st.f3kp = sm[13 * S + c]; st.f3km = sm[10 * S + c]; st.f3ip = F3[cxp]; st.f3im = F3[cxm];
       T tdiag, t1, t2;
       op_eval(st, tdiag, t1, t2);
       sm[c] = (sR[c] * dx2 - t1 - t2) / tdiag;
     }
     __syncthreads();
   }
-  for (int e = threadIdx.x; e < TX * TY; e += blockDim.x) {
-    int x = HB + e % TX, y = HB + e / TX;
-    dst[(i64)(i0 + x) + (i64)n * (j0 + y) + n2 * k] = sm[y * W + x];
+  constexpr int NVI = TX / VW;
+  V* vdst = reinterpret_cast<V*>(dst);
+  for (int e = threadIdx.x; e < NVI * TY; e += blockDim.x) {
+    const int x0 = HB + (e % NVI) * VW, y = HB + e / NVI;
+    vdst[((i64)(i0 + x0) + (i64)n * (j0 + y) + n2 * k) / VW] = SplitRow<T>::load(sm + y * W, H2, x0);
   }
 }
 
