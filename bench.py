@@ -44,10 +44,16 @@ import numpy as np  # noqa: E402
 
 METRIC = "s per 512³ reconstruction to residual 1e-8: mixed vs FP64 GPU; stencil HBM GB/s"
 UNIT = "s/reconstruction"
-# Algorithmic bytes per processed cell (per updated cell for the colour kernel):
-# Gauss-Seidel colour sweep reads phi, rhs and 6 coefficients and writes phi
-# (9 words); the residual reads phi, rhs, 6 coefficients and writes r (9 words).
-ALG_WORDS = {"gs": 9, "residual": 9}
+# Algorithmic words per processed cell.  One launch of the fused Gauss-Seidel
+# plane kernel updates every cell of the planes of one parity (n^3/2 cells):
+# it must read phi, rhs and the 6 metric coefficients of those planes (8 words
+# per updated cell), phi and coefficients 3, 5, 6 of the planes of the other
+# parity (4 words per updated cell, each plane once although two planes use
+# it) and write phi (1 word): 13 words.  The residual reads phi, rhs and the 6
+# coefficients and writes r: 9 words per cell.
+ALG_WORDS = {"gs": 13, "residual": 9}
+KERNEL_NAME = {"gs32": "k_gs_plane<float,32,16>", "gs64": "k_gs_plane<double,32,8>",
+               "res64": "k_residual<double>", "res32": "k_residual<float>"}
 
 
 def parse():
@@ -322,6 +328,8 @@ def main():
     kinds = {"gs32": mmh.K_GS | mmh.K_F32, "gs64": mmh.K_GS, "res64": mmh.K_RESIDUAL,
              "res32": mmh.K_RESIDUAL | mmh.K_F32, "none": None}
     pk = kinds[args.profile]
+    if pk is not None:
+        pk |= mmh.K_AT(n)  # the finest grid level only: the launches that dominate the step
     clocks = ClockSampler(local)
     clocks.start()
     ms_mixed, diags, launches, prof = timed(ctx, args.steps, pk)
@@ -379,14 +387,13 @@ def main():
     roofline = None
     if prof and prof[0] > 0:
         nl, pms, cells = prof
-        word = 4 if pk & mmh.K_F32 else 8
+        word = 4 if args.profile.endswith("32") else 8
         kname = args.profile
         words = ALG_WORDS["gs" if kname.startswith("gs") else "residual"]
         alg_bytes = cells * words * word
         achieved = alg_bytes / (pms / 1000.0) / 1e9
-        tr = traffic_from_profiles(kname)
-        roofline = {"kernel": {"gs32": "k_gs_colour<float>", "gs64": "k_gs_colour<double>",
-                               "res64": "k_residual<double>", "res32": "k_residual<float>"}[kname],
+        tr = traffic_from_profiles(KERNEL_NAME[kname])
+        roofline = {"kernel": f"{KERNEL_NAME[kname]} on the {n}^3 level",
                     "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else peak_src,
                     "traffic": (tr * cells / nl) if tr else None,

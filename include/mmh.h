@@ -197,6 +197,8 @@ int mmh_relax_noalloc_f64(const double* d_deformpot, const double* d_rho, double
 #define MMH_K_PROLONG 6
 #define MMH_K_RESTRICT 7
 #define MMH_K_F32 256
+/* OR-ed into the kind: time only the launches on the n^3 grid level. */
+#define MMH_K_AT(n) ((n) << 12)
 int mmh_profile_start(int kind);
 int mmh_profile_stop(int* launches, double* ms, long long* cells);
 

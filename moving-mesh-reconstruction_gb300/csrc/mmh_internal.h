@@ -17,8 +17,8 @@ enum KernelKind {
   KK_GS = 1, KK_RESIDUAL = 2, KK_RESTRICT_RESID = 3, KK_METRIC = 4, KK_SMOOTH = 5, KK_PROLONG = 6,
   KK_RESTRICT = 7, KK_LIMITER = 8, KK_RELAXING = 9, KK_SPECTRAL = 10, KK_APPLY = 11, KK_F32 = 256
 };
-void prof_begin(int kind, cudaStream_t s, i64 cells);
-void prof_end(int kind, cudaStream_t s);
+void prof_begin(int kind, cudaStream_t s, i64 cells, int n);
+void prof_end(int kind, cudaStream_t s, int n);
 int prof_start(int kind);
 int prof_stop(int* launches, double* ms, long long* cells);
 template <class T> inline int kk(int base) { return base | (sizeof(T) == 4 ? KK_F32 : 0); }

@@ -40,8 +40,16 @@ int prof_start(int kind) {
   return 0;
 }
 
-void prof_begin(int kind, cudaStream_t s, i64 cells) {
-  if (g_prof.kind == 0 || kind != g_prof.kind) return;
+// The armed kind may carry a grid filter in bits 12 and up (MMH_K_AT(n)):
+// then only launches on that grid are timed.
+static bool prof_match(int kind, int n) {
+  if (g_prof.kind == 0 || kind != (g_prof.kind & 0xfff)) return false;
+  const int at = g_prof.kind >> 12;
+  return at == 0 || at == n;
+}
+
+void prof_begin(int kind, cudaStream_t s, i64 cells, int n) {
+  if (!prof_match(kind, n)) return;
   if (g_prof.used >= (int)g_prof.ev.size() / 2) {
     g_prof.dropped++;
     return;
@@ -50,8 +58,8 @@ void prof_begin(int kind, cudaStream_t s, i64 cells) {
   g_prof.cells += cells;
 }
 
-void prof_end(int kind, cudaStream_t s) {
-  if (g_prof.kind == 0 || kind != g_prof.kind) return;
+void prof_end(int kind, cudaStream_t s, int n) {
+  if (!prof_match(kind, n)) return;
   if (g_prof.used >= (int)g_prof.ev.size() / 2) return;
   cudaEventRecord(g_prof.ev[2 * g_prof.used + 1], s);
   g_prof.used++;

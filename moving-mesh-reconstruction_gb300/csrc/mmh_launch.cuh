@@ -12,9 +12,9 @@ template <class T>
 void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
   T di2 = T(1) / (dx * dx);
-  prof_begin(kk<T>(KK_METRIC), s, n3);
+  prof_begin(kk<T>(KK_METRIC), s, n3, n);
   k_metric<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(def, rho, n, di2, coef);
-  prof_end(kk<T>(KK_METRIC), s);
+  prof_end(kk<T>(KK_METRIC), s, n);
   count_launch();
 }
 
@@ -43,9 +43,9 @@ void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nswe
     T* b = scratch;
     for (int sw = 0; sw < nsweeps; ++sw) {
       for (int kpar = 0; kpar < 2; ++kpar) {
-        prof_begin(kk<T>(KK_GS), s, 4 * h3);
+        prof_begin(kk<T>(KK_GS), s, 4 * h3, n);
         k_gs_plane<T, TX, TY><<<grid, 256, smem, s>>>(a, kpar == 0 ? a : b, b, rhs, coef, n, dx2, kpar);
-        prof_end(kk<T>(KK_GS), s);
+        prof_end(kk<T>(KK_GS), s, n);
         count_launch();
       }
       T* t = a;
@@ -57,9 +57,9 @@ void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nswe
   }
   if (n <= 16) {
     if (nsweeps > 0) {
-      prof_begin(kk<T>(KK_GS), s, h3 * 8 * nsweeps);
+      prof_begin(kk<T>(KK_GS), s, h3 * 8 * nsweeps, n);
       k_gs_small<T><<<1, 512, 0, s>>>(phi, rhs, coef, n, dx2, nsweeps);
-      prof_end(kk<T>(KK_GS), s);
+      prof_end(kk<T>(KK_GS), s, n);
       count_launch();
     }
     return;
@@ -69,9 +69,9 @@ void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nswe
     for (int kpar = 0; kpar < 2; ++kpar)
       for (int io = 0; io < 2; ++io)
         for (int jo = 0; jo < 2; ++jo) {
-          prof_begin(kk<T>(KK_GS), s, h3);
+          prof_begin(kk<T>(KK_GS), s, h3, n);
           k_gs_colour<T><<<g, kBlock, 0, s>>>(phi, rhs, coef, n, dx2, kpar, io, jo);
-          prof_end(kk<T>(KK_GS), s);
+          prof_end(kk<T>(KK_GS), s, n);
           count_launch();
         }
 }
@@ -81,45 +81,45 @@ void launch_residual(const T* phi, const T* rhs, const T* coef, int n, T dx, T* 
                      unsigned long long* maxbits, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
   T di2 = T(1) / (dx * dx);
-  prof_begin(kk<T>(KK_RESIDUAL), s, n3);
+  prof_begin(kk<T>(KK_RESIDUAL), s, n3, n);
   k_residual<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(phi, rhs, coef, n, di2, r, r32, maxbits);
-  prof_end(kk<T>(KK_RESIDUAL), s);
+  prof_end(kk<T>(KK_RESIDUAL), s, n);
   count_launch();
 }
 
 template <class T>
 void launch_restrict_resid(const T* r, int n, int special, T* coarse, cudaStream_t s) {
   i64 h3 = (i64)(n / 2) * (n / 2) * (n / 2);
-  prof_begin(kk<T>(KK_RESTRICT_RESID), s, h3);
+  prof_begin(kk<T>(KK_RESTRICT_RESID), s, h3, n);
   k_restrict_resid<T><<<grid_of(h3, kBlock), kBlock, 0, s>>>(r, n, special, coarse);
-  prof_end(kk<T>(KK_RESTRICT_RESID), s);
+  prof_end(kk<T>(KK_RESTRICT_RESID), s, n);
   count_launch();
 }
 
 template <class T>
 void launch_restrict27(const T* fine, int n, T* coarse, cudaStream_t s) {
   i64 h3 = (i64)(n / 2) * (n / 2) * (n / 2);
-  prof_begin(kk<T>(KK_RESTRICT), s, h3);
+  prof_begin(kk<T>(KK_RESTRICT), s, h3, n);
   k_restrict27<T><<<grid_of(h3, kBlock), kBlock, 0, s>>>(fine, n, coarse);
-  prof_end(kk<T>(KK_RESTRICT), s);
+  prof_end(kk<T>(KK_RESTRICT), s, n);
   count_launch();
 }
 
 template <class T>
 void launch_smooth27(const T* in, int n, T* out, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
-  prof_begin(kk<T>(KK_SMOOTH), s, n3);
+  prof_begin(kk<T>(KK_SMOOTH), s, n3, n);
   k_smooth27<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(in, n, out);
-  prof_end(kk<T>(KK_SMOOTH), s);
+  prof_end(kk<T>(KK_SMOOTH), s, n);
   count_launch();
 }
 
 template <class T>
 void launch_prolong_add(T* u, const T* uh, int n, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
-  prof_begin(kk<T>(KK_PROLONG), s, n3);
+  prof_begin(kk<T>(KK_PROLONG), s, n3, n);
   k_prolong_add<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(u, uh, n);
-  prof_end(kk<T>(KK_PROLONG), s);
+  prof_end(kk<T>(KK_PROLONG), s, n);
   count_launch();
 }
 

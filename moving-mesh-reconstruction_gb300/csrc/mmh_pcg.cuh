@@ -76,9 +76,9 @@ __global__ void k_pcg_pupdate(T* __restrict__ p, const T* __restrict__ z, i64 co
 template <class T>
 void launch_apply(const T* p, const T* coef, int n, T dx, T* q, unsigned long long* qbits, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
-  prof_begin(kk<T>(KK_APPLY), s, n3);
+  prof_begin(kk<T>(KK_APPLY), s, n3, n);
   k_apply<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(p, coef, n, T(1) / (dx * dx), q, qbits);
-  prof_end(kk<T>(KK_APPLY), s);
+  prof_end(kk<T>(KK_APPLY), s, n);
   count_launch();
 }
 

@@ -213,7 +213,7 @@ int vcycle(mmh_ctx* c, int l) {
   bool at_ng = (n == c->n);
   bool guard = !at_ng && (c->cfg.schedule != MMH_SCHED_TOL || c->cfg.precond_guards);
   if (n == 4) {
-    if (std::is_same<T, float>::value) {
+    if constexpr (std::is_same<T, float>::value) {
       // coarsest grid solved in FP64
       Hier<float>& F = c->h32;
       i64 n3 = 64;

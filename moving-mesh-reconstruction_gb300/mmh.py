@@ -46,6 +46,11 @@ K_GS, K_RESIDUAL, K_RESTRICT_RESID, K_METRIC, K_SMOOTH, K_PROLONG, K_RESTRICT = 
 K_F32 = 256
 
 
+def K_AT(n):
+    """Grid filter for profile_start: time only the launches on the n^3 level."""
+    return int(n) << 12
+
+
 class MMHError(RuntimeError):
     def __init__(self, code, what=""):
         self.code = code
