@@ -27,32 +27,17 @@ template <class T> struct Vec16;
 template <> struct Vec16<float> { typedef float4 type; };
 template <> struct Vec16<double> { typedef double2 type; };
 
-// A 16-byte group of a tile row (elements x0..x0+VW-1, x0 a multiple of 4
-// for float, of 2 for double) stored into / loaded from a parity-split row:
-// even x at [x/2], odd x at [H2 + x/2].
-template <class T> struct SplitRow;
-template <> struct SplitRow<float> {
-  static __device__ __forceinline__ void store(float* row, int H2, int x0, float4 v) {
-    *reinterpret_cast<float2*>(row + (x0 >> 1)) = make_float2(v.x, v.z);
-    *reinterpret_cast<float2*>(row + H2 + (x0 >> 1)) = make_float2(v.y, v.w);
-  }
-  static __device__ __forceinline__ float4 load(const float* row, int H2, int x0) {
-    float2 e = *reinterpret_cast<const float2*>(row + (x0 >> 1));
-    float2 o = *reinterpret_cast<const float2*>(row + H2 + (x0 >> 1));
-    return make_float4(e.x, o.x, e.y, o.y);
-  }
-};
-template <> struct SplitRow<double> {
-  static __device__ __forceinline__ void store(double* row, int H2, int x0, double2 v) {
-    row[x0 >> 1] = v.x;
-    row[H2 + (x0 >> 1)] = v.y;
-  }
-  static __device__ __forceinline__ double2 load(const double* row, int H2, int x0) {
-    return make_double2(row[x0 >> 1], row[H2 + (x0 >> 1)]);
-  }
-};
-
+// (i, j, k) of cell t.  Grid sizes are powers of two (the library checks),
+// which turns the index split into shifts; the division form stays for any
+// other size.
 __device__ __forceinline__ void cell_of(i64 t, int n, int& i, int& j, int& k) {
+  if ((n & (n - 1)) == 0) {
+    const int lg = __ffs(n) - 1;
+    i = (int)t & (n - 1);
+    j = (int)(t >> lg) & (n - 1);
+    k = (int)(t >> (2 * lg));
+    return;
+  }
   i = (int)(t % n);
   i64 r = t / n;
   j = (int)(r % n);
@@ -130,16 +115,21 @@ __device__ __forceinline__ unsigned long long ord_of(double x) {
   unsigned long long b = (unsigned long long)__double_as_longlong(x);
   return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
+__device__ __forceinline__ double from_ord(unsigned long long o) {
+  unsigned long long b = (o >> 63) ? (o & 0x7FFFFFFFFFFFFFFFull) : ~o;
+  return __longlong_as_double((long long)b);
+}
 
 __device__ __forceinline__ double warp_max(double v) {
   for (int d = 16; d > 0; d >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, d));
   return v;
 }
 
-// max of non-negative values (NaN wins: its bit pattern is above +inf)
-__device__ __forceinline__ void block_max_commit(double v, unsigned long long* out) {
+// Block-wide max of non-negative values into *out (FP64 bits, atomicMax):
+// the bit patterns of non-negative floating-point numbers are ordered like
+// their values (NaN above inf), so the reduction is integer-only.
+__device__ __forceinline__ void block_max_commit_bits(unsigned long long b, unsigned long long* out) {
   __shared__ unsigned long long s_m[32];
-  unsigned long long b = (unsigned long long)__double_as_longlong(v);
   for (int d = 16; d > 0; d >>= 1) {
     unsigned long long o = shfl_down_u64(b, d);
     b = o > b ? o : b;
@@ -154,6 +144,27 @@ __device__ __forceinline__ void block_max_commit(double v, unsigned long long* o
     atomicMax(out, m);
   }
 }
+__device__ __forceinline__ void block_max_commit(double v, unsigned long long* out) {
+  block_max_commit_bits((unsigned long long)__double_as_longlong(v), out);
+}
+// FP32 values reduce as 32-bit patterns within the warp and are widened to
+// FP64 once per warp (a widening is an FP64-pipe operation).
+__device__ __forceinline__ void block_max_commit(float v, unsigned long long* out) {
+  unsigned b = __float_as_uint(v);
+  for (int d = 16; d > 0; d >>= 1) {
+    unsigned o = __shfl_down_sync(0xffffffffu, b, d);
+    b = o > b ? o : b;
+  }
+  unsigned long long w = 0;
+  if ((threadIdx.x & 31) == 0) w = (unsigned long long)__double_as_longlong((double)__uint_as_float(b));
+  block_max_commit_bits(w, out);
+}
+__device__ __forceinline__ unsigned abs_bits(float x) { return __float_as_uint(x) & 0x7FFFFFFFu; }
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ float from_bits(unsigned b) { return __uint_as_float(b); }
+__device__ __forceinline__ double from_bits(unsigned long long b) { return __longlong_as_double((long long)b); }
 
 // ---------------------------------------------------------------------------
 // Curvilinear metric (cbajraw, mmh/gauss1.f90:1107-1210, non-lsquare branch)
@@ -317,33 +328,166 @@ __global__ void __launch_bounds__(512) k_gs_small(T* __restrict__ phi, const T* 
     }
 }
 
-// All four in-plane colours of one plane P (k%2 == kpar) for a TX x TY tile,
-// staged in shared memory with a 4-cell halo; colour q = 2*io + jo is applied
-// on the tile grown by 3-q cells, so the interior ends exactly as after the
-// four global colour phases (cells of one colour never read each other).
-// The half sweep reads its own planes from src, the neighbour planes P+-1
-// (not written during the half sweep) from nbr, and writes dst != src, so no
-// tile can read a halo that another tile has already updated.  Needs n >= TX+8
-// and n >= TY+8.  Shared-memory slots: 0 phi(P), 1 rhs(P), 2-7 f1..f6(P),
-// 8/9 phi(P-1)/phi(P+1), 10-12 f3,f5,f6(P-1), 13-15 f3,f5,f6(P+1).
+// The same sweeps with the whole grid held in shared memory (phi, rhs and the
+// six coefficients: 8*n^3 words, n <= 8), read once and written back once; a
+// colour phase then costs shared-memory latency instead of L2 latency.  Used
+// for the coarsest levels, where one CTA runs tens of sweeps.
+template <class T>
+__global__ void __launch_bounds__(512) k_gs_small_sm(T* __restrict__ phi, const T* __restrict__ rhs,
+                                                      const T* __restrict__ coef, int n, T dx2, int nsweeps) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int h = n >> 1;
+  const int tot = h * h * h;
+  const int n3 = n * n * n;
+  T* sp = reinterpret_cast<T*>(smem_raw);
+  T* sr = sp + n3;
+  T* sc = sr + n3;
+  for (int e = threadIdx.x; e < n3; e += blockDim.x) {
+    sp[e] = phi[e];
+    sr[e] = rhs[e];
+  }
+  for (int e = threadIdx.x; e < 6 * n3; e += blockDim.x) sc[e] = coef[e];
+  __syncthreads();
+  for (int sw = 0; sw < nsweeps; ++sw)
+    for (int q = 0; q < 8; ++q) {
+      const int kpar = q >> 2, io = (q >> 1) & 1, jo = q & 1;
+      for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+        int ti = t % h, tj = (t / h) % h, tk = t / (h * h);
+        int i = 2 * ti + io, j = 2 * tj + jo, k = 2 * tk + kpar;
+        T tdiag, t1, t2;
+        op_terms(sp, sc, n, (i64)n3, i, j, k, tdiag, t1, t2);
+        i64 c = IDX(i, j, k, n);
+        sp[c] = (sr[c] * dx2 - t1 - t2) / tdiag;
+      }
+      __syncthreads();
+    }
+  for (int e = threadIdx.x; e < n3; e += blockDim.x) phi[e] = sp[e];
+}
+
+// Tile geometry of the fused plane kernel.  A tile holds TX x TY interior
+// cells of one plane and a halo of HB = 4 cells: W x HT cells.  Colour
+// q = 2*io + jo (x parity io, y parity jo) is applied on NXC = W/2 - 2 cells
+// of each of its rows, x = XS(io) + 2m (XS = 4 for even x, 1 for odd x), and
+// on the rows ys(q) = HB-2+q, ys(q)+2, ... (ny(q) = TY/2+3-q rows).  With the
+// colours in the reference's order (io outer, jo inner), the later colours
+// read updated cells of the earlier ones within one cell in x and within
+// 3-q rows in y, so this region covers everything they read and the interior
+// ends exactly as after the four global colour phases; the extra cells a
+// colour computes beyond that are never read.
+//
+// Shared memory.  Fields read at neighbours (stencil fields) are stored with
+// the even rows first and the odd rows OFFB words after them, a pitch of Q
+// words between two rows of one parity, and every row split into its even-x
+// and its odd-x half (H2 words each).  Cell m of row t of a colour then sits
+// at word const + Q*t + m, and Q = NXC (mod 32) puts the words of any 32
+// consecutive cells of a colour in 32 different banks (16 different bank
+// pairs for 8-byte words): a colour phase reads shared memory without bank
+// conflicts.  Fields read only at the cell itself (centre fields) are stored
+// compacted per colour, cell e of colour q at cbase(q) + e.  Q, OFFB, H2 and
+// NXC are even, so two cells x0 and x0+2 of a 16-byte group are adjacent
+// 8-byte-aligned words in either layout and are stored as one pair.
+template <class T, int TX, int TY>
+struct GsGeom {
+  static constexpr int HB = 4, W = TX + 2 * HB, HT = TY + 2 * HB, H2 = W / 2, NXC = H2 - 2;
+  static constexpr int Q = NXC + 32 * ((W - NXC + 31) / 32);
+  static constexpr int OFFB0 = (HT / 2) * Q;
+  static constexpr int OFFB = OFFB0 + ((20 - OFFB0 % 32) + 32) % 32;  // first odd row (fewer store conflicts)
+  static constexpr int SF = OFFB + (HT / 2) * Q;  // words of one stencil field
+  static constexpr int NC = NXC * (2 * TY + 6);   // words of one centre field (four colours)
+  static constexpr int NSF = 8, NCF = 8;
+  static constexpr int WORDS = NSF * SF + NCF * NC;
+  static __device__ __forceinline__ constexpr int XS(int io) { return io ? 1 : HB; }
+  static __device__ __forceinline__ constexpr int ys(int q) { return HB - 2 + q; }
+  static __device__ __forceinline__ constexpr int ny(int q) { return TY / 2 + 3 - q; }
+  static __device__ __forceinline__ constexpr int cbase(int q) { return NXC * (q * (TY / 2 + 3) - q * (q - 1) / 2); }
+  static __device__ __forceinline__ int word(int x, int y) {
+    return (y & 1) * OFFB + (y >> 1) * Q + (x & 1) * H2 + (x >> 1);
+  }
+  static_assert(Q >= W && (Q - NXC) % 32 == 0 && Q % 2 == 0 && OFFB % 2 == 0 && NXC % 2 == 0, "row pitch");
+  static_assert(HT % 2 == 0 && TX % 4 == 0, "tile shape");
+  // the computed x ranges, [4, W-2] even and [1, W-5] odd, start and end on
+  // whole pairs (x0, x0+2) of the 16-byte groups
+  static_assert(HB % 4 == 0 && (HB + 2 * (NXC - 1)) % 4 == 2 && (1 + 2 * (NXC - 1)) % 4 == 3, "pairs");
+};
+
+// Per 16-byte group (cells x0..x0+VW-1 of tile row y, x0 a multiple of VW, so
+// cell x0+j has the x parity of j): its stencil word sw (cell x0+j at
+// sw + (j&1)*H2 + (j>>1)) and, per x parity io, its centre word cw[io] (cell
+// x0+io+2h at cw[io] + h) and whether those cells are computed (cv[io]).
+template <class G, int VW>
+struct GsSlot {
+  int sw, cw[2];
+  bool cv[2];
+  __device__ __forceinline__ GsSlot(int x0, int y) {
+    sw = (y & 1) * G::OFFB + (y >> 1) * G::Q + (x0 >> 1);
+    const int jo = y & 1;
+#pragma unroll
+    for (int io = 0; io < 2; ++io) {
+      const int q = 2 * io + jo, t2 = y - G::ys(q);
+      const int xa = x0 + io, xb = x0 + io + 2 * (VW / 2 - 1);  // first and last cell of parity io
+      cw[io] = G::cbase(q) + (t2 >> 1) * G::NXC + ((xa - G::XS(io)) >> 1);
+      cv[io] = t2 >= 0 && t2 < 2 * G::ny(q) && xa >= G::XS(io) && xb <= G::XS(io) + 2 * (G::NXC - 1);
+    }
+  }
+};
+
+// Store one 16-byte group into a stencil field / a centre field.
+template <class G>
+__device__ __forceinline__ void gs_put_stencil(float* f, const GsSlot<G, 4>& sl, const float4& v) {
+  *reinterpret_cast<float2*>(f + sl.sw) = make_float2(v.x, v.z);
+  *reinterpret_cast<float2*>(f + sl.sw + G::H2) = make_float2(v.y, v.w);
+}
+template <class G>
+__device__ __forceinline__ void gs_put_stencil(double* f, const GsSlot<G, 2>& sl, const double2& v) {
+  f[sl.sw] = v.x;
+  f[sl.sw + G::H2] = v.y;
+}
+template <class G>
+__device__ __forceinline__ void gs_put_centre(float* f, const GsSlot<G, 4>& sl, const float4& v) {
+  if (sl.cv[0]) *reinterpret_cast<float2*>(f + sl.cw[0]) = make_float2(v.x, v.z);
+  if (sl.cv[1]) *reinterpret_cast<float2*>(f + sl.cw[1]) = make_float2(v.y, v.w);
+}
+template <class G>
+__device__ __forceinline__ void gs_put_centre(double* f, const GsSlot<G, 2>& sl, const double2& v) {
+  if (sl.cv[0]) f[sl.cw[0]] = v.x;
+  if (sl.cv[1]) f[sl.cw[1]] = v.y;
+}
+template <class G>
+__device__ __forceinline__ float4 gs_get_stencil(const float* f, int sw) {
+  float2 e = *reinterpret_cast<const float2*>(f + sw);
+  float2 o = *reinterpret_cast<const float2*>(f + sw + G::H2);
+  return make_float4(e.x, o.x, e.y, o.y);
+}
+template <class G>
+__device__ __forceinline__ double2 gs_get_stencil(const double* f, int sw) {
+  return make_double2(f[sw], f[sw + G::H2]);
+}
+
+// All four in-plane colours of one plane P (k%2 == kpar) for one tile (see
+// GsGeom).  The half sweep reads its own planes from src, the neighbour planes
+// P+-1 (not written during the half sweep) from nbr, and writes dst != src,
+// so no tile can read a halo that another tile has already updated.  Needs
+// n >= TX+8 and n >= TY+8.  Stencil fields: 0 phi(P), 1 phi(P-1), 2 phi(P+1),
+// 3-7 f1..f5(P).  Centre fields: 0 rhs(P), 1 f6(P), 2-4 f3,f5,f6(P-1),
+// 5-7 f3,f5,f6(P+1).
 template <class T, int TX, int TY>
 __global__ void __launch_bounds__(256) k_gs_plane(const T* __restrict__ src, const T* __restrict__ nbr,
                                                   T* __restrict__ dst, const T* __restrict__ rhs,
                                                   const T* __restrict__ coef, int n, T dx2, int kpar) {
-  constexpr int HB = 4, W = TX + 2 * HB, HT = TY + 2 * HB, S = W * HT;
+  typedef GsGeom<T, TX, TY> G;
+  constexpr int HB = G::HB, W = G::W, HT = G::HT, H2 = G::H2, NXC = G::NXC, Q = G::Q, OFFB = G::OFFB;
+  constexpr int SF = G::SF, NC = G::NC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
+  T* sc = sm + G::NSF * SF;
   const i64 n2 = (i64)n * n, n3 = n2 * n;
   const int i0 = blockIdx.x * TX - HB, j0 = blockIdx.y * TY - HB, k = 2 * blockIdx.z + kpar;
   const int kmn = wm(k, n), kpn = wp(k, n);
   // 16-byte loads: a row segment of the tile starts 16-byte aligned (i0 is a
   // multiple of 4 elements) and a 16-byte group never straddles the periodic
   // wrap (n is a multiple of the group), so each group is one aligned load.
-  // Each tile row is stored parity-split (even x first, then odd x), so the
-  // cells of one colour and each of their x-neighbours are contiguous in
-  // shared memory and a colour phase reads it without bank conflicts.
   typedef typename Vec16<T>::type V;
-  constexpr int VW = 16 / (int)sizeof(T), NV = W / VW, NVT = NV * HT, H2 = W / 2;
+  constexpr int VW = 16 / (int)sizeof(T), NV = W / VW, NVT = NV * HT;
   const V* vsrc = reinterpret_cast<const V*>(src);
   const V* vnbr = reinterpret_cast<const V*>(nbr);
   const V* vrhs = reinterpret_cast<const V*>(rhs);
@@ -356,58 +500,64 @@ __global__ void __launch_bounds__(256) k_gs_plane(const T* __restrict__ src, con
     gj += (gj < 0) ? n : ((gj >= n) ? -n : 0);
     const i64 b = (i64)gi + (i64)n * gj;
     const i64 cP = (b + n2 * k) / VW, cm = (b + n2 * kmn) / VW, cp = (b + n2 * kpn) / VW;
-    T* row = sm + y * W;
-    SplitRow<T>::store(row + 0 * S, H2, x0, vsrc[cP]);
-    SplitRow<T>::store(row + 1 * S, H2, x0, vrhs[cP]);
+    V v[16];
+    v[0] = vsrc[cP];
+    v[1] = vnbr[cm];
+    v[2] = vnbr[cp];
 #pragma unroll
-    for (int f = 0; f < 6; ++f) SplitRow<T>::store(row + (2 + f) * S, H2, x0, vcoef[f * nv3 + cP]);
-    SplitRow<T>::store(row + 8 * S, H2, x0, vnbr[cm]);
-    SplitRow<T>::store(row + 9 * S, H2, x0, vnbr[cp]);
-    SplitRow<T>::store(row + 10 * S, H2, x0, vcoef[2 * nv3 + cm]);
-    SplitRow<T>::store(row + 11 * S, H2, x0, vcoef[4 * nv3 + cm]);
-    SplitRow<T>::store(row + 12 * S, H2, x0, vcoef[5 * nv3 + cm]);
-    SplitRow<T>::store(row + 13 * S, H2, x0, vcoef[2 * nv3 + cp]);
-    SplitRow<T>::store(row + 14 * S, H2, x0, vcoef[4 * nv3 + cp]);
-    SplitRow<T>::store(row + 15 * S, H2, x0, vcoef[5 * nv3 + cp]);
+    for (int f = 0; f < 5; ++f) v[3 + f] = vcoef[f * nv3 + cP];
+    v[8] = vrhs[cP];
+    v[9] = vcoef[5 * nv3 + cP];
+    v[10] = vcoef[2 * nv3 + cm];
+    v[11] = vcoef[4 * nv3 + cm];
+    v[12] = vcoef[5 * nv3 + cm];
+    v[13] = vcoef[2 * nv3 + cp];
+    v[14] = vcoef[4 * nv3 + cp];
+    v[15] = vcoef[5 * nv3 + cp];
+    const GsSlot<G, VW> sl(x0, y);
+#pragma unroll
+    for (int f = 0; f < 8; ++f) gs_put_stencil<G>(sm + f * SF, sl, v[f]);
+#pragma unroll
+    for (int f = 0; f < 8; ++f) gs_put_centre<G>(sc + f * NC, sl, v[8 + f]);
   }
   __syncthreads();
-  const T* sP = sm;
-  const T* sR = sm + S;
-  const T* F1 = sm + 2 * S;
-  const T* F2 = sm + 3 * S;
-  const T* F3 = sm + 4 * S;
-  const T* F4 = sm + 5 * S;
-  const T* F5 = sm + 6 * S;
-  const T* F6 = sm + 7 * S;
-  const T* sKm = sm + 8 * S;
-  const T* sKp = sm + 9 * S;
+  T* sP = sm;
+  const T* sKm = sm + 1 * SF;
+  const T* sKp = sm + 2 * SF;
+  const T* F1 = sm + 3 * SF;
+  const T* F2 = sm + 4 * SF;
+  const T* F3 = sm + 5 * SF;
+  const T* F4 = sm + 6 * SF;
+  const T* F5 = sm + 7 * SF;
 #pragma unroll 1
   for (int q = 0; q < 4; ++q) {
-    const int io = q >> 1, jo = q & 1, r = 3 - q;
-    const int xs = HB - r + ((HB - r) & 1 ? (io ? 0 : 1) : io);
-    const int ys = HB - r + ((HB - r) & 1 ? (jo ? 0 : 1) : jo);
-    const int nx = (HB + TX + r - xs + 1) / 2, ny = (HB + TY + r - ys + 1) / 2;
-    // offsets from (row + x/2) of the cell and of its x+1 / x-1 neighbours
-    const int oc = io * H2, oxp = (1 - io) * H2 + io, oxm = (1 - io) * H2 + io - 1;
-    for (int e = threadIdx.x; e < nx * ny; e += blockDim.x) {
-      const int x = xs + 2 * (e % nx), y = ys + 2 * (e / nx);
-      const int base = y * W + (x >> 1);
-      const int c = base + oc, cxp = base + oxp, cxm = base + oxm;
+    const int io = q >> 1, jo = q & 1;
+    const int cnt = NXC * G::ny(q);
+    // word offsets of the x+-1 and y+-1 neighbours (constant within a colour)
+    const int oxp = io ? 1 - H2 : H2, oxm = io ? -H2 : H2 - 1;
+    const int oyp = jo ? Q - OFFB : OFFB, oym = jo ? -OFFB : OFFB - Q;
+    const T* cen = sc + G::cbase(q);
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      const int m = e % NXC, t = e / NXC;
+      const int c = G::word(G::XS(io) + 2 * m, G::ys(q) + 2 * t);
+      const int cxp = c + oxp, cxm = c + oxm, cyp = c + oyp, cym = c + oym;
       Stencil<T> st;
-      st.c = sP[c]; st.ip = sP[cxp]; st.im = sP[cxm]; st.jp = sP[c + W]; st.jm = sP[c - W];
+      st.c = sP[c]; st.ip = sP[cxp]; st.im = sP[cxm]; st.jp = sP[cyp]; st.jm = sP[cym];
       st.kp = sKp[c]; st.km = sKm[c];
-      st.ppk = sP[cxp + W]; st.mpk = sP[cxm + W]; st.pmk = sP[cxp - W]; st.mmk = sP[cxm - W];
-      st.jpkp = sKp[c + W]; st.jmkp = sKp[c - W]; st.jpkm = sKm[c + W]; st.jmkm = sKm[c - W];
+      st.ppk = sP[cxp + oyp]; st.mpk = sP[cxm + oyp]; st.pmk = sP[cxp + oym]; st.mmk = sP[cxm + oym];
+      st.jpkp = sKp[cyp]; st.jmkp = sKp[cym]; st.jpkm = sKm[cyp]; st.jmkm = sKm[cym];
       st.ipkp = sKp[cxp]; st.imkp = sKp[cxm]; st.ipkm = sKm[cxp]; st.imkm = sKm[cxm];
       st.f1c = F1[c]; st.f1ip = F1[cxp]; st.f1im = F1[cxm];
-      st.f4c = F4[c]; st.f4jp = F4[c + W]; st.f4jm = F4[c - W];
-      st.f6c = F6[c]; st.f6kp = sm[15 * S + c]; st.f6km = sm[12 * S + c];
-      st.f2jp = F2[c + W]; st.f2jm = F2[c - W]; st.f2ip = F2[cxp]; st.f2im = F2[cxm];
-      st.f5kp = sm[14 * S + c]; st.f5km = sm[11 * S + c]; st.f5jp = F5[c + W]; st.f5jm = F5[c - W];
-      st.f3kp = sm[13 * S + c]; st.f3km = sm[10 * S + c]; st.f3ip = F3[cxp]; st.f3im = F3[cxm];
+      st.f4c = F4[c]; st.f4jp = F4[cyp]; st.f4jm = F4[cym];
+      st.f2jp = F2[cyp]; st.f2jm = F2[cym]; st.f2ip = F2[cxp]; st.f2im = F2[cxm];
+      st.f5jp = F5[cyp]; st.f5jm = F5[cym];
+      st.f3ip = F3[cxp]; st.f3im = F3[cxm];
+      st.f6c = cen[1 * NC + e];
+      st.f3km = cen[2 * NC + e]; st.f5km = cen[3 * NC + e]; st.f6km = cen[4 * NC + e];
+      st.f3kp = cen[5 * NC + e]; st.f5kp = cen[6 * NC + e]; st.f6kp = cen[7 * NC + e];
       T tdiag, t1, t2;
       op_eval(st, tdiag, t1, t2);
-      sm[c] = (sR[c] * dx2 - t1 - t2) / tdiag;
+      sP[c] = (cen[e] * dx2 - t1 - t2) / tdiag;
     }
     __syncthreads();
   }
@@ -415,18 +565,20 @@ __global__ void __launch_bounds__(256) k_gs_plane(const T* __restrict__ src, con
   V* vdst = reinterpret_cast<V*>(dst);
   for (int e = threadIdx.x; e < NVI * TY; e += blockDim.x) {
     const int x0 = HB + (e % NVI) * VW, y = HB + e / NVI;
-    vdst[((i64)(i0 + x0) + (i64)n * (j0 + y) + n2 * k) / VW] = SplitRow<T>::load(sm + y * W, H2, x0);
+    vdst[((i64)(i0 + x0) + (i64)n * (j0 + y) + n2 * k) / VW] = gs_get_stencil<G>(sP, G::word(x0, y));
   }
 }
 
 // Residual r = rhs - L[phi] on every cell (calcresid), max-norm into maxbits.
-// r may be null; r32 (float copy of the residual) may be null.
-template <class T>
+// r may be null; r32 (float copy of the residual) may be null.  Contract
+// only names a separate instantiation: the translation unit that instantiates
+// it decides whether multiply-adds are fused.
+template <class T, bool Contract = false>
 __global__ void k_residual(const T* __restrict__ phi, const T* __restrict__ rhs, const T* __restrict__ coef, int n,
                            T di2, T* __restrict__ r, float* __restrict__ r32, unsigned long long* maxbits) {
   i64 n3 = (i64)n * n * n;
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  double m = 0.0;
+  T m = T(0);
   if (t < n3) {
     int i, j, k;
     cell_of(t, n, i, j, k);
@@ -435,7 +587,7 @@ __global__ void k_residual(const T* __restrict__ phi, const T* __restrict__ rhs,
     T tr = rhs[t] - (t1 + t2 + tdiag * phi[t]) * di2;
     if (r) r[t] = tr;
     if (r32) r32[t] = (float)tr;
-    m = fabs((double)tr);
+    m = fabs(tr);
   }
   if (maxbits) block_max_commit(m, maxbits);
 }

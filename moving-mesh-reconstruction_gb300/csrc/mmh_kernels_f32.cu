@@ -6,4 +6,16 @@
 namespace mmh {
 MMH_INSTANTIATE(float)
 MMH_INSTANTIATE_PCG(float)
+
+// FP64 residual with fused multiply-adds, for the outer loop of the mixed
+// form (fewer FP64 operations; that form is not bit-matched to the oracle).
+void launch_residual_fma(const double* phi, const double* rhs, const double* coef, int n, double dx, float* r32,
+                         unsigned long long* maxbits, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  double di2 = 1.0 / (dx * dx);
+  prof_begin(KK_RESIDUAL, s, n3, n);
+  k_residual<double, true><<<grid_of(n3, kBlock), kBlock, 0, s>>>(phi, rhs, coef, n, di2, nullptr, r32, maxbits);
+  prof_end(KK_RESIDUAL, s, n);
+  count_launch();
+}
 }  // namespace mmh

@@ -264,12 +264,45 @@ void launch_limiter_pass1(double* tmp, const double* def, const double* rho, int
   count_launch();
 }
 
-__global__ void k_limiter_mask(double* __restrict__ defplim, const double* __restrict__ def,
-                               const double* __restrict__ defp, int n, double dtold, double cmpmaxglobal, LimDev* st,
-                               uint8_t* __restrict__ mask) {
+// Bounds of the smallest eigenvalue that compression_of computes, from the
+// values it computes first (mu = trace/3, am): every root r_i = am*cos(.)
+// lies in [-am, am] and rounding is monotone, so min_i fl(r_i + mu) >=
+// fl(mu - am) = lo.  The root through theta + 2pi/3 has cos <= -1/2 up to
+// rounding, so the minimum is <= mu - am/2 + rounding < hi.
+__device__ __forceinline__ void compression_bounds(double c11, double c12, double c13, double c22, double c23,
+                                                   double c33, double& lo, double& hi) {
+  double trace = c11 + c22 + c33;
+  double mu = trace / 3.0;
+  double d11 = c11 - mu;
+  double d22 = c22 - mu;
+  double a = -(d11 * d11 + c12 * c12 + c13 * c13 + d11 * d22 + d22 * d22 + c23 * c23);
+  if (fabs(a) < 1.e-20) a = 1.e-20;
+  double am = 2.0 * sqrt(fabs(-a) / 3.0);
+  lo = mu - am;
+  hi = (mu - 0.49 * am) + 1e-14 * (fabs(mu) + am);
+}
+
+// Final compression test (limiter.f90:498-533): defplim = tlim where tlim > 0,
+// the count of such cells, and cmax = max compression.  The trigonometric
+// evaluation is exact only where it can matter.  A cell with lo > 1/cmpmax
+// has tlim < 0 for certain.  Such a cell can be skipped for cmax too when its
+// upper bound 1/lo is below the compression of a cell that is evaluated: the
+// block's cell with the smallest hi, or any cell already folded into the
+// global maximum.  The cells left are compacted so whole warps evaluate them.
+__global__ void __launch_bounds__(256) k_limiter_mask(double* __restrict__ defplim, const double* __restrict__ def,
+                                                      const double* __restrict__ defp, int n, double dtold,
+                                                      double cmpmaxglobal, LimDev* st, uint8_t* __restrict__ mask) {
+  __shared__ double s_c[6][256];
+  __shared__ int s_list[256];
+  __shared__ int s_cnt;
+  __shared__ unsigned long long s_buf[32];
+  __shared__ unsigned long long s_lam;
   i64 n3 = (i64)n * n * n;
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long cnt = 0, cm = ord_of(0.0);
+  if (threadIdx.x == 0) s_cnt = 0;
+  const double cmpmax = cmpmaxglobal * 1.0;
+  double c[6] = {0, 0, 0, 0, 0, 0};
+  double lo = 0.0, hi = 0.0;
   if (t < n3) {
     int i, j, k;
     cell_of(t, n, i, j, k);
@@ -290,21 +323,49 @@ __global__ void k_limiter_mask(double* __restrict__ defplim, const double* __res
     phixz = phixz + (D_(ip, j, kp) - D_(im, j, kp) - D_(ip, j, km) + D_(im, j, km)) / 4.0;
 #undef P_
 #undef D_
-    double compression = compression_of(1.0 + phixx, phixy, phixz, 1.0 + phiyy, phiyz, 1.0 + phizz);
-    double cmpmax = cmpmaxglobal * 1.0;
+    c[0] = 1.0 + phixx; c[1] = phixy; c[2] = phixz; c[3] = 1.0 + phiyy; c[4] = phiyz; c[5] = 1.0 + phizz;
+    compression_bounds(c[0], c[1], c[2], c[3], c[4], c[5], lo, hi);
+  }
+  const bool pd = t < n3 && lo > 0.0;
+  // smallest upper bound of the block's positive definite cells
+  unsigned long long lam = block_u64(pd ? ord_of(hi) : ord_of(INFINITY), s_buf, 2);
+  if (threadIdx.x == 0) s_lam = lam;
+  __syncthreads();
+  const double lam_b = from_ord(s_lam);
+  // the largest compression folded in so far (exact values of evaluated cells)
+  const double tg = from_ord(*(volatile unsigned long long*)&st->cmax);
+  const double lam_g = tg > 0.0 ? (1.0 / tg) * (1.0 + 1e-15) : INFINITY;
+  const bool skip = pd && dtold > 0.0 && lo > (1.0 / cmpmax) * (1.0 + 1e-12) && (lo > lam_b || lo >= lam_g);
+  if (t < n3) {
+    if (skip) {
+      defplim[t] = 0.0;
+      if (mask) mask[t] = 0;
+    } else {
+      int pos = atomicAdd(&s_cnt, 1);
+      s_list[pos] = threadIdx.x;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) s_c[q][pos] = c[q];
+    }
+  }
+  __syncthreads();
+  unsigned long long cnt = 0, cm = ord_of(0.0);
+  const int ncand = s_cnt;
+  for (int q = threadIdx.x; q < ncand; q += blockDim.x) {
+    const i64 tt = (i64)blockIdx.x * blockDim.x + s_list[q];
+    double compression = compression_of(s_c[0][q], s_c[1][q], s_c[2][q], s_c[3][q], s_c[4][q], s_c[5][q]);
     double tlim = 3.0 * (1.0 / cmpmax - 1.0 / compression) / dtold;
-    cm = ord_of(fmax(0.0, compression));
+    unsigned long long o = ord_of(fmax(0.0, compression));
+    cm = o > cm ? o : cm;
     double v = 0.0;
     uint8_t mk = 0;
     if (tlim > 0.0) {
-      cnt = 1;
+      cnt += 1;
       v = tlim;
       mk = 1;
     }
-    defplim[t] = v;
-    if (mask) mask[t] = mk;
+    defplim[tt] = v;
+    if (mask) mask[tt] = mk;
   }
-  __shared__ unsigned long long s_buf[32];
   unsigned long long r = block_u64(cnt, s_buf, 0);
   if (threadIdx.x == 0 && r) atomicAdd(&st->ncompress, r);
   r = block_u64(cm, s_buf, 1);
@@ -338,7 +399,7 @@ void launch_lim_reset(LimDev* st, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // Spectral kernels
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double2 spec_mode(double2 x, int kx, int ky, int kz, int n, int mode) {
+__device__ __forceinline__ double2 spec_mode(double2 x, int kx, int ky, int kz, int n, int mode, const double* ctab) {
   const double pi = 3.14159265358979323846264338328;
   double re = x.x, im = x.y;
   if (mode <= 2) {
@@ -363,11 +424,9 @@ __device__ __forceinline__ double2 spec_mode(double2 x, int kx, int ky, int kz, 
     double f = k1 * k1 + k2 * k2 + k3 * k3;
     return make_double2(re * f, im * f);
   } else {
-    // / (2cos kx + 2cos ky + 2cos kz - 6), DC real part zeroed (limiter.f90:561-576)
-    double xk = 2 * pi * kx / n;
-    double yk = 2 * pi * (ky + 1 - 1.) / n;
-    double zk = 2 * pi * (kz + 1 - 1.) / n;
-    double akernel = 2 * cos(xk) + 2 * cos(yk) + 2 * cos(zk) - 6;
+    // / (2cos kx + 2cos ky + 2cos kz - 6), DC real part zeroed (limiter.f90:561-576);
+    // ctab[k] = cos(2 pi k / n), the reference's angles (ky + 1 - 1. is ky exactly)
+    double akernel = 2 * ctab[kx] + 2 * ctab[ky] + 2 * ctab[kz] - 6;
     if (fabs(akernel) < 1e-10) akernel = 1;
     double r2 = re / akernel, i2 = im / akernel;
     if (kx == 0 && ky == 0 && kz == 0) r2 = 0.0;
@@ -375,26 +434,44 @@ __device__ __forceinline__ double2 spec_mode(double2 x, int kx, int ky, int kz, 
   }
 }
 
+// Tables of the spectral kernels, computed once per context with the same
+// expressions the kernels used: tab[2kx], tab[2kx+1] = cos, sin(-2 pi kx / n)
+// for kx < n/2 (the packing twiddle), tab[n + k] = cos(2 pi k / n).
+__global__ void k_spec_tables(double* tab, int n) {
+  const double pi = 3.14159265358979323846264338328;
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  if (k < n / 2) {
+    double th = -2.0 * pi * k / n;
+    tab[2 * k] = cos(th);
+    tab[2 * k + 1] = sin(th);
+  }
+  tab[n + k] = cos(2 * pi * k / n);
+}
+void launch_spec_tables(double* tab, int n, cudaStream_t s) {
+  k_spec_tables<<<grid_of(n, kBlock), kBlock, 0, s>>>(tab, n);
+  count_launch();
+}
+
 __global__ void k_spec_pack(const double2* __restrict__ Xc, int n, int mode, double2* __restrict__ Z,
-                            const LimDev* st) {
+                            const LimDev* st, const double* __restrict__ tab) {
   if (mode == 4 && st->ncompress == 0) return;
   int M = n / 2, H = M + 1;
   i64 tot = (i64)M * n * n;
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= tot) return;
-  int kx = (int)(t % M);
-  i64 r = t / M;
-  int ky = (int)(r % n), kz = (int)(r / n);
-  int kx2 = M - kx, ky2 = (n - ky) % n, kz2 = (n - kz) % n;
+  const int lgm = __ffs(M) - 1, lgn = lgm + 1;  // n is a power of two
+  int kx = (int)t & (M - 1);
+  int ky = (int)(t >> lgm) & (n - 1), kz = (int)(t >> (lgm + lgn));
+  int kx2 = M - kx, ky2 = (n - ky) & (n - 1), kz2 = (n - kz) & (n - 1);
   // X_NR(k) = conj(Xc(k)) : spectrum with exp(+2 pi i k.x / n)
   double2 a = Xc[kx + (i64)H * (ky + (i64)n * kz)];
   double2 b = Xc[kx2 + (i64)H * (ky2 + (i64)n * kz2)];
-  double2 A = spec_mode(make_double2(a.x, -a.y), kx, ky, kz, n, mode);
-  double2 B = spec_mode(make_double2(b.x, -b.y), kx2, ky2, kz2, n, mode);
+  const double* ctab = tab + n;
+  double2 A = spec_mode(make_double2(a.x, -a.y), kx, ky, kz, n, mode, ctab);
+  double2 B = spec_mode(make_double2(b.x, -b.y), kx2, ky2, kz2, n, mode, ctab);
   B.y = -B.y;  // conj
-  const double pi = 3.14159265358979323846264338328;
-  double th = -2.0 * pi * kx / n;
-  double wr = cos(th), wi = sin(th);
+  double wr = tab[2 * kx], wi = tab[2 * kx + 1];
   double sr = A.x + B.x, si = A.y + B.y;
   double dr = A.x - B.x, di = A.y - B.y;
   double wdr = wr * dr - wi * di, wdi = wr * di + wi * dr;
@@ -402,9 +479,9 @@ __global__ void k_spec_pack(const double2* __restrict__ Xc, int n, int mode, dou
   Z[t] = make_double2(0.5 * sr - 0.5 * wdi, 0.5 * si + 0.5 * wdr);
 }
 
-void launch_spec_pack(const void* Xc, int n, int mode, void* Z, const LimDev* st, cudaStream_t s) {
+void launch_spec_pack(const void* Xc, int n, int mode, void* Z, const LimDev* st, const double* tab, cudaStream_t s) {
   i64 tot = (i64)(n / 2) * n * n;
-  k_spec_pack<<<grid_of(tot, kBlock), kBlock, 0, s>>>((const double2*)Xc, n, mode, (double2*)Z, st);
+  k_spec_pack<<<grid_of(tot, kBlock), kBlock, 0, s>>>((const double2*)Xc, n, mode, (double2*)Z, st, tab);
   count_launch();
 }
 
@@ -436,15 +513,37 @@ void launch_spec_unpack(const void* z, int n, double* out, int stride_out, int a
 // ---------------------------------------------------------------------------
 // relaxing-TVD, density component (relaxing.f90).  u(2:5) = 0, so the Euler
 // flux of the density is the zero momentum and the pressure vanishes; the
-// expressions below keep the reference's operations on those zero components.
+// results are those of the reference's operations on those zero components.
+// FP64 arithmetic dominates these kernels, so each keeps only the operations
+// whose result is not already known exactly.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double zdiv(double d) { return 0.0 / d; }
+
+// 0.0 / d with IEEE semantics: a signed zero for finite non-zero and infinite
+// d, the division itself (NaN) only for zero or NaN d.
+__device__ __forceinline__ double zdiv(double d) { return (d == d && d != 0.0) ? copysign(0.0, d) : 0.0 / d; }
+// biased binary exponent: 0 for zero and subnormals, 2047 for inf and NaN
+__device__ __forceinline__ int bexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
+
+// dpv (relaxing.f90:269-496) forms, at every stencil point along axis a, the
+// flux w_a = v_a / c divided by the freezing speed and then only the half sums
+// (u + w_a)/2 and half differences (u - w_a)/2.  Those six values per cell
+// are computed once here: sd[a] = (u + w_a)/2, sd[3 + a] = (u - w_a)/2.
+__device__ __forceinline__ void store_sd(double* __restrict__ sd, i64 n3, i64 t, double u0, double wx, double wy,
+                                         double wz) {
+  sd[0 * n3 + t] = (u0 + wx) / 2.0;
+  sd[1 * n3 + t] = (u0 + wy) / 2.0;
+  sd[2 * n3 + t] = (u0 + wz) / 2.0;
+  sd[3 * n3 + t] = (u0 - wx) / 2.0;
+  sd[4 * n3 + t] = (u0 - wy) / 2.0;
+  sd[5 * n3 + t] = (u0 - wz) / 2.0;
+}
 
 // stage 1: calcbaj + cflkeuler + flux of u at every cell.
-// baj: 7 planes (b11,b12,b13,b22,b23,b33,det); vt: 3 planes (flux along x,y,z)
+// baj: 7 planes (b11,b12,b13,b22,b23,b33,det); cc: freezing speed; sd: the
+// half sums and differences of store_sd.
 __global__ void k_relax_stage1(const double* __restrict__ rho, const double* __restrict__ def,
                                const double* __restrict__ defp, int n, double* __restrict__ baj,
-                               double* __restrict__ cc, double* __restrict__ vt) {
+                               double* __restrict__ cc, double* __restrict__ sd) {
   i64 n3 = (i64)n * n * n;
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n3) return;
@@ -464,29 +563,41 @@ __global__ void k_relax_stage1(const double* __restrict__ rho, const double* __r
   double dyp = defp[IDX(i, jp, k, n)], dym = defp[IDX(i, jm, k, n)];
   double dzp = defp[IDX(i, j, kp, n)], dzm = defp[IDX(i, j, km, n)];
   double u0 = rho[t];
+  double c;
   // cflkeuler (relaxing.f90:1097-1135)
   {
     double pdx = (dxp - dxm) / 2.0, pdy = (dyp - dym) / 2.0, pdz = (dzp - dzm) / 2.0;
     double det = m.det;
-    double vx = zdiv(u0), vy = zdiv(u0), vz = zdiv(u0);
-    double rhoc = u0 / det;
-    double kin = rhoc * (vx * vx + vy * vy + vz * vz) / 2.0;
-    double ed = zdiv(det) - kin;
-    double pressure = (gamma - 1.0) * ed;
-    double cs = sqrt(gamma * fabs(pressure / rhoc));
+    double vx = zdiv(u0), vy = vx, vz = vx;
     double v1 = vx - pdx, v2 = vy - pdy, v3 = vz - pdz;
     double vv1 = m.b11 * v1 + m.b12 * v2 + m.b13 * v3;
     double vv2 = m.b12 * v1 + m.b22 * v2 + m.b23 * v3;
     double vv3 = m.b13 * v1 + m.b23 * v2 + m.b33 * v3;
-    double blim1 = cs * sqrt(m.b11 * m.b11 + m.b12 * m.b12 + m.b13 * m.b13) + fabs(vv1);
-    double blim2 = cs * sqrt(m.b12 * m.b12 + m.b22 * m.b22 + m.b23 * m.b23) + fabs(vv2);
-    double blim3 = cs * sqrt(m.b13 * m.b13 + m.b23 * m.b23 + m.b33 * m.b33) + fabs(vv3);
-    cc[t] = fmax(fmax(blim1, blim2), blim3);
+    // With u0 and det finite and non-zero, u0/det finite and non-zero and every
+    // b finite below 2^500, the kinetic and internal energies are signed
+    // zeros, so the sound speed cs is +0, cs*sqrt(...) is +0 and each bound is
+    // |vv|: the same bits as the full expression, which runs otherwise.
+    const int eu = bexp(u0), ed = bexp(det);
+    const int eb = max(max(max(bexp(m.b11), bexp(m.b12)), max(bexp(m.b13), bexp(m.b22))), max(bexp(m.b23), bexp(m.b33)));
+    if (eu >= 1 && eu <= 2046 && ed >= 1 && ed <= 2046 && abs(eu - ed) <= 1000 && eb <= 1523) {
+      c = fmax(fmax(fabs(vv1), fabs(vv2)), fabs(vv3));
+    } else {
+      double rhoc = u0 / det;
+      double kin = rhoc * (vx * vx + vy * vy + vz * vz) / 2.0;
+      double edn = zdiv(det) - kin;
+      double pressure = (gamma - 1.0) * edn;
+      double cs = sqrt(gamma * fabs(pressure / rhoc));
+      double blim1 = cs * sqrt(m.b11 * m.b11 + m.b12 * m.b12 + m.b13 * m.b13) + fabs(vv1);
+      double blim2 = cs * sqrt(m.b12 * m.b12 + m.b22 * m.b22 + m.b23 * m.b23) + fabs(vv2);
+      double blim3 = cs * sqrt(m.b13 * m.b13 + m.b23 * m.b23 + m.b33 * m.b33) + fabs(vv3);
+      c = fmax(fmax(blim1, blim2), blim3);
+    }
+    cc[t] = c;
   }
   // flux (relaxing.f90:970-988) of the density
   {
     double rg = m.det;
-    double mx = zdiv(rg), my = zdiv(rg), mz = zdiv(rg);
+    double mx = zdiv(rg), my = mx, mz = mx;
     double pdxg = (dxp - dxm) / 2.0 / rg;
     double pdyg = (dyp - dym) / 2.0 / rg;
     double pdzg = (dzp - dzm) / 2.0 / rg;
@@ -494,21 +605,23 @@ __global__ void k_relax_stage1(const double* __restrict__ rho, const double* __r
     double vtt1 = mx - u0 * pdxg;
     double vtt2 = my - u0 * pdyg;
     double vtt3 = mz - u0 * pdzg;
-    vt[0 * n3 + t] = b11 * vtt1 + b12 * vtt2 + b13 * vtt3;
-    vt[1 * n3 + t] = b12 * vtt1 + b22 * vtt2 + b23 * vtt3;
-    vt[2 * n3 + t] = b13 * vtt1 + b23 * vtt2 + b33 * vtt3;
+    store_sd(sd, n3, t, u0, (b11 * vtt1 + b12 * vtt2 + b13 * vtt3) / c, (b12 * vtt1 + b22 * vtt2 + b23 * vtt3) / c,
+             (b13 * vtt1 + b23 * vtt2 + b33 * vtt3) / c);
   }
 }
 
 void launch_relax_stage1(const double* rho, const double* def, const double* defp, int n, double* baj, double* cc,
-                         double* vt, cudaStream_t s) {
+                         double* sd, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
-  k_relax_stage1<<<grid_of(n3, kBlock), kBlock, 0, s>>>(rho, def, defp, n, baj, cc, vt);
+  k_relax_stage1<<<grid_of(n3, kBlock), kBlock, 0, s>>>(rho, def, defp, n, baj, cc, sd);
   count_launch();
 }
 
+// flux of the half-step state u1 with the metric of stage 1 (relaxing.f90:
+// 970-988), as the half sums and differences of store_sd.
 __global__ void k_relax_flux(const double* __restrict__ u1, const double* __restrict__ defp,
-                             const double* __restrict__ baj, int n, double* __restrict__ vt) {
+                             const double* __restrict__ baj, const double* __restrict__ cc, int n,
+                             double* __restrict__ sd) {
   i64 n3 = (i64)n * n * n;
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n3) return;
@@ -517,7 +630,8 @@ __global__ void k_relax_flux(const double* __restrict__ u1, const double* __rest
   int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
   double rg = baj[6 * n3 + t];
   double u0 = u1[t];
-  double mx = zdiv(rg), my = zdiv(rg), mz = zdiv(rg);
+  double c = cc[t];
+  double mx = zdiv(rg), my = mx, mz = mx;
   double pdxg = (defp[IDX(ip, j, k, n)] - defp[IDX(im, j, k, n)]) / 2.0 / rg;
   double pdyg = (defp[IDX(i, jp, k, n)] - defp[IDX(i, jm, k, n)]) / 2.0 / rg;
   double pdzg = (defp[IDX(i, j, kp, n)] - defp[IDX(i, j, km, n)]) / 2.0 / rg;
@@ -526,103 +640,109 @@ __global__ void k_relax_flux(const double* __restrict__ u1, const double* __rest
   double vtt1 = mx - u0 * pdxg;
   double vtt2 = my - u0 * pdyg;
   double vtt3 = mz - u0 * pdzg;
-  vt[0 * n3 + t] = b11 * vtt1 + b12 * vtt2 + b13 * vtt3;
-  vt[1 * n3 + t] = b12 * vtt1 + b22 * vtt2 + b23 * vtt3;
-  vt[2 * n3 + t] = b13 * vtt1 + b23 * vtt2 + b33 * vtt3;
+  store_sd(sd, n3, t, u0, (b11 * vtt1 + b12 * vtt2 + b13 * vtt3) / c, (b12 * vtt1 + b22 * vtt2 + b23 * vtt3) / c,
+           (b13 * vtt1 + b23 * vtt2 + b33 * vtt3) / c);
 }
 
-void launch_relax_flux(const double* u1, const double* defp, const double* baj, int n, double* vt, cudaStream_t s) {
+void launch_relax_flux(const double* u1, const double* defp, const double* baj, const double* cc, int n, double* sd,
+                       cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
-  k_relax_flux<<<grid_of(n3, kBlock), kBlock, 0, s>>>(u1, defp, baj, n, vt);
+  k_relax_flux<<<grid_of(n3, kBlock), kBlock, 0, s>>>(u1, defp, baj, cc, n, sd);
   count_launch();
 }
 
 __device__ __forceinline__ double fsign1(double a) { return a >= 0.0 ? 1.0 : -1.0; }
+// minmod of relaxing.f90 with wslopelim = 1.5, wbee = 1:
+//   mm = min(1.5*lo, 1*hi + 0*lo), result (sign(a) + sign(b)) * mm / 2.
+// For finite lo, 1*hi + 0*lo is hi; for mm below 2^1023, (+-2)*mm/2 is +-mm
+// and 0*mm/2 is +0.  Those cases skip the multiplications; the others run
+// the expression as written.
 __device__ __forceinline__ double minmod(double a, double b) {
   const double wslopelim = 1.5, wbee = 1.0;
   double x = fabs(a), y = fabs(b);
   double lo = fmin(x, y), hi = fmax(x, y);
-  double mm = fmin(wslopelim * lo, wbee * hi + (1.0 - wbee) * lo);
+  double mm = bexp(lo) < 2047 ? fmin(wslopelim * lo, hi) : fmin(wslopelim * lo, wbee * hi + (1.0 - wbee) * lo);
+  if (bexp(mm) < 2046) {
+    const bool pa = a >= 0.0, pb = b >= 0.0;
+    return pa != pb ? 0.0 : (pa ? mm : -mm);
+  }
   return (fsign1(a) + fsign1(b)) * mm / 2.0;
 }
-__device__ __forceinline__ double wphalf(double um, double vm, double u0, double v0, double up, double vp, double upp,
-                                         double vpp) {
-  double a = (u0 + v0) / 2.0;
-  double b = (up - vp) / 2.0;
-  double da = (up + vp) / 2.0 - a;
-  double dam = a - (um + vm) / 2.0;
+// wphalf (relaxing.f90) from the half sums s = (u+w)/2 at the cells -1, 0, +1
+// and the half differences d = (u-w)/2 at the cells 0, +1, +2 of the face.
+__device__ __forceinline__ double wphalf_sd(double sm, double s0, double sp, double d0, double dp, double dpp) {
+  double a = s0;
+  double b = dp;
+  double da = sp - a;
+  double dam = a - sm;
   double ap = a + minmod(dam, da) / 2.0;
-  double db = (upp - vpp) / 2.0 - b;
-  double dbm = b - (u0 - v0) / 2.0;
+  double db = dpp - b;
+  double dbm = b - d0;
   double bp = b - minmod(db, dbm) / 2.0;
   return ap - bp;
 }
 
-// dpv (relaxing.f90:269-496) for the density, then out = ubase - res*dt.
-__global__ void k_relax_dpv(const double* __restrict__ u, const double* __restrict__ vt,
-                            const double* __restrict__ cc, int n, const double* __restrict__ ubase, double dt,
+// Face fluxes of dpv (relaxing.f90:269-496): g_a[cell] is the flux through
+// the upper face of the cell along axis a, (c(+1) + c(0))/2 * wphalf over the
+// cells -1, 0, +1, +2 of that axis.  dpv takes the difference of the upper
+// and the lower face of each cell; the lower face is the upper face of the
+// neighbour below, computed from the same operands in the same order, so each
+// face is evaluated once here instead of once from each side.
+__global__ void k_relax_faces(const double* __restrict__ sd, const double* __restrict__ cc, int n,
+                              double* __restrict__ g) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  int i, j, k;
+  cell_of(t, n, i, j, k);
+  const double c0 = cc[t];
+  {
+    int im = wm(i, n), ip = wp(i, n), ipp = wp(ip, n);
+    i64 a = IDX(im, j, k, n), b = IDX(ip, j, k, n), d = IDX(ipp, j, k, n);
+    const double* S = sd;
+    const double* D = sd + 3 * n3;
+    double fl = wphalf_sd(S[a], S[t], S[b], D[t], D[b], D[d]);
+    g[t] = (cc[b] + c0) / 2.0 * fl;
+  }
+  {
+    int jm = wm(j, n), jp = wp(j, n), jpp = wp(jp, n);
+    i64 a = IDX(i, jm, k, n), b = IDX(i, jp, k, n), d = IDX(i, jpp, k, n);
+    const double* S = sd + n3;
+    const double* D = sd + 4 * n3;
+    double fl = wphalf_sd(S[a], S[t], S[b], D[t], D[b], D[d]);
+    g[n3 + t] = (cc[b] + c0) / 2.0 * fl;
+  }
+  {
+    int km = wm(k, n), kp = wp(k, n), kpp = wp(kp, n);
+    i64 a = IDX(i, j, km, n), b = IDX(i, j, kp, n), d = IDX(i, j, kpp, n);
+    const double* S = sd + 2 * n3;
+    const double* D = sd + 5 * n3;
+    double fl = wphalf_sd(S[a], S[t], S[b], D[t], D[b], D[d]);
+    g[2 * n3 + t] = (cc[b] + c0) / 2.0 * fl;
+  }
+}
+
+// dpv residual from the face fluxes, in the reference's order (z, then x,
+// then y), and out = ubase - res*dt.
+__global__ void k_relax_div(const double* __restrict__ g, int n, const double* __restrict__ ubase, double dt,
                             double* __restrict__ out) {
   i64 n3 = (i64)n * n * n;
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n3) return;
   int i, j, k;
   cell_of(t, n, i, j, k);
-  const double* vx = vt;
-  const double* vy = vt + n3;
-  const double* vz = vt + 2 * n3;
-  double ck = cc[t];
-  double r;
-  {
-    double uz[5], wz[5];
-#pragma unroll
-    for (int q = 0; q < 5; ++q) {
-      int kq = ((k + q - 2) % n + n) % n;
-      i64 cq = IDX(i, j, kq, n);
-      uz[q] = u[cq];
-      wz[q] = vz[cq] / cc[cq];
-    }
-    double flz1 = wphalf(uz[0], wz[0], uz[1], wz[1], uz[2], wz[2], uz[3], wz[3]);
-    double flz2 = wphalf(uz[1], wz[1], uz[2], wz[2], uz[3], wz[3], uz[4], wz[4]);
-    double ckp = cc[IDX(i, j, wp(k, n), n)], ckm = cc[IDX(i, j, wm(k, n), n)];
-    r = (ckp + ck) / 2.0 * flz2 - (ck + ckm) / 2.0 * flz1;
-  }
-  {
-    double ux[5], wx[5];
-#pragma unroll
-    for (int q = 0; q < 5; ++q) {
-      int iq = ((i + q - 2) % n + n) % n;
-      i64 cq = IDX(iq, j, k, n);
-      ux[q] = u[cq];
-      wx[q] = vx[cq] / cc[cq];
-    }
-    double flx0 = wphalf(ux[1], wx[1], ux[2], wx[2], ux[3], wx[3], ux[4], wx[4]);
-    double flxm = wphalf(ux[0], wx[0], ux[1], wx[1], ux[2], wx[2], ux[3], wx[3]);
-    double cip = cc[IDX(wp(i, n), j, k, n)], cim = cc[IDX(wm(i, n), j, k, n)];
-    double fp = (cip + ck) / 2.0 * flx0;
-    double fm = (ck + cim) / 2.0 * flxm;
-    r = r + fp - fm;
-  }
-  {
-    double uy[5], wy[5];
-#pragma unroll
-    for (int q = 0; q < 5; ++q) {
-      int jq = ((j + q - 2) % n + n) % n;
-      i64 cq = IDX(i, jq, k, n);
-      uy[q] = u[cq];
-      wy[q] = vy[cq] / cc[cq];
-    }
-    double fly0 = wphalf(uy[1], wy[1], uy[2], wy[2], uy[3], wy[3], uy[4], wy[4]);
-    double flym = wphalf(uy[0], wy[0], uy[1], wy[1], uy[2], wy[2], uy[3], wy[3]);
-    double cjp = cc[IDX(i, wp(j, n), k, n)], cjm = cc[IDX(i, wm(j, n), k, n)];
-    r = r + (cjp + ck) / 2.0 * fly0 - (ck + cjm) / 2.0 * flym;
-  }
+  double r = g[2 * n3 + t] - g[2 * n3 + IDX(i, j, wm(k, n), n)];
+  r = r + g[t] - g[IDX(wm(i, n), j, k, n)];
+  r = r + g[n3 + t] - g[n3 + IDX(i, wm(j, n), k, n)];
   out[t] = ubase[t] - r * dt;
 }
 
-void launch_relax_dpv(const double* u, const double* vt, const double* cc, int n, const double* ubase, double dt,
-                      double* out, cudaStream_t s) {
+void launch_relax_dpv(const double* sd, const double* cc, int n, const double* ubase, double dt, double* out,
+                      double* gface, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
-  k_relax_dpv<<<grid_of(n3, kBlock), kBlock, 0, s>>>(u, vt, cc, n, ubase, dt, out);
+  k_relax_faces<<<grid_of(n3, kBlock), kBlock, 0, s>>>(sd, cc, n, gface);
+  count_launch();
+  k_relax_div<<<grid_of(n3, kBlock), kBlock, 0, s>>>(gface, n, ubase, dt, out);
   count_launch();
 }
 

@@ -31,7 +31,7 @@ void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nswe
   T dx2 = dx * dx;
   if (n >= 64) {
     constexpr int TX = GsTile<T>::TX, TY = GsTile<T>::TY;
-    const size_t smem = sizeof(T) * 16 * (TX + 8) * (TY + 8);
+    const size_t smem = sizeof(T) * GsGeom<T, TX, TY>::WORDS;
     static bool attr = false;
     if (!attr) {
       cudaFuncSetAttribute(k_gs_plane<T, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -53,6 +53,15 @@ void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nswe
       b = t;
     }
     if (a != phi) cudaMemcpyAsync(phi, a, sizeof(T) * (size_t)n * n * n, cudaMemcpyDeviceToDevice, s);
+    return;
+  }
+  if (n <= 8) {
+    if (nsweeps > 0) {
+      prof_begin(kk<T>(KK_GS), s, h3 * 8 * nsweeps, n);
+      k_gs_small_sm<T><<<1, 512, sizeof(T) * 8 * n * n * n, s>>>(phi, rhs, coef, n, dx2, nsweeps);
+      prof_end(kk<T>(KK_GS), s, n);
+      count_launch();
+    }
     return;
   }
   if (n <= 16) {
@@ -160,12 +169,12 @@ void launch_fill(T* a, i64 count, T v, cudaStream_t s) {
 
 template <class T>
 __global__ void k_absmax(const T* __restrict__ a, i64 count, unsigned long long* maxbits) {
-  double m = 0.0;
+  decltype(abs_bits(T(0))) m = 0;
   for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (i64)gridDim.x * blockDim.x) {
-    double v = fabs((double)a[t]);
-    m = (v > m || v != v) ? v : m;
+    auto v = abs_bits(a[t]);
+    m = v > m ? v : m;
   }
-  block_max_commit(m, maxbits);
+  block_max_commit(from_bits(m), maxbits);
 }
 
 template <class T>

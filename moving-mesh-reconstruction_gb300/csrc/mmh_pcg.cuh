@@ -16,7 +16,7 @@ __global__ void k_apply(const T* __restrict__ p, const T* __restrict__ coef, int
                         unsigned long long* qbits) {
   i64 n3 = (i64)n * n * n;
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  double m = 0.0;
+  T m = T(0);
   if (t < n3) {
     int i, j, k;
     cell_of(t, n, i, j, k);
@@ -24,10 +24,29 @@ __global__ void k_apply(const T* __restrict__ p, const T* __restrict__ coef, int
     op_terms(p, coef, n, n3, i, j, k, tdiag, t1, t2);
     T v = (t1 + t2 + tdiag * p[t]) * di2;
     q[t] = v;
-    m = fabs((double)v);
+    m = fabs(v);
   }
   block_max_commit(m, qbits);
 }
+
+// trunc(a*b * 2^sh) for FP32 a, b from their bits: the product of the 24-bit
+// significands is exact in 64 bits, so this equals fx_bits of the (exact)
+// FP64 product without any FP64 operation.
+__device__ __forceinline__ __int128 fx_prod(float a, float b, int sh) {
+  unsigned ua = __float_as_uint(a), ub = __float_as_uint(b);
+  int ea = (int)((ua >> 23) & 0xFF), eb = (int)((ub >> 23) & 0xFF);
+  unsigned ma = ua & 0x7FFFFFu, mb = ub & 0x7FFFFFu;
+  if (ea) ma |= 0x800000u; else ea = 1;
+  if (eb) mb |= 0x800000u; else eb = 1;
+  unsigned long long m = (unsigned long long)ma * mb;
+  int s = ea + eb - 300 + sh;
+  unsigned __int128 v;
+  if (s >= 0) v = (unsigned __int128)m << s;
+  else if (s > -64) v = (unsigned __int128)(m >> (-s));
+  else v = 0;
+  return ((ua ^ ub) >> 31) ? -(__int128)v : (__int128)v;
+}
+__device__ __forceinline__ __int128 fx_prod(double a, double b, int sh) { return fx_bits(a * b, sh); }
 
 template <class T>
 __global__ void k_dot(const T* __restrict__ a, const T* __restrict__ b, i64 count, const unsigned long long* abits,
@@ -37,7 +56,7 @@ __global__ void k_dot(const T* __restrict__ a, const T* __restrict__ b, i64 coun
   if (ma > 0.0 && mb > 0.0) {
     int E = ilogb(ma) + ilogb(mb) + 2;
     for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (i64)gridDim.x * blockDim.x)
-      s += fx_bits((double)a[t] * (double)b[t], 96 - E);
+      s += fx_prod(a[t], b[t], 96 - E);
   }
   fx_block_commit(s, acc);
 }
@@ -48,12 +67,12 @@ __global__ void k_pcg_update(T* __restrict__ x, T* __restrict__ r, const T* __re
                              i64 count, const double* __restrict__ alpha, unsigned long long* rbits) {
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   T a = (T)*alpha;
-  double m = 0.0;
+  T m = T(0);
   if (t < count) {
     x[t] = x[t] + a * p[t];
     T v = r[t] - a * q[t];
     r[t] = v;
-    m = fabs((double)v);
+    m = fabs(v);
   }
   block_max_commit(m, rbits);
 }
@@ -64,11 +83,11 @@ __global__ void k_pcg_pupdate(T* __restrict__ p, const T* __restrict__ z, i64 co
                               unsigned long long* pbits) {
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   T b = (T)*beta;
-  double m = 0.0;
+  T m = T(0);
   if (t < count) {
     T v = z[t] + b * p[t];
     p[t] = v;
-    m = fabs((double)v);
+    m = fabs(v);
   }
   block_max_commit(m, pbits);
 }

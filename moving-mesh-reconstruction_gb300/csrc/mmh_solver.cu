@@ -105,9 +105,10 @@ struct mmh_ctx {
   double *px = nullptr, *pb = nullptr, *pp = nullptr, *pq = nullptr;
   float *pe32 = nullptr, *pb32 = nullptr, *pp32 = nullptr, *pq32 = nullptr;
   // relaxing
-  double *baj = nullptr, *cc = nullptr, *vt = nullptr, *u1 = nullptr;
+  double *baj = nullptr, *cc = nullptr, *vt = nullptr, *u1 = nullptr, *gface = nullptr;
   // spectral
   void *Xc = nullptr, *Z = nullptr;
+  double* spectab = nullptr;  // twiddle and cosine tables of the spectral kernels
   cufftHandle pd2z = 0, pz2z = 0;
   bool plans = false;
   Scal* sc = nullptr;   // device
@@ -173,13 +174,14 @@ template <>
 Hier<float>& hier<float>(mmh_ctx* c) { return c->h32; }
 
 // relax(): nrelax 8-colour sweeps, then residual (mode 3: full weighting into
-// rhs[l+1] and max norm; mode 2: max norm only) into *maxslot.
+// rhs[l+1] and max norm; mode 2: max norm only; mode 0: none) into *maxslot.
 template <class T>
 int relax_level(mmh_ctx* c, int l, int nrelax, int mode, unsigned long long* maxslot) {
   Hier<T>& H = hier<T>(c);
   int n = c->nl[l];
   T dx = T(double(1 << l));
   launch_gs_sweeps<T>(H.u[l], H.rhs[l], H.coef[l], n, dx, nrelax, H.r[l], c->s);
+  if (mode == 0) return MMH_OK;
   CK(cudaMemsetAsync(maxslot, 0, 8, c->s));
   launch_residual<T>(H.u[l], H.rhs[l], H.coef[l], n, dx, mode == 3 ? H.r[l] : (T*)nullptr, nullptr, maxslot, c->s);
   if (mode == 3) launch_restrict_resid<T>(H.r[l], n, special_plane(nrelax, n), H.rhs[l + 1], c->s);
@@ -212,6 +214,10 @@ int vcycle(mmh_ctx* c, int l) {
   bool ref = c->cfg.schedule == MMH_SCHED_REF;
   bool at_ng = (n == c->n);
   bool guard = !at_ng && (c->cfg.schedule != MMH_SCHED_TOL || c->cfg.precond_guards);
+  // the post-relaxation residual norms feed the guards and the reference's
+  // diagnostics only; the preconditioner of the tolerance schedule without
+  // guards skips them
+  const int post = (guard || c->cfg.schedule != MMH_SCHED_TOL) ? 2 : 0;
   if (n == 4) {
     if constexpr (std::is_same<T, float>::value) {
       // coarsest grid solved in FP64
@@ -223,8 +229,8 @@ int vcycle(mmh_ctx* c, int l) {
       launch_d2f(c->h64.u[l], F.u[l], n3, c->s);
       return MMH_OK;
     }
-    RET(relax_level<T>(c, l, 32, 2, &c->sc->r1bits[l]));
-    RET(relax_level<T>(c, l, 32, 2, &c->sc->errbits[l]));
+    RET(relax_level<T>(c, l, 32, post, &c->sc->r1bits[l]));
+    RET(relax_level<T>(c, l, 32, post, &c->sc->errbits[l]));
     return guard_or_zerosum<T>(c, l, 1.001, 1.e-5, guard);
   }
   int nrelax = ref ? 4 * c->n / n : c->cfg.nu1;
@@ -234,7 +240,7 @@ int vcycle(mmh_ctx* c, int l) {
   launch_fill<T>(H.u[l + 1], (i64)nh * nh * nh, T(0), c->s);
   RET(vcycle<T>(c, l + 1));
   launch_prolong_add<T>(H.u[l], H.u[l + 1], n, c->s);
-  RET(relax_level<T>(c, l, nrelax2, 2, &c->sc->errbits[l]));
+  RET(relax_level<T>(c, l, nrelax2, post, &c->sc->errbits[l]));
   return guard_or_zerosum<T>(c, l, 1.0, -HUGE_VAL, guard);
 }
 
@@ -340,11 +346,15 @@ int pcg_core(mmh_ctx* c, int l0, double dx, T* x, const T* b, T* p, T* q, double
 }
 
 // FP64 true residual of x against b at level l0: max|b - L x| (also copied
-// to FP32 in r32 when given).
+// to FP32 in r32 when given).  The mixed form evaluates it with fused
+// multiply-adds; the FP64 form keeps the reference's separate roundings.
 int true_residual(mmh_ctx* c, int l0, double dx, const double* x, const double* b, float* r32, double* rmax) {
   int n = c->nl[l0];
   CK(cudaMemsetAsync(&c->sc->resbits, 0, 8, c->s));
-  launch_residual<double>(x, b, c->h64.coef[l0], n, dx, nullptr, r32, &c->sc->resbits, c->s);
+  if (c->cfg.precision == MMH_MIXED)
+    launch_residual_fma(x, b, c->h64.coef[l0], n, dx, r32, &c->sc->resbits, c->s);
+  else
+    launch_residual<double>(x, b, c->h64.coef[l0], n, dx, nullptr, r32, &c->sc->resbits, c->s);
   RET(pull_scal(c));
   *rmax = bits_to_double(c->hsc->resbits);
   return MMH_OK;
@@ -470,8 +480,7 @@ int multigrid_level(mmh_ctx* c, int l0, double dx, mmh_diag* d) {
     if (rn > 0) {
       for (cycles = 0;; ) {
         CK(cudaMemsetAsync(&c->sc->resbits, 0, 8, c->s));
-        launch_residual<double>(c->h64.u[l0], c->h64.rhs[l0], c->h64.coef[l0], n, dx, nullptr, F.rhs[l0],
-                                &c->sc->resbits, c->s);
+        launch_residual_fma(c->h64.u[l0], c->h64.rhs[l0], c->h64.coef[l0], n, dx, F.rhs[l0], &c->sc->resbits, c->s);
         RET(pull_scal(c));
         rel = bits_to_double(c->hsc->resbits) / rn;
         if (!(rel == rel) || rel <= c->cfg.tol) break;
@@ -535,6 +544,8 @@ int make_plans(mmh_ctx* c) {
   CKF(cufftPlan3d(&c->pz2z, n, n, n / 2, CUFFT_Z2Z));
   CKF(cufftSetStream(c->pd2z, c->s));
   CKF(cufftSetStream(c->pz2z, c->s));
+  RET(c->alloc(&c->spectab, 2 * (i64)n));
+  launch_spec_tables(c->spectab, n, c->s);
   c->plans = true;
   return MMH_OK;
 }
@@ -544,7 +555,7 @@ int make_plans(mmh_ctx* c) {
 int limiter_poisson(mmh_ctx* c, double* defp, const double* defplim) {
   RET(make_plans(c));
   CKF(cufftExecD2Z(c->pd2z, (cufftDoubleReal*)defplim, (cufftDoubleComplex*)c->Xc));
-  launch_spec_pack(c->Xc, c->n, 4, c->Z, &c->sc->lim, c->s);
+  launch_spec_pack(c->Xc, c->n, 4, c->Z, &c->sc->lim, c->spectab, c->s);
   CKF(cufftExecZ2Z(c->pz2z, (cufftDoubleComplex*)c->Z, (cufftDoubleComplex*)c->Z, CUFFT_FORWARD));
   launch_spec_unpack(c->Z, c->n, defp, 1, 1, &c->sc->lim, c->s);
   return MMH_OK;
@@ -580,9 +591,9 @@ int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t
 int relaxing_dev(mmh_ctx* c, double dt) {
   int n = c->n;
   launch_relax_stage1(c->rho, c->def, c->defp(), n, c->baj, c->cc, c->vt, c->s);
-  launch_relax_dpv(c->rho, c->vt, c->cc, n, c->rho, dt / 2.0, c->u1, c->s);
-  launch_relax_flux(c->u1, c->defp(), c->baj, n, c->vt, c->s);
-  launch_relax_dpv(c->u1, c->vt, c->cc, n, c->rho, dt, c->rho, c->s);
+  launch_relax_dpv(c->vt, c->cc, n, c->rho, dt / 2.0, c->u1, c->gface, c->s);
+  launch_relax_flux(c->u1, c->defp(), c->baj, c->cc, n, c->vt, c->s);
+  launch_relax_dpv(c->vt, c->cc, n, c->rho, dt, c->rho, c->gface, c->s);
   return MMH_OK;
 }
 
@@ -591,12 +602,12 @@ int spectral_outputs(mmh_ctx* c, const double* src, double* d_grad, double* d_de
   RET(make_plans(c));
   CKF(cufftExecD2Z(c->pd2z, (cufftDoubleReal*)src, (cufftDoubleComplex*)c->Xc));
   for (int ax = 0; ax < 3 && d_grad; ++ax) {
-    launch_spec_pack(c->Xc, c->n, ax, c->Z, &c->sc->lim, c->s);
+    launch_spec_pack(c->Xc, c->n, ax, c->Z, &c->sc->lim, c->spectab, c->s);
     CKF(cufftExecZ2Z(c->pz2z, (cufftDoubleComplex*)c->Z, (cufftDoubleComplex*)c->Z, CUFFT_FORWARD));
     launch_spec_unpack(c->Z, c->n, d_grad + ax * c->n3, 1, 0, &c->sc->lim, c->s);
   }
   if (d_delta) {
-    launch_spec_pack(c->Xc, c->n, 3, c->Z, &c->sc->lim, c->s);
+    launch_spec_pack(c->Xc, c->n, 3, c->Z, &c->sc->lim, c->spectab, c->s);
     CKF(cufftExecZ2Z(c->pz2z, (cufftDoubleComplex*)c->Z, (cufftDoubleComplex*)c->Z, CUFFT_FORWARD));
     launch_spec_unpack(c->Z, c->n, d_delta, 1, 0, &c->sc->lim, c->s);
   }
@@ -881,7 +892,8 @@ int mmh_create(mmh_ctx** out, const mmh_config* cfg) {
   }
   A(&c->baj, 7 * n3);
   A(&c->cc, n3);
-  A(&c->vt, 3 * n3);
+  A(&c->vt, 6 * n3);  // half sums and differences of the relaxing fluxes
+  A(&c->gface, 3 * n3);
   A(&c->u1, n3);
   A((double**)&c->Xc, 2 * (i64)(n / 2 + 1) * n * n);
   A((double**)&c->Z, 2 * (i64)(n / 2) * n * n);
