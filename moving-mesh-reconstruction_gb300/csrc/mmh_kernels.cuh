@@ -373,113 +373,72 @@ __global__ void __launch_bounds__(512) k_gs_small_sm(T* __restrict__ phi, const 
 // read updated cells of the earlier ones within one cell in x and within
 // 3-q rows in y, so this region covers everything they read and the interior
 // ends exactly as after the four global colour phases; the extra cells a
-// colour computes beyond that are never read.
+// colour computes beyond that are never read.  Row 0 of the tile is never
+// read and is not loaded.
 //
-// Shared memory.  Fields read at neighbours (stencil fields) are stored with
-// the even rows first and the odd rows OFFB words after them, a pitch of Q
-// words between two rows of one parity, and every row split into its even-x
-// and its odd-x half (H2 words each).  Cell m of row t of a colour then sits
-// at word const + Q*t + m, and Q = NXC (mod 32) puts the words of any 32
-// consecutive cells of a colour in 32 different banks (16 different bank
-// pairs for 8-byte words): a colour phase reads shared memory without bank
-// conflicts.  Fields read only at the cell itself (centre fields) are stored
-// compacted per colour, cell e of colour q at cbase(q) + e.  Q, OFFB, H2 and
-// NXC are even, so two cells x0 and x0+2 of a 16-byte group are adjacent
-// 8-byte-aligned words in either layout and are stored as one pair.
+// Shared memory holds the fields read at neighbours (phi of planes P-1, P,
+// P+1 and coefficients 1-5 of P) with the even rows first and the odd rows
+// OFFB words after them, a pitch of Q words between two rows of one parity,
+// and every row split into its even-x and its odd-x half (H2 words each).
+// Cell m of row t of a colour then sits at word const + Q*t + m, and
+// Q = NXC (mod 32) puts the words of any 32 consecutive cells of a colour in
+// 32 different banks (16 different bank pairs for 8-byte words): a colour
+// phase reads shared memory without bank conflicts.  Q, OFFB and H2 are
+// even, so the cells x0, x0+2 of a 16-byte group are one aligned pair.  The
+// fields read only at the cell itself (rhs, coefficient 6 of P, coefficients
+// 3, 5, 6 of P-1 and P+1) are read from global memory by the thread that
+// updates the cell.
 template <class T, int TX, int TY>
 struct GsGeom {
   static constexpr int HB = 4, W = TX + 2 * HB, HT = TY + 2 * HB, H2 = W / 2, NXC = H2 - 2;
   static constexpr int Q = NXC + 32 * ((W - NXC + 31) / 32);
   static constexpr int OFFB0 = (HT / 2) * Q;
   static constexpr int OFFB = OFFB0 + ((20 - OFFB0 % 32) + 32) % 32;  // first odd row (fewer store conflicts)
-  static constexpr int SF = OFFB + (HT / 2) * Q;  // words of one stencil field
-  static constexpr int NC = NXC * (2 * TY + 6);   // words of one centre field (four colours)
-  static constexpr int NSF = 8, NCF = 8;
-  static constexpr int WORDS = NSF * SF + NCF * NC;
+  static constexpr int SF = OFFB + (HT / 2) * Q;                       // words of one field
+  static constexpr int NSF = 8;
+  static constexpr int WORDS = NSF * SF;
   static __device__ __forceinline__ constexpr int XS(int io) { return io ? 1 : HB; }
   static __device__ __forceinline__ constexpr int ys(int q) { return HB - 2 + q; }
   static __device__ __forceinline__ constexpr int ny(int q) { return TY / 2 + 3 - q; }
-  static __device__ __forceinline__ constexpr int cbase(int q) { return NXC * (q * (TY / 2 + 3) - q * (q - 1) / 2); }
   static __device__ __forceinline__ int word(int x, int y) {
     return (y & 1) * OFFB + (y >> 1) * Q + (x & 1) * H2 + (x >> 1);
   }
-  static_assert(Q >= W && (Q - NXC) % 32 == 0 && Q % 2 == 0 && OFFB % 2 == 0 && NXC % 2 == 0, "row pitch");
-  static_assert(HT % 2 == 0 && TX % 4 == 0, "tile shape");
-  // the computed x ranges, [4, W-2] even and [1, W-5] odd, start and end on
-  // whole pairs (x0, x0+2) of the 16-byte groups
-  static_assert(HB % 4 == 0 && (HB + 2 * (NXC - 1)) % 4 == 2 && (1 + 2 * (NXC - 1)) % 4 == 3, "pairs");
+  static_assert(Q >= W && (Q - NXC) % 32 == 0 && Q % 2 == 0 && OFFB % 2 == 0, "row pitch");
+  static_assert(HT % 2 == 0 && TX % 4 == 0 && HB == 4, "tile shape");
 };
 
-// Per 16-byte group (cells x0..x0+VW-1 of tile row y, x0 a multiple of VW, so
-// cell x0+j has the x parity of j): its stencil word sw (cell x0+j at
-// sw + (j&1)*H2 + (j>>1)) and, per x parity io, its centre word cw[io] (cell
-// x0+io+2h at cw[io] + h) and whether those cells are computed (cv[io]).
-template <class G, int VW>
-struct GsSlot {
-  int sw, cw[2];
-  bool cv[2];
-  __device__ __forceinline__ GsSlot(int x0, int y) {
-    sw = (y & 1) * G::OFFB + (y >> 1) * G::Q + (x0 >> 1);
-    const int jo = y & 1;
-#pragma unroll
-    for (int io = 0; io < 2; ++io) {
-      const int q = 2 * io + jo, t2 = y - G::ys(q);
-      const int xa = x0 + io, xb = x0 + io + 2 * (VW / 2 - 1);  // first and last cell of parity io
-      cw[io] = G::cbase(q) + (t2 >> 1) * G::NXC + ((xa - G::XS(io)) >> 1);
-      cv[io] = t2 >= 0 && t2 < 2 * G::ny(q) && xa >= G::XS(io) && xb <= G::XS(io) + 2 * (G::NXC - 1);
-    }
-  }
-};
-
-// Store one 16-byte group into a stencil field / a centre field.
-template <class G>
-__device__ __forceinline__ void gs_put_stencil(float* f, const GsSlot<G, 4>& sl, const float4& v) {
-  *reinterpret_cast<float2*>(f + sl.sw) = make_float2(v.x, v.z);
-  *reinterpret_cast<float2*>(f + sl.sw + G::H2) = make_float2(v.y, v.w);
+// Store one 16-byte group (cells x0..x0+VW-1 of tile row y) into a field at
+// its word sw = word(x0, y); read one back.
+__device__ __forceinline__ void gs_put(float* f, int sw, int h2, const float4& v) {
+  *reinterpret_cast<float2*>(f + sw) = make_float2(v.x, v.z);
+  *reinterpret_cast<float2*>(f + sw + h2) = make_float2(v.y, v.w);
 }
-template <class G>
-__device__ __forceinline__ void gs_put_stencil(double* f, const GsSlot<G, 2>& sl, const double2& v) {
-  f[sl.sw] = v.x;
-  f[sl.sw + G::H2] = v.y;
+__device__ __forceinline__ void gs_put(double* f, int sw, int h2, const double2& v) {
+  f[sw] = v.x;
+  f[sw + h2] = v.y;
 }
-template <class G>
-__device__ __forceinline__ void gs_put_centre(float* f, const GsSlot<G, 4>& sl, const float4& v) {
-  if (sl.cv[0]) *reinterpret_cast<float2*>(f + sl.cw[0]) = make_float2(v.x, v.z);
-  if (sl.cv[1]) *reinterpret_cast<float2*>(f + sl.cw[1]) = make_float2(v.y, v.w);
-}
-template <class G>
-__device__ __forceinline__ void gs_put_centre(double* f, const GsSlot<G, 2>& sl, const double2& v) {
-  if (sl.cv[0]) f[sl.cw[0]] = v.x;
-  if (sl.cv[1]) f[sl.cw[1]] = v.y;
-}
-template <class G>
-__device__ __forceinline__ float4 gs_get_stencil(const float* f, int sw) {
+__device__ __forceinline__ float4 gs_get(const float* f, int sw, int h2) {
   float2 e = *reinterpret_cast<const float2*>(f + sw);
-  float2 o = *reinterpret_cast<const float2*>(f + sw + G::H2);
+  float2 o = *reinterpret_cast<const float2*>(f + sw + h2);
   return make_float4(e.x, o.x, e.y, o.y);
 }
-template <class G>
-__device__ __forceinline__ double2 gs_get_stencil(const double* f, int sw) {
-  return make_double2(f[sw], f[sw + G::H2]);
-}
+__device__ __forceinline__ double2 gs_get(const double* f, int sw, int h2) { return make_double2(f[sw], f[sw + h2]); }
 
 // All four in-plane colours of one plane P (k%2 == kpar) for one tile (see
 // GsGeom).  The half sweep reads its own planes from src, the neighbour planes
 // P+-1 (not written during the half sweep) from nbr, and writes dst != src,
 // so no tile can read a halo that another tile has already updated.  Needs
-// n >= TX+8 and n >= TY+8.  Stencil fields: 0 phi(P), 1 phi(P-1), 2 phi(P+1),
-// 3-7 f1..f5(P).  Centre fields: 0 rhs(P), 1 f6(P), 2-4 f3,f5,f6(P-1),
-// 5-7 f3,f5,f6(P+1).
+// n >= TX+8 and n >= TY+8.  The register budget of 4 CTAs per SM lets the
+// compiler keep the tile's global loads in flight together.
 template <class T, int TX, int TY>
-__global__ void __launch_bounds__(256) k_gs_plane(const T* __restrict__ src, const T* __restrict__ nbr,
-                                                  T* __restrict__ dst, const T* __restrict__ rhs,
-                                                  const T* __restrict__ coef, int n, T dx2, int kpar) {
+__global__ void __launch_bounds__(256, 4) k_gs_plane(const T* __restrict__ src, const T* __restrict__ nbr,
+                                                     T* __restrict__ dst, const T* __restrict__ rhs,
+                                                     const T* __restrict__ coef, int n, T dx2, int kpar) {
   typedef GsGeom<T, TX, TY> G;
   constexpr int HB = G::HB, W = G::W, HT = G::HT, H2 = G::H2, NXC = G::NXC, Q = G::Q, OFFB = G::OFFB;
-  constexpr int SF = G::SF, NC = G::NC;
+  constexpr int SF = G::SF;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
-  T* sc = sm + G::NSF * SF;
   const i64 n2 = (i64)n * n, n3 = n2 * n;
   const int i0 = blockIdx.x * TX - HB, j0 = blockIdx.y * TY - HB, k = 2 * blockIdx.z + kpar;
   const int kmn = wm(k, n), kpn = wp(k, n);
@@ -487,38 +446,27 @@ __global__ void __launch_bounds__(256) k_gs_plane(const T* __restrict__ src, con
   // multiple of 4 elements) and a 16-byte group never straddles the periodic
   // wrap (n is a multiple of the group), so each group is one aligned load.
   typedef typename Vec16<T>::type V;
-  constexpr int VW = 16 / (int)sizeof(T), NV = W / VW, NVT = NV * HT;
+  constexpr int VW = 16 / (int)sizeof(T), NV = W / VW, NVT = NV * (HT - 1);
   const V* vsrc = reinterpret_cast<const V*>(src);
   const V* vnbr = reinterpret_cast<const V*>(nbr);
-  const V* vrhs = reinterpret_cast<const V*>(rhs);
   const V* vcoef = reinterpret_cast<const V*>(coef);
   const i64 nv3 = n3 / VW;
   for (int e = threadIdx.x; e < NVT; e += blockDim.x) {
-    const int xv = e % NV, y = e / NV, x0 = xv * VW;
+    const int xv = e % NV, y = 1 + e / NV, x0 = xv * VW;
     int gi = i0 + x0, gj = j0 + y;
     gi += (gi < 0) ? n : ((gi >= n) ? -n : 0);
     gj += (gj < 0) ? n : ((gj >= n) ? -n : 0);
     const i64 b = (i64)gi + (i64)n * gj;
     const i64 cP = (b + n2 * k) / VW, cm = (b + n2 * kmn) / VW, cp = (b + n2 * kpn) / VW;
-    V v[16];
+    V v[8];
     v[0] = vsrc[cP];
     v[1] = vnbr[cm];
     v[2] = vnbr[cp];
 #pragma unroll
     for (int f = 0; f < 5; ++f) v[3 + f] = vcoef[f * nv3 + cP];
-    v[8] = vrhs[cP];
-    v[9] = vcoef[5 * nv3 + cP];
-    v[10] = vcoef[2 * nv3 + cm];
-    v[11] = vcoef[4 * nv3 + cm];
-    v[12] = vcoef[5 * nv3 + cm];
-    v[13] = vcoef[2 * nv3 + cp];
-    v[14] = vcoef[4 * nv3 + cp];
-    v[15] = vcoef[5 * nv3 + cp];
-    const GsSlot<G, VW> sl(x0, y);
+    const int sw = G::word(x0, y);
 #pragma unroll
-    for (int f = 0; f < 8; ++f) gs_put_stencil<G>(sm + f * SF, sl, v[f]);
-#pragma unroll
-    for (int f = 0; f < 8; ++f) gs_put_centre<G>(sc + f * NC, sl, v[8 + f]);
+    for (int f = 0; f < 8; ++f) gs_put(sm + f * SF, sw, H2, v[f]);
   }
   __syncthreads();
   T* sP = sm;
@@ -529,19 +477,30 @@ __global__ void __launch_bounds__(256) k_gs_plane(const T* __restrict__ src, con
   const T* F3 = sm + 5 * SF;
   const T* F4 = sm + 6 * SF;
   const T* F5 = sm + 7 * SF;
-#pragma unroll 1
+  const T* f3 = coef + 2 * n3;
+  const T* f5 = coef + 4 * n3;
+  const T* f6 = coef + 5 * n3;
+#pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int io = q >> 1, jo = q & 1;
     const int cnt = NXC * G::ny(q);
     // word offsets of the x+-1 and y+-1 neighbours (constant within a colour)
     const int oxp = io ? 1 - H2 : H2, oxm = io ? -H2 : H2 - 1;
     const int oyp = jo ? Q - OFFB : OFFB, oym = jo ? -OFFB : OFFB - Q;
-    const T* cen = sc + G::cbase(q);
     for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
       const int m = e % NXC, t = e / NXC;
-      const int c = G::word(G::XS(io) + 2 * m, G::ys(q) + 2 * t);
+      const int x = G::XS(io) + 2 * m, y = G::ys(q) + 2 * t;
+      const int c = G::word(x, y);
+      int gi = i0 + x, gj = j0 + y;
+      gi += (gi < 0) ? n : ((gi >= n) ? -n : 0);
+      gj += (gj < 0) ? n : ((gj >= n) ? -n : 0);
+      const i64 g = (i64)gi + (i64)n * gj;
+      const i64 gt = g + n2 * k, gm = g + n2 * kmn, gp = g + n2 * kpn;
       const int cxp = c + oxp, cxm = c + oxm, cyp = c + oyp, cym = c + oym;
       Stencil<T> st;
+      st.f6c = f6[gt]; st.f6km = f6[gm]; st.f6kp = f6[gp];
+      st.f3km = f3[gm]; st.f5km = f5[gm]; st.f3kp = f3[gp]; st.f5kp = f5[gp];
+      const T r = rhs[gt];
       st.c = sP[c]; st.ip = sP[cxp]; st.im = sP[cxm]; st.jp = sP[cyp]; st.jm = sP[cym];
       st.kp = sKp[c]; st.km = sKm[c];
       st.ppk = sP[cxp + oyp]; st.mpk = sP[cxm + oyp]; st.pmk = sP[cxp + oym]; st.mmk = sP[cxm + oym];
@@ -552,12 +511,9 @@ __global__ void __launch_bounds__(256) k_gs_plane(const T* __restrict__ src, con
       st.f2jp = F2[cyp]; st.f2jm = F2[cym]; st.f2ip = F2[cxp]; st.f2im = F2[cxm];
       st.f5jp = F5[cyp]; st.f5jm = F5[cym];
       st.f3ip = F3[cxp]; st.f3im = F3[cxm];
-      st.f6c = cen[1 * NC + e];
-      st.f3km = cen[2 * NC + e]; st.f5km = cen[3 * NC + e]; st.f6km = cen[4 * NC + e];
-      st.f3kp = cen[5 * NC + e]; st.f5kp = cen[6 * NC + e]; st.f6kp = cen[7 * NC + e];
       T tdiag, t1, t2;
       op_eval(st, tdiag, t1, t2);
-      sP[c] = (cen[e] * dx2 - t1 - t2) / tdiag;
+      sP[c] = (r * dx2 - t1 - t2) / tdiag;
     }
     __syncthreads();
   }
@@ -565,7 +521,7 @@ __global__ void __launch_bounds__(256) k_gs_plane(const T* __restrict__ src, con
   V* vdst = reinterpret_cast<V*>(dst);
   for (int e = threadIdx.x; e < NVI * TY; e += blockDim.x) {
     const int x0 = HB + (e % NVI) * VW, y = HB + e / NVI;
-    vdst[((i64)(i0 + x0) + (i64)n * (j0 + y) + n2 * k) / VW] = gs_get_stencil<G>(sP, G::word(x0, y));
+    vdst[((i64)(i0 + x0) + (i64)n * (j0 + y) + n2 * k) / VW] = gs_get(sP, G::word(x0, y), H2);
   }
 }
 
@@ -590,6 +546,93 @@ __global__ void k_residual(const T* __restrict__ phi, const T* __restrict__ rhs,
     m = fabs(tr);
   }
   if (maxbits) block_max_commit(m, maxbits);
+}
+
+// The residual (MODE 0: r = rhs - L[phi], calcresid) or the operator (MODE 1:
+// q = L[p]) of every cell of one TX x TY tile of one plane.  The fields the
+// 19-point stencil reads at neighbours (phi of planes P-1, P, P+1 and
+// coefficients 1-5 of P) are staged in shared memory, row-major with an x halo
+// of 4 (aligned 16-byte loads) and a y halo of 1; the fields read only at the
+// cell itself come straight from global memory.  A warp covers 32 consecutive
+// cells of a row, so the shared reads are conflict-free and the global
+// accesses coalesced.  Same arithmetic as k_residual / k_apply.  Needs
+// n >= TX and n a multiple of TY.
+template <class T, int MODE, bool Contract = false>
+__global__ void __launch_bounds__(256) k_stencil_plane(const T* __restrict__ phi, const T* __restrict__ rhs,
+                                                       const T* __restrict__ coef, int n, T di2, T* __restrict__ out,
+                                                       float* __restrict__ out32, unsigned long long* maxbits) {
+  constexpr int TX = 32, TY = 16, HX = 4, W = TX + 2 * HX, HT = TY + 2, S = W * HT;
+  __shared__ __align__(16) T sm[8 * S];  // 0 phi(P), 1 phi(P-1), 2 phi(P+1), 3-7 f1..f5(P)
+  const i64 n2 = (i64)n * n, n3 = n2 * n;
+  const int i0 = blockIdx.x * TX - HX, j0 = blockIdx.y * TY - 1, k = blockIdx.z;
+  const int kmn = wm(k, n), kpn = wp(k, n);
+  typedef typename Vec16<T>::type V;
+  constexpr int VW = 16 / (int)sizeof(T), NV = W / VW, NVT = NV * HT;
+  const V* vphi = reinterpret_cast<const V*>(phi);
+  const V* vcoef = reinterpret_cast<const V*>(coef);
+  const i64 nv3 = n3 / VW;
+  for (int e = threadIdx.x; e < NVT; e += blockDim.x) {
+    const int xv = e % NV, y = e / NV, x0 = xv * VW;
+    int gi = i0 + x0, gj = j0 + y;
+    gi += (gi < 0) ? n : ((gi >= n) ? -n : 0);
+    gj += (gj < 0) ? n : ((gj >= n) ? -n : 0);
+    const i64 b = (i64)gi + (i64)n * gj;
+    const i64 cP = (b + n2 * k) / VW, cm = (b + n2 * kmn) / VW, cp = (b + n2 * kpn) / VW;
+    V v[8];
+    v[0] = vphi[cP];
+    v[1] = vphi[cm];
+    v[2] = vphi[cp];
+#pragma unroll
+    for (int f = 0; f < 5; ++f) v[3 + f] = vcoef[f * nv3 + cP];
+#pragma unroll
+    for (int f = 0; f < 8; ++f) *reinterpret_cast<V*>(sm + f * S + y * W + x0) = v[f];
+  }
+  __syncthreads();
+  const T* P = sm;
+  const T* Km = sm + S;
+  const T* Kp = sm + 2 * S;
+  const T* F1 = sm + 3 * S;
+  const T* F2 = sm + 4 * S;
+  const T* F3 = sm + 5 * S;
+  const T* F4 = sm + 6 * S;
+  const T* F5 = sm + 7 * S;
+  const T* f3 = coef + 2 * n3;
+  const T* f5 = coef + 4 * n3;
+  const T* f6 = coef + 5 * n3;
+  decltype(abs_bits(T(0))) mb = 0;
+  const int tx = threadIdx.x % TX;
+  for (int ty = threadIdx.x / TX; ty < TY; ty += blockDim.x / TX) {
+    const int c = (1 + ty) * W + HX + tx;
+    const i64 g = (i64)(blockIdx.x * TX + tx) + (i64)n * (blockIdx.y * TY + ty);
+    const i64 gt = g + n2 * k, gm = g + n2 * kmn, gp = g + n2 * kpn;
+    Stencil<T> st;
+    st.c = P[c]; st.ip = P[c + 1]; st.im = P[c - 1]; st.jp = P[c + W]; st.jm = P[c - W];
+    st.kp = Kp[c]; st.km = Km[c];
+    st.ppk = P[c + 1 + W]; st.mpk = P[c - 1 + W]; st.pmk = P[c + 1 - W]; st.mmk = P[c - 1 - W];
+    st.jpkp = Kp[c + W]; st.jmkp = Kp[c - W]; st.jpkm = Km[c + W]; st.jmkm = Km[c - W];
+    st.ipkp = Kp[c + 1]; st.imkp = Kp[c - 1]; st.ipkm = Km[c + 1]; st.imkm = Km[c - 1];
+    st.f1c = F1[c]; st.f1ip = F1[c + 1]; st.f1im = F1[c - 1];
+    st.f4c = F4[c]; st.f4jp = F4[c + W]; st.f4jm = F4[c - W];
+    st.f2jp = F2[c + W]; st.f2jm = F2[c - W]; st.f2ip = F2[c + 1]; st.f2im = F2[c - 1];
+    st.f5jp = F5[c + W]; st.f5jm = F5[c - W];
+    st.f3ip = F3[c + 1]; st.f3im = F3[c - 1];
+    st.f6c = f6[gt]; st.f6kp = f6[gp]; st.f6km = f6[gm];
+    st.f5kp = f5[gp]; st.f5km = f5[gm];
+    st.f3kp = f3[gp]; st.f3km = f3[gm];
+    T tdiag, t1, t2;
+    op_eval(st, tdiag, t1, t2);
+    T v;
+    if (MODE == 0) {
+      v = rhs[gt] - (t1 + t2 + tdiag * st.c) * di2;
+      if (out32) out32[gt] = (float)v;
+    } else {
+      v = (t1 + t2 + tdiag * st.c) * di2;
+    }
+    if (out) out[gt] = v;
+    const auto vb = abs_bits(v);
+    mb = vb > mb ? vb : mb;
+  }
+  if (maxbits) block_max_commit(from_bits(mb), maxbits);
 }
 
 // Full-weighting restriction of the residual with the reference's

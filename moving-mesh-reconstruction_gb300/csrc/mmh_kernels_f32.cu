@@ -14,7 +14,11 @@ void launch_residual_fma(const double* phi, const double* rhs, const double* coe
   i64 n3 = (i64)n * n * n;
   double di2 = 1.0 / (dx * dx);
   prof_begin(KK_RESIDUAL, s, n3, n);
-  k_residual<double, true><<<grid_of(n3, kBlock), kBlock, 0, s>>>(phi, rhs, coef, n, di2, nullptr, r32, maxbits);
+  if (n >= 32)
+    k_stencil_plane<double, 0, true><<<dim3(n / 32, n / 16, n), 256, 0, s>>>(phi, rhs, coef, n, di2, nullptr, r32,
+                                                                             maxbits);
+  else
+    k_residual<double, true><<<grid_of(n3, kBlock), kBlock, 0, s>>>(phi, rhs, coef, n, di2, nullptr, r32, maxbits);
   prof_end(KK_RESIDUAL, s, n);
   count_launch();
 }

@@ -91,7 +91,10 @@ void launch_residual(const T* phi, const T* rhs, const T* coef, int n, T dx, T* 
   i64 n3 = (i64)n * n * n;
   T di2 = T(1) / (dx * dx);
   prof_begin(kk<T>(KK_RESIDUAL), s, n3, n);
-  k_residual<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(phi, rhs, coef, n, di2, r, r32, maxbits);
+  if (n >= 32)
+    k_stencil_plane<T, 0><<<dim3(n / 32, n / 16, n), 256, 0, s>>>(phi, rhs, coef, n, di2, r, r32, maxbits);
+  else
+    k_residual<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(phi, rhs, coef, n, di2, r, r32, maxbits);
   prof_end(kk<T>(KK_RESIDUAL), s, n);
   count_launch();
 }

@@ -96,7 +96,11 @@ template <class T>
 void launch_apply(const T* p, const T* coef, int n, T dx, T* q, unsigned long long* qbits, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
   prof_begin(kk<T>(KK_APPLY), s, n3, n);
-  k_apply<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(p, coef, n, T(1) / (dx * dx), q, qbits);
+  if (n >= 32)
+    k_stencil_plane<T, 1><<<dim3(n / 32, n / 16, n), 256, 0, s>>>(p, nullptr, coef, n, T(1) / (dx * dx), q, nullptr,
+                                                                 qbits);
+  else
+    k_apply<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(p, coef, n, T(1) / (dx * dx), q, qbits);
   prof_end(kk<T>(KK_APPLY), s, n);
   count_launch();
 }

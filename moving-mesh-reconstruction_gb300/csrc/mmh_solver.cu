@@ -228,10 +228,11 @@ int vcycle(mmh_ctx* c, int l) {
       RET(vcycle_fp64(c, l));
       launch_d2f(c->h64.u[l], F.u[l], n3, c->s);
       return MMH_OK;
+    } else {
+      RET(relax_level<T>(c, l, 32, post, &c->sc->r1bits[l]));
+      RET(relax_level<T>(c, l, 32, post, &c->sc->errbits[l]));
+      return guard_or_zerosum<T>(c, l, 1.001, 1.e-5, guard);
     }
-    RET(relax_level<T>(c, l, 32, post, &c->sc->r1bits[l]));
-    RET(relax_level<T>(c, l, 32, post, &c->sc->errbits[l]));
-    return guard_or_zerosum<T>(c, l, 1.001, 1.e-5, guard);
   }
   int nrelax = ref ? 4 * c->n / n : c->cfg.nu1;
   int nrelax2 = ref ? 4 * c->n / n : c->cfg.nu2;
