@@ -393,7 +393,7 @@ struct GsGeom {
   static constexpr int HB = 4, W = TX + 2 * HB, HT = TY + 2 * HB, H2 = W / 2, NXC = H2 - 2;
   static constexpr int Q = NXC + 32 * ((W - NXC + 31) / 32);
   static constexpr int OFFB0 = (HT / 2) * Q;
-  static constexpr int OFFB = OFFB0 + ((20 - OFFB0 % 32) + 32) % 32;  // first odd row (fewer store conflicts)
+  static constexpr int OFFB = OFFB0 + ((30 - OFFB0 % 32) + 32) % 32;  // first odd row (fewer store conflicts)
   static constexpr int SF = OFFB + (HT / 2) * Q;                       // words of one field
   static constexpr int NSF = 8;
   static constexpr int WORDS = NSF * SF;

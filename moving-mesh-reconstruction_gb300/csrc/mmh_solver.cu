@@ -840,11 +840,21 @@ int mmh_create(mmh_ctx** out, const mmh_config* cfg) {
     if (rc == MMH_OK) rc = c->alloc(p, count);
   };
   i64 n3 = c->n3;
+  // Scratch that is dead while relaxing runs (finest-level multigrid scratch,
+  // limiter and spectral buffers, PCG vectors) shares one allocation with the
+  // relaxing buffers, which are dead whenever that scratch is in use: this
+  // takes 18 fields off the footprint (1024^3 fits on one GPU).
+  struct Piece {
+    void** p;
+    size_t bytes;
+  };
+  std::vector<Piece> shared;
+  auto S = [&](auto** p, i64 count) { shared.push_back({(void**)p, sizeof(**p) * (size_t)count}); };
   A(&c->def, n3);
   A(&c->rho, n3);
-  A(&c->scr, n3);
-  A(&c->defplim, n3);
-  A(&c->det, n3);
+  S(&c->scr, n3);
+  S(&c->defplim, n3);
+  S(&c->det, n3);
   c->h64.u.resize(c->nlev);
   c->h64.rhs.resize(c->nlev);
   c->h64.coef.resize(c->nlev);
@@ -855,12 +865,14 @@ int mmh_create(mmh_ctx** out, const mmh_config* cfg) {
     i64 m3 = (i64)c->nl[l] * c->nl[l] * c->nl[l];
     A(&c->h64.u[l], m3);
     A(&c->h64.rhs[l], m3);
-    A(&c->h64.coef[l], 6 * m3);
-    A(&c->h64.r[l], m3);
     if (l == 0) {
+      S(&c->h64.coef[l], 6 * m3);
+      S(&c->h64.r[l], m3);
       c->defl[0] = c->def;
       c->rhol[0] = c->rho;
     } else {
+      A(&c->h64.coef[l], 6 * m3);
+      A(&c->h64.r[l], m3);
       A(&c->defl[l], m3);
       A(&c->rhol[l], m3);
     }
@@ -872,32 +884,54 @@ int mmh_create(mmh_ctx** out, const mmh_config* cfg) {
     c->h32.r.resize(c->nlev);
     for (int l = 0; l < c->nlev; ++l) {
       i64 m3 = (i64)c->nl[l] * c->nl[l] * c->nl[l];
-      A(&c->h32.u[l], m3);
-      A(&c->h32.rhs[l], m3);
-      A(&c->h32.coef[l], 6 * m3);
-      A(&c->h32.r[l], m3);
+      if (l == 0) {
+        S(&c->h32.u[l], m3);
+        S(&c->h32.rhs[l], m3);
+        S(&c->h32.coef[l], 6 * m3);
+        S(&c->h32.r[l], m3);
+      } else {
+        A(&c->h32.u[l], m3);
+        A(&c->h32.rhs[l], m3);
+        A(&c->h32.coef[l], 6 * m3);
+        A(&c->h32.r[l], m3);
+      }
     }
   }
   if (cfg->schedule == MMH_SCHED_TOL) {
-    A(&c->px, n3);
-    A(&c->pb, n3);
+    S(&c->px, n3);
+    S(&c->pb, n3);
     if (cfg->precision == MMH_FP64) {
-      A(&c->pp, n3);
-      A(&c->pq, n3);
+      S(&c->pp, n3);
+      S(&c->pq, n3);
     } else {
-      A(&c->pe32, n3);
-      A(&c->pb32, n3);
-      A(&c->pp32, n3);
-      A(&c->pq32, n3);
+      S(&c->pe32, n3);
+      S(&c->pb32, n3);
+      S(&c->pp32, n3);
+      S(&c->pq32, n3);
     }
   }
-  A(&c->baj, 7 * n3);
-  A(&c->cc, n3);
-  A(&c->vt, 6 * n3);  // half sums and differences of the relaxing fluxes
-  A(&c->gface, 3 * n3);
-  A(&c->u1, n3);
-  A((double**)&c->Xc, 2 * (i64)(n / 2 + 1) * n * n);
-  A((double**)&c->Z, 2 * (i64)(n / 2) * n * n);
+  S((double**)&c->Xc, 2 * (i64)(n / 2 + 1) * n * n);
+  S((double**)&c->Z, 2 * (i64)(n / 2) * n * n);
+  {
+    const size_t align = 256;
+    size_t total = 0;
+    for (const Piece& q : shared) total += (q.bytes + align - 1) / align * align;
+    const size_t relax_bytes = sizeof(double) * 18 * (size_t)n3;  // baj 7, cc 1, sd 6, faces 3, u1 1
+    double* arena = nullptr;
+    A(&arena, (i64)((std::max(total, relax_bytes) + sizeof(double) - 1) / sizeof(double)));
+    if (rc == MMH_OK) {
+      char* at = reinterpret_cast<char*>(arena);
+      for (const Piece& q : shared) {
+        *q.p = at;
+        at += (q.bytes + align - 1) / align * align;
+      }
+      c->baj = arena;
+      c->cc = arena + 7 * n3;
+      c->vt = arena + 8 * n3;  // half sums and differences of the relaxing fluxes
+      c->gface = arena + 14 * n3;
+      c->u1 = arena + 17 * n3;
+    }
+  }
   A(&c->sc, 1);
   if (rc == MMH_OK && cudaMallocHost((void**)&c->hsc, sizeof(Scal)) != cudaSuccess) rc = MMH_ERR_NOMEM;
   if (rc == MMH_OK && cudaMemsetAsync(c->sc, 0, sizeof(Scal), c->s) != cudaSuccess) rc = MMH_ERR_CUDA;
