@@ -20,6 +20,7 @@ enum KernelKind {
 void prof_begin(int kind, cudaStream_t s, i64 cells, int n);
 void prof_end(int kind, cudaStream_t s, int n);
 int prof_start(int kind);
+bool prof_armed();  // timing hooks armed: launches must stay individual (no graph replay)
 int prof_stop(int* launches, double* ms, long long* cells);
 template <class T> inline int kk(int base) { return base | (sizeof(T) == 4 ? KK_F32 : 0); }
 

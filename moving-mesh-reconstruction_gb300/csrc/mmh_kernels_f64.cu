@@ -27,6 +27,8 @@ struct Prof {
 Prof g_prof;
 }  // namespace
 
+bool prof_armed() { return g_prof.kind != 0; }
+
 int prof_start(int kind) {
   if (g_prof.ev.empty()) {
     g_prof.ev.resize(2 * 8192);

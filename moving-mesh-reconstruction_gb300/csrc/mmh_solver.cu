@@ -113,6 +113,12 @@ struct mmh_ctx {
   bool plans = false;
   Scal* sc = nullptr;   // device
   Scal* hsc = nullptr;  // pinned host mirror
+  // CUDA graphs of the preconditioner cycle per precision (0 FP64, 1 FP32) and
+  // entry level, with the number of library kernels one replay runs
+  cudaGraphExec_t pgraph[2][16] = {};
+  unsigned long long pgraph_launches[2][16] = {};
+  bool pgraph_seen[2][16] = {};
+  bool graphs = true;
   std::vector<void*> allocs;
   int last_status = MMH_OK;
 
@@ -288,6 +294,48 @@ int precond(mmh_ctx* c, int l0, unsigned long long* zbits) {
   return MMH_OK;
 }
 
+// The preconditioner cycle runs tens of launches with no host
+// synchronisation, so after one direct run (which also performs the one-time
+// kernel attribute setup) it is captured into a CUDA graph and replayed: one
+// launch per application instead of one per kernel.  Direct runs stay when
+// the kernel timing hooks are armed (they time launches one by one) or when a
+// capture fails.
+template <class T>
+int precond_replay(mmh_ctx* c, int l0, unsigned long long* zbits) {
+  const int ti = std::is_same<T, float>::value ? 1 : 0;
+  if (!c->graphs || l0 >= 16 || prof_armed()) return precond<T>(c, l0, zbits);
+  cudaGraphExec_t& ex = c->pgraph[ti][l0];
+  if (!ex) {
+    if (!c->pgraph_seen[ti][l0]) {
+      c->pgraph_seen[ti][l0] = true;
+      return precond<T>(c, l0, zbits);
+    }
+    const unsigned long long before = launch_count();
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      c->graphs = false;
+      return precond<T>(c, l0, zbits);
+    }
+    int rc = precond<T>(c, l0, zbits);
+    cudaError_t e = cudaStreamEndCapture(c->s, &g);
+    if (rc == MMH_OK && e == cudaSuccess && g && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess) {
+      cudaGraphDestroy(g);
+      c->pgraph_launches[ti][l0] = launch_count() - before;  // counted once, for the first replay
+      CK(cudaGraphLaunch(ex, c->s));
+      return MMH_OK;
+    }
+    if (g) cudaGraphDestroy(g);
+    ex = nullptr;
+    cudaGetLastError();
+    c->graphs = false;
+    return precond<T>(c, l0, zbits);
+  }
+  CK(cudaGraphLaunch(ex, c->s));
+  count_launch((int)c->pgraph_launches[ti][l0]);
+  return MMH_OK;
+}
+
 // Flexible preconditioned conjugate gradients on L x = b at level l0 in
 // precision T, one V-cycle per iteration as preconditioner, until
 // max|r| <= tol * bn (recurrence residual) or maxit iterations.  The
@@ -310,7 +358,7 @@ int pcg_core(mmh_ctx* c, int l0, double dx, T* x, const T* b, T* p, T* q, double
   int it = 0;
   int status = MMH_OK;
   if (rel > tol) {
-    RET(precond<T>(c, l0, &P->zbits));
+    RET(precond_replay<T>(c, l0, &P->zbits));
     CK(cudaMemcpyAsync(p, z, sizeof(T) * n3, cudaMemcpyDeviceToDevice, c->s));
     CK(cudaMemcpyAsync(&P->pbits, &P->zbits, 8, cudaMemcpyDeviceToDevice, c->s));
     launch_dot<T>(r, z, n3, &P->rbits, &P->zbits, P->acc[0], c->s);
@@ -330,7 +378,7 @@ int pcg_core(mmh_ctx* c, int l0, double dx, T* x, const T* b, T* p, T* q, double
         status = MMH_ERR_DIVERGED;
         break;
       }
-      RET(precond<T>(c, l0, &P->zbits));
+      RET(precond_replay<T>(c, l0, &P->zbits));
       CK(cudaMemsetAsync(P->acc[0], 0, 16, c->s));
       CK(cudaMemsetAsync(P->acc[2], 0, 16, c->s));
       launch_dot<T>(z, q, n3, &P->zbits, &P->qbits, P->acc[2], c->s);
@@ -800,6 +848,9 @@ int mmh_destroy(mmh_ctx* c) {
     cufftDestroy(c->pd2z);
     cufftDestroy(c->pz2z);
   }
+  for (auto& row : c->pgraph)
+    for (cudaGraphExec_t& ex : row)
+      if (ex) cudaGraphExecDestroy(ex);
   for (void* p : c->allocs) cudaFree(p);
   if (c->hsc) cudaFreeHost(c->hsc);
   if (c->own_stream && c->s) cudaStreamDestroy(c->s);
