@@ -166,6 +166,27 @@ int mmh_outputs_dev(mmh_ctx* ctx, double* d_grad, double* d_delta);
 /* Device pointers of the resident state (n^3 doubles each). */
 int mmh_state_dev(mmh_ctx* ctx, double** d_def, double** d_rho, double** d_defp);
 
+/* ---- batched realisations (no single call in the reference) ------------ */
+/* One independent reconstruction of mmh/main.f90:83-179: density rho (n^3,
+ * Fortran order, host), def = 0, niter deformation iterations, then the
+ * outputs; def/grad/delta are host outputs (each may be NULL: not copied). */
+typedef struct mmh_problem {
+  int n;             /* grid size: power of two, 8..1024 */
+  int niter;         /* deformation iterations */
+  const double* rho; /* n^3 density */
+  double* def;       /* n^3 deformation potential out */
+  double* grad;      /* 3 n^3 displacement out (scalar2gradient) */
+  double* delta;     /* n^3 density out (defp2delta) */
+  int status;        /* out: MMH_OK, or the error of this problem */
+  int vcycles;       /* out: V-cycles / PCG iterations of its last solve */
+} mmh_problem;
+/* Run count problems with the settings of cfg (cfg->n is ignored: each problem
+ * has its own) on `workers` concurrent host threads, each with its own CUDA
+ * stream and one context per grid size, reused across that worker's problems
+ * (largest problems first).  Results are those of running each problem alone.
+ * Returns MMH_OK, or the first failing problem's status (all problems run). */
+int mmh_batch_run(const mmh_config* cfg, mmh_problem* probs, int count, int workers);
+
 /* ---- allocation-free relax (no counterpart in the reference) ----------- */
 /* For callers that cannot let a library allocate device memory (a driver that
  * hands out every buffer from its own pool, or one that must not allocate in a

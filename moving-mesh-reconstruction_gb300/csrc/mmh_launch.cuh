@@ -32,11 +32,11 @@ void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nswe
   if (n >= 64) {
     constexpr int TX = GsTile<T>::TX, TY = GsTile<T>::TY;
     const size_t smem = sizeof(T) * GsGeom<T, TX, TY>::WORDS;
-    static bool attr = false;
-    if (!attr) {
-      cudaFuncSetAttribute(k_gs_plane<T, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      attr = true;
-    }
+    // once per process (thread-safe static initialisation)
+    static const bool attr =
+        cudaFuncSetAttribute(k_gs_plane<T, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+        cudaSuccess;
+    (void)attr;
     dim3 grid(n / TX, n / TY, n / 2);
     // double buffer: a sweep reads a and leaves the swept field in b
     T* a = phi;

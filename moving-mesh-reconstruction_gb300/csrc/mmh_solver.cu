@@ -703,15 +703,19 @@ int download(mmh_ctx* c, const double* src, H* dst, i64 count) {
 template <class H>
 int upload_density(mmh_ctx* c, const H* u, int nf, i64 n3, double* dst) {
   if (nf < 1 || nf > 5) return MMH_ERR_ARG;
-  H* tmpu = nullptr;
-  CK(cudaMallocAsync((void**)&tmpu, sizeof(H) * n3 * nf, c->s));
+  if (nf == 1 && std::is_same<H, double>::value) {
+    CK(cudaMemcpyAsync(dst, u, sizeof(double) * n3, cudaMemcpyHostToDevice, c->s));
+    return MMH_OK;
+  }
+  // staged in the finest-level coefficient planes (6 n^3 doubles), which hold
+  // nothing between solves
+  H* tmpu = reinterpret_cast<H*>(c->h64.coef[0]);
   CK(cudaMemcpyAsync(tmpu, u, sizeof(H) * n3 * nf, cudaMemcpyHostToDevice, c->s));
   CK(cudaMemsetAsync(&c->sc->bad, 0, sizeof(int), c->s));
   if (std::is_same<H, double>::value)
     launch_extract_density_d((const double*)tmpu, nf, n3, dst, &c->sc->bad, c->s);
   else
     launch_extract_density_f((const float*)tmpu, nf, n3, dst, &c->sc->bad, c->s);
-  CK(cudaFreeAsync(tmpu, c->s));
   RET(pull_scal(c));
   if (c->hsc->bad) return MMH_ERR_UNSUPPORTED;
   return MMH_OK;
@@ -786,11 +790,9 @@ int spectral_host(mmh_ctx* c, const H* in, H* out, const int* nn, bool grad) {
   if (!c || !in || !out || !nn) return MMH_ERR_ARG;
   if (nn[0] != c->n || nn[1] != c->n || nn[2] != c->n) return MMH_ERR_SIZE;
   RET(upload(c, in, c->scr, c->n3));
-  double* o = nullptr;
-  CK(cudaMallocAsync((void**)&o, sizeof(double) * c->n3 * (grad ? 3 : 1), c->s));
+  double* o = c->h64.coef[0];  // staging: holds nothing between solves
   int st = spectral_outputs(c, c->scr, grad ? o : nullptr, grad ? nullptr : o);
   if (st == MMH_OK) st = download(c, o, out, c->n3 * (grad ? 3 : 1));
-  cudaFreeAsync(o, c->s);
   return st;
 }
 
@@ -1241,12 +1243,12 @@ int mmh_store_f64(mmh_ctx* c, double* def, double* u, int nfluid) {
 
 int mmh_outputs_f64(mmh_ctx* c, double* grad, double* delta) {
   if (!c) return MMH_ERR_ARG;
-  double* o = nullptr;
-  CK(cudaMallocAsync((void**)&o, sizeof(double) * c->n3 * 4, c->s));
+  // staged in the finest-level coefficient planes (6 n^3 doubles), which hold
+  // nothing between solves and are not used by the spectral transforms
+  double* o = c->h64.coef[0];
   int st = spectral_outputs(c, c->def, grad ? o : nullptr, delta ? o + 3 * c->n3 : nullptr);
   if (st == MMH_OK && grad) st = download(c, o, grad, 3 * c->n3);
   if (st == MMH_OK && delta) st = download(c, o + 3 * c->n3, delta, c->n3);
-  cudaFreeAsync(o, c->s);
   return st;
 }
 

@@ -38,7 +38,7 @@ EXPORTS = (
     "mmh_rgzerosum_f64", "mmh_nsmooth_f64", "mmh_limiter_pass1_f64", "mmh_limiter_mask_f64",
     "mmh_limiter_poisson_f64", "mmh_load_f64", "mmh_load_dev", "mmh_iterate", "mmh_store_f64",
     "mmh_outputs_f64", "mmh_outputs_dev", "mmh_state_dev", "mmh_profile_start", "mmh_profile_stop",
-    "mmh_relax_noalloc_f64",
+    "mmh_relax_noalloc_f64", "mmh_batch_run",
 )
 
 # kernel kinds for the timing hooks
@@ -74,6 +74,11 @@ class Diag(C.Structure):
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad"}
+
+
+class Problem(C.Structure):
+    _fields_ = [("n", C.c_int), ("niter", C.c_int), ("rho", C.c_void_p), ("def_", C.c_void_p),
+                ("grad", C.c_void_p), ("delta", C.c_void_p), ("status", C.c_int), ("vcycles", C.c_int)]
 
 
 _lib = None
@@ -340,3 +345,37 @@ def reconstruct(rho, niter, precision=MMH_FP64, schedule=MMH_SCHED_REF, tol=1e-1
             ctx.outputs(grad, delta)
             res["grad"], res["delta"] = grad, delta
         return res
+
+
+def batch_run(rhos, niter, workers=4, precision=MMH_MIXED, schedule=MMH_SCHED_TOL, tol=1e-8, max_cycles=200,
+              outputs=True, device=0, check=True, **kw):
+    """mmh_batch_run: independent reconstructions of the densities `rhos`
+    (Fortran-ordered float64 cubes, any mix of power-of-two sizes) on
+    `workers` concurrent host workers.  Returns one dict per problem with
+    def, grad, delta (None when outputs=False), status and vcycles; raises
+    MMHError on a failed problem unless check=False."""
+    L = lib()
+    cfg = Config()
+    L.mmh_config_default(C.byref(cfg), 8)
+    cfg.precision, cfg.schedule, cfg.tol, cfg.max_cycles, cfg.device = (int(precision), int(schedule), float(tol),
+                                                                       int(max_cycles), int(device))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    probs = (Problem * len(rhos))()
+    keep = []
+    for i, r in enumerate(rhos):
+        r = _farr(r, np.float64)
+        n = r.shape[0]
+        d = np.zeros((n, n, n), order="F")
+        g = np.zeros((n, n, n, 3), order="F") if outputs else None
+        de = np.zeros((n, n, n), order="F") if outputs else None
+        keep.append((r, d, g, de))
+        probs[i] = Problem(n, int(niter), r.ctypes.data, d.ctypes.data, None if g is None else g.ctypes.data,
+                           None if de is None else de.ctypes.data, 0, 0)
+    rc = L.mmh_batch_run(C.byref(cfg), probs, len(rhos), int(workers))
+    out = [{"def": k[1], "grad": k[2], "delta": k[3], "status": probs[i].status, "vcycles": probs[i].vcycles}
+           for i, k in enumerate(keep)]
+    if check and rc not in (MMH_OK, MMH_ERR_DIVERGED):
+        raise MMHError(rc, "batch_run")
+    return out
+
