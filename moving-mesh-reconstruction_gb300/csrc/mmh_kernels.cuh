@@ -405,6 +405,7 @@ struct GsGeom {
   }
   static_assert(Q >= W && (Q - NXC) % 32 == 0 && Q % 2 == 0 && OFFB % 2 == 0, "row pitch");
   static_assert(HT % 2 == 0 && TX % 4 == 0 && HB == 4, "tile shape");
+  static_assert(NXC * (TY / 2 + 3) <= 256, "one cell per thread and colour (256 threads)");
 };
 
 // Store one 16-byte group (cells x0..x0+VW-1 of tile row y) into a field at
@@ -451,6 +452,28 @@ __global__ void __launch_bounds__(256, 4) k_gs_plane(const T* __restrict__ src, 
   const V* vnbr = reinterpret_cast<const V*>(nbr);
   const V* vcoef = reinterpret_cast<const V*>(coef);
   const i64 nv3 = n3 / VW;
+  const T* f3 = coef + 2 * n3;
+  const T* f5 = coef + 4 * n3;
+  const T* f6 = coef + 5 * n3;
+  // The fields read only at the cell itself (rhs, coefficient 6 of P,
+  // coefficients 3, 5, 6 of P+-1) of this thread's cell of colour q (at most
+  // one cell per colour): colour 0's are requested before the tile loads and
+  // colour q+1's while colour q computes, so their latency overlaps work.
+  auto centre = [&](int q, T* o) {
+    const int io = q >> 1;
+    const int e = threadIdx.x;
+    if (e >= NXC * G::ny(q)) return;
+    const int m = e % NXC, t = e / NXC;
+    int gi = i0 + G::XS(io) + 2 * m, gj = j0 + G::ys(q) + 2 * t;
+    gi += (gi < 0) ? n : ((gi >= n) ? -n : 0);
+    gj += (gj < 0) ? n : ((gj >= n) ? -n : 0);
+    const i64 g = (i64)gi + (i64)n * gj;
+    const i64 gt = g + n2 * k, gm = g + n2 * kmn, gp = g + n2 * kpn;
+    o[0] = rhs[gt]; o[1] = f6[gt]; o[2] = f6[gm]; o[3] = f6[gp];
+    o[4] = f3[gm]; o[5] = f5[gm]; o[6] = f3[gp]; o[7] = f5[gp];
+  };
+  T pre[8];
+  centre(0, pre);
   for (int e = threadIdx.x; e < NVT; e += blockDim.x) {
     const int xv = e % NV, y = 1 + e / NV, x0 = xv * VW;
     int gi = i0 + x0, gj = j0 + y;
@@ -477,30 +500,28 @@ __global__ void __launch_bounds__(256, 4) k_gs_plane(const T* __restrict__ src, 
   const T* F3 = sm + 5 * SF;
   const T* F4 = sm + 6 * SF;
   const T* F5 = sm + 7 * SF;
-  const T* f3 = coef + 2 * n3;
-  const T* f5 = coef + 4 * n3;
-  const T* f6 = coef + 5 * n3;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
+    T cur[8];
+#pragma unroll
+    for (int z = 0; z < 8; ++z) cur[z] = pre[z];
+    if (q < 3) centre(q + 1, pre);
     const int io = q >> 1, jo = q & 1;
     const int cnt = NXC * G::ny(q);
     // word offsets of the x+-1 and y+-1 neighbours (constant within a colour)
     const int oxp = io ? 1 - H2 : H2, oxm = io ? -H2 : H2 - 1;
     const int oyp = jo ? Q - OFFB : OFFB, oym = jo ? -OFFB : OFFB - Q;
-    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    // one cell per thread: a colour has at most NXC * ny(0) <= 256 cells
+    if (threadIdx.x < cnt) {
+      const int e = threadIdx.x;
       const int m = e % NXC, t = e / NXC;
       const int x = G::XS(io) + 2 * m, y = G::ys(q) + 2 * t;
       const int c = G::word(x, y);
-      int gi = i0 + x, gj = j0 + y;
-      gi += (gi < 0) ? n : ((gi >= n) ? -n : 0);
-      gj += (gj < 0) ? n : ((gj >= n) ? -n : 0);
-      const i64 g = (i64)gi + (i64)n * gj;
-      const i64 gt = g + n2 * k, gm = g + n2 * kmn, gp = g + n2 * kpn;
       const int cxp = c + oxp, cxm = c + oxm, cyp = c + oyp, cym = c + oym;
       Stencil<T> st;
-      st.f6c = f6[gt]; st.f6km = f6[gm]; st.f6kp = f6[gp];
-      st.f3km = f3[gm]; st.f5km = f5[gm]; st.f3kp = f3[gp]; st.f5kp = f5[gp];
-      const T r = rhs[gt];
+      st.f6c = cur[1]; st.f6km = cur[2]; st.f6kp = cur[3];
+      st.f3km = cur[4]; st.f5km = cur[5]; st.f3kp = cur[6]; st.f5kp = cur[7];
+      const T r = cur[0];
       st.c = sP[c]; st.ip = sP[cxp]; st.im = sP[cxm]; st.jp = sP[cyp]; st.jm = sP[cym];
       st.kp = sKp[c]; st.km = sKm[c];
       st.ppk = sP[cxp + oyp]; st.mpk = sP[cxm + oyp]; st.pmk = sP[cxp + oym]; st.mmk = sP[cxm + oym];
@@ -571,6 +592,24 @@ __global__ void __launch_bounds__(256) k_stencil_plane(const T* __restrict__ phi
   const V* vphi = reinterpret_cast<const V*>(phi);
   const V* vcoef = reinterpret_cast<const V*>(coef);
   const i64 nv3 = n3 / VW;
+  // the fields read only at the thread's own cells are requested first, so
+  // their latency overlaps the tile loads
+  constexpr int NCELL = TY / (256 / TX);
+  const int tx = threadIdx.x % TX, ty0 = threadIdx.x / TX;
+  const T* f3 = coef + 2 * n3;
+  const T* f5 = coef + 4 * n3;
+  const T* f6 = coef + 5 * n3;
+  T c6[NCELL], c6p[NCELL], c6m[NCELL], c5p[NCELL], c5m[NCELL], c3p[NCELL], c3m[NCELL], cr[NCELL];
+#pragma unroll
+  for (int q = 0; q < NCELL; ++q) {
+    const int ty = ty0 + q * (256 / TX);
+    const i64 g = (i64)(blockIdx.x * TX + tx) + (i64)n * (blockIdx.y * TY + ty);
+    const i64 gt = g + n2 * k, gm = g + n2 * kmn, gp = g + n2 * kpn;
+    c6[q] = f6[gt]; c6p[q] = f6[gp]; c6m[q] = f6[gm];
+    c5p[q] = f5[gp]; c5m[q] = f5[gm];
+    c3p[q] = f3[gp]; c3m[q] = f3[gm];
+    cr[q] = MODE == 0 ? rhs[gt] : T(0);
+  }
   for (int e = threadIdx.x; e < NVT; e += blockDim.x) {
     const int xv = e % NV, y = e / NV, x0 = xv * VW;
     int gi = i0 + x0, gj = j0 + y;
@@ -596,15 +635,12 @@ __global__ void __launch_bounds__(256) k_stencil_plane(const T* __restrict__ phi
   const T* F3 = sm + 5 * S;
   const T* F4 = sm + 6 * S;
   const T* F5 = sm + 7 * S;
-  const T* f3 = coef + 2 * n3;
-  const T* f5 = coef + 4 * n3;
-  const T* f6 = coef + 5 * n3;
   decltype(abs_bits(T(0))) mb = 0;
-  const int tx = threadIdx.x % TX;
-  for (int ty = threadIdx.x / TX; ty < TY; ty += blockDim.x / TX) {
+#pragma unroll
+  for (int q = 0; q < NCELL; ++q) {
+    const int ty = ty0 + q * (256 / TX);
     const int c = (1 + ty) * W + HX + tx;
-    const i64 g = (i64)(blockIdx.x * TX + tx) + (i64)n * (blockIdx.y * TY + ty);
-    const i64 gt = g + n2 * k, gm = g + n2 * kmn, gp = g + n2 * kpn;
+    const i64 gt = (i64)(blockIdx.x * TX + tx) + (i64)n * (blockIdx.y * TY + ty) + n2 * k;
     Stencil<T> st;
     st.c = P[c]; st.ip = P[c + 1]; st.im = P[c - 1]; st.jp = P[c + W]; st.jm = P[c - W];
     st.kp = Kp[c]; st.km = Km[c];
@@ -616,14 +652,14 @@ __global__ void __launch_bounds__(256) k_stencil_plane(const T* __restrict__ phi
     st.f2jp = F2[c + W]; st.f2jm = F2[c - W]; st.f2ip = F2[c + 1]; st.f2im = F2[c - 1];
     st.f5jp = F5[c + W]; st.f5jm = F5[c - W];
     st.f3ip = F3[c + 1]; st.f3im = F3[c - 1];
-    st.f6c = f6[gt]; st.f6kp = f6[gp]; st.f6km = f6[gm];
-    st.f5kp = f5[gp]; st.f5km = f5[gm];
-    st.f3kp = f3[gp]; st.f3km = f3[gm];
+    st.f6c = c6[q]; st.f6kp = c6p[q]; st.f6km = c6m[q];
+    st.f5kp = c5p[q]; st.f5km = c5m[q];
+    st.f3kp = c3p[q]; st.f3km = c3m[q];
     T tdiag, t1, t2;
     op_eval(st, tdiag, t1, t2);
     T v;
     if (MODE == 0) {
-      v = rhs[gt] - (t1 + t2 + tdiag * st.c) * di2;
+      v = cr[q] - (t1 + t2 + tdiag * st.c) * di2;
       if (out32) out32[gt] = (float)v;
     } else {
       v = (t1 + t2 + tdiag * st.c) * di2;

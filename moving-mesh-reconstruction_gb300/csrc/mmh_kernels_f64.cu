@@ -525,6 +525,10 @@ void launch_spec_unpack(const void* z, int n, double* out, int stride_out, int a
 __device__ __forceinline__ double zdiv(double d) { return (d == d && d != 0.0) ? copysign(0.0, d) : 0.0 / d; }
 // biased binary exponent: 0 for zero and subnormals, 2047 for inf and NaN
 __device__ __forceinline__ int bexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
+// MIN/MAX as the restatement evaluates them (std::min / std::max: a
+// comparison and a select), so NaN arguments propagate the same way.
+__device__ __forceinline__ double ref_min(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double ref_max(double a, double b) { return (a < b) ? b : a; }
 
 // dpv (relaxing.f90:269-496) forms, at every stencil point along axis a, the
 // flux w_a = v_a / c divided by the freezing speed and then only the half sums
@@ -582,7 +586,7 @@ __global__ void k_relax_stage1(const double* __restrict__ rho, const double* __r
     const int eu = bexp(u0), ed = bexp(det);
     const int eb = max(max(max(bexp(m.b11), bexp(m.b12)), max(bexp(m.b13), bexp(m.b22))), max(bexp(m.b23), bexp(m.b33)));
     if (eu >= 1 && eu <= 2046 && ed >= 1 && ed <= 2046 && abs(eu - ed) <= 1000 && eb <= 1523) {
-      c = fmax(fmax(fabs(vv1), fabs(vv2)), fabs(vv3));
+      c = ref_max(ref_max(fabs(vv1), fabs(vv2)), fabs(vv3));
     } else {
       double rhoc = u0 / det;
       double kin = rhoc * (vx * vx + vy * vy + vz * vz) / 2.0;
@@ -592,7 +596,7 @@ __global__ void k_relax_stage1(const double* __restrict__ rho, const double* __r
       double blim1 = cs * sqrt(m.b11 * m.b11 + m.b12 * m.b12 + m.b13 * m.b13) + fabs(vv1);
       double blim2 = cs * sqrt(m.b12 * m.b12 + m.b22 * m.b22 + m.b23 * m.b23) + fabs(vv2);
       double blim3 = cs * sqrt(m.b13 * m.b13 + m.b23 * m.b23 + m.b33 * m.b33) + fabs(vv3);
-      c = fmax(fmax(blim1, blim2), blim3);
+      c = ref_max(ref_max(blim1, blim2), blim3);
     }
     cc[t] = c;
   }
@@ -662,8 +666,8 @@ __device__ __forceinline__ double fsign1(double a) { return a >= 0.0 ? 1.0 : -1.
 __device__ __forceinline__ double minmod(double a, double b) {
   const double wslopelim = 1.5, wbee = 1.0;
   double x = fabs(a), y = fabs(b);
-  double lo = fmin(x, y), hi = fmax(x, y);
-  double mm = bexp(lo) < 2047 ? fmin(wslopelim * lo, hi) : fmin(wslopelim * lo, wbee * hi + (1.0 - wbee) * lo);
+  double lo = ref_min(x, y), hi = ref_max(x, y);
+  double mm = bexp(lo) < 2047 ? ref_min(wslopelim * lo, hi) : ref_min(wslopelim * lo, wbee * hi + (1.0 - wbee) * lo);
   if (bexp(mm) < 2046) {
     const bool pa = a >= 0.0, pb = b >= 0.0;
     return pa != pb ? 0.0 : (pa ? mm : -mm);

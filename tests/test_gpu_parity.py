@@ -244,6 +244,30 @@ def test_relaxing_bitexact(mmh, oracle, fields, n):
     assert np.all(ug[1:] == 0)
 
 
+@pytest.mark.parametrize("n", [16, 32])
+def test_relaxing_degenerate_cells(mmh, oracle, fields, n):
+    """Cells with zero density and a tangled metric take the relaxing
+    kernels' general paths (0/x by division, the full sound-speed expression,
+    minmod with NaN operands): the density has the oracle's bits, NaN where
+    the reference produces NaN.  (The reference's momentum and energy turn
+    NaN next to an empty cell, 0/0 in its velocity; the GPU carries only the
+    density and leaves u(2:5) at zero.)"""
+    defpot = smooth_field(n, 3.0, 18)  # strong deformation: tangled cells, det <= 0
+    defp = smooth_field(n, 0.05, 19)
+    _, u = fields.initial_state(n, sigma=1.0, seed=20)
+    rng = np.random.default_rng(n)
+    flat = u[0].reshape(-1, order="F")
+    flat[rng.choice(flat.size, 12, replace=False)] = 0.0  # empty cells
+    u[0] = flat.reshape((n, n, n), order="F")
+    uo = oracle.relaxing(u, defpot, defp)
+    ug = u.copy(order="F")
+    with mmh.Context(n) as ctx:
+        ctx.relaxing(ug, defpot, defp)
+    assert np.array_equal(uo[0], ug[0], equal_nan=True)
+    assert np.isnan(uo[0]).any()  # the degenerate cells did reach the general paths
+    assert np.all(ug[1:] == 0)
+
+
 @pytest.mark.parametrize("n,sigma,amp", [(16, 1.0, 0.05), (32, 1.5, 0.3), (16, 1.0, 2.0), (32, 1.5, 2.0)])
 def test_calcdefp_ref(mmh, oracle, fields, n, sigma, amp):
     """calcdefp (reference schedule): bit-exact without the FFT correction,
