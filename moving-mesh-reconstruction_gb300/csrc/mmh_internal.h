@@ -97,5 +97,10 @@ void launch_pcg_update(T* x, T* r, const T* p, const T* q, i64 count, const doub
 template <class T>
 void launch_pcg_pupdate(T* p, const T* z, i64 count, const double* beta, unsigned long long* pbits, cudaStream_t s);
 void launch_pcg_scalar(PcgDev* st, int stage, cudaStream_t s);
+// Fast deterministic FP32 dot product (mixed form's inner solve): kDotBlocks
+// block sums in `part`, result into acc in the exact dot's fixed-point form.
+constexpr int kDotBlocks = 152 * 8;
+void launch_dot_fast(const float* a, const float* b, i64 count, const unsigned long long* abits,
+                     const unsigned long long* bbits, unsigned long long* acc, double* part, cudaStream_t s);
 
 }  // namespace mmh

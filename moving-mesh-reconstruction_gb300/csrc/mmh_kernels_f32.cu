@@ -7,6 +7,69 @@ namespace mmh {
 MMH_INSTANTIATE(float)
 MMH_INSTANTIATE_PCG(float)
 
+// Dot product of two FP32 vectors for the mixed form's inner solve, whose
+// results are not bit-matched to the oracle: a fixed grid of kDotBlocks
+// blocks, each thread summing its strided products in FP32 with four
+// accumulators, each block reducing in a fixed pattern, and one block adding
+// the block sums in FP64 in a fixed order -- deterministic, and bound by
+// memory instead of by the integer work of the exact form.  The result is
+// stored in the fixed-point form (same scale) the PCG scalar kernel reads.
+__device__ __forceinline__ float block_sum_f32(float v, float* buf) {
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) buf[w] = v;
+  __syncthreads();
+  float t = 0.f;
+  if (threadIdx.x == 0)
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += buf[q];
+  return t;
+}
+
+__global__ void __launch_bounds__(256) k_dot_f32_part(const float* __restrict__ a, const float* __restrict__ b,
+                                                      i64 count, double* __restrict__ part) {
+  __shared__ float buf[32];
+  const i64 stride = (i64)gridDim.x * blockDim.x;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+  for (; t + 3 * stride < count; t += 4 * stride) {
+    s0 += a[t] * b[t];
+    s1 += a[t + stride] * b[t + stride];
+    s2 += a[t + 2 * stride] * b[t + 2 * stride];
+    s3 += a[t + 3 * stride] * b[t + 3 * stride];
+  }
+  for (; t < count; t += stride) s0 += a[t] * b[t];
+  const float blk = block_sum_f32((s0 + s1) + (s2 + s3), buf);
+  if (threadIdx.x == 0) part[blockIdx.x] = (double)blk;
+}
+
+__global__ void __launch_bounds__(256) k_dot_f32_final(const double* __restrict__ part, int nparts,
+                                                       const unsigned long long* abits,
+                                                       const unsigned long long* bbits, unsigned long long* acc) {
+  __shared__ double buf[256];
+  double s = 0.0;
+  for (int q = threadIdx.x; q < nparts; q += blockDim.x) s += part[q];
+  buf[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) buf[threadIdx.x] += buf[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double ma = bits_d(abits), mb = bits_d(bbits);
+    __int128 v = 0;
+    if (ma > 0.0 && mb > 0.0 && fabs(buf[0]) < INFINITY) v = fx_bits(buf[0], 96 - (ilogb(ma) + ilogb(mb) + 2));
+    acc[0] = (unsigned long long)v;
+    acc[1] = (unsigned long long)((unsigned __int128)v >> 64);
+  }
+}
+
+void launch_dot_fast(const float* a, const float* b, i64 count, const unsigned long long* abits,
+                            const unsigned long long* bbits, unsigned long long* acc, double* part, cudaStream_t s) {
+  k_dot_f32_part<<<kDotBlocks, 256, 0, s>>>(a, b, count, part);
+  k_dot_f32_final<<<1, 256, 0, s>>>(part, kDotBlocks, abits, bbits, acc);
+  count_launch(2);
+}
+
 // FP64 residual with fused multiply-adds, for the outer loop of the mixed
 // form (fewer FP64 operations; that form is not bit-matched to the oracle).
 void launch_residual_fma(const double* phi, const double* rhs, const double* coef, int n, double dx, float* r32,

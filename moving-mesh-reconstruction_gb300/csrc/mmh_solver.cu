@@ -108,7 +108,8 @@ struct mmh_ctx {
   double *baj = nullptr, *cc = nullptr, *vt = nullptr, *u1 = nullptr, *gface = nullptr;
   // spectral
   void *Xc = nullptr, *Z = nullptr;
-  double* spectab = nullptr;  // twiddle and cosine tables of the spectral kernels
+  double* spectab = nullptr;
+  double* dotpart = nullptr;  // block sums of the fast FP32 dot products  // twiddle and cosine tables of the spectral kernels
   cufftHandle pd2z = 0, pz2z = 0;
   bool plans = false;
   Scal* sc = nullptr;   // device
@@ -341,6 +342,17 @@ int precond_replay(mmh_ctx* c, int l0, unsigned long long* zbits) {
 // max|r| <= tol * bn (recurrence residual) or maxit iterations.  The
 // residual lives in H.rhs[l0] (the preconditioner's right-hand side) and the
 // preconditioned residual in H.u[l0].  Dot products are exact (FP64 scalars).
+// Dot product of the PCG in precision T: exact and order-free in FP64 (the
+// oracle's bits), fast and deterministic in FP32 (the mixed inner solve).
+template <class T>
+void pcg_dot(mmh_ctx* c, const T* a, const T* b, i64 n3, const unsigned long long* abits,
+             const unsigned long long* bbits, unsigned long long* acc) {
+  if constexpr (std::is_same<T, float>::value)
+    launch_dot_fast(a, b, n3, abits, bbits, acc, c->dotpart, c->s);
+  else
+    launch_dot<T>(a, b, n3, abits, bbits, acc, c->s);
+}
+
 template <class T>
 int pcg_core(mmh_ctx* c, int l0, double dx, T* x, const T* b, T* p, T* q, double bn, double tol, int maxit,
              int* iters, double* rel_out, double* r0_out) {
@@ -361,13 +373,13 @@ int pcg_core(mmh_ctx* c, int l0, double dx, T* x, const T* b, T* p, T* q, double
     RET(precond_replay<T>(c, l0, &P->zbits));
     CK(cudaMemcpyAsync(p, z, sizeof(T) * n3, cudaMemcpyDeviceToDevice, c->s));
     CK(cudaMemcpyAsync(&P->pbits, &P->zbits, 8, cudaMemcpyDeviceToDevice, c->s));
-    launch_dot<T>(r, z, n3, &P->rbits, &P->zbits, P->acc[0], c->s);
+    pcg_dot<T>(c, r, z, n3, &P->rbits, &P->zbits, P->acc[0]);
     launch_pcg_scalar(P, 0, c->s);
     for (it = 1;; ++it) {
       CK(cudaMemsetAsync(&P->qbits, 0, 8, c->s));
       launch_apply<T>(p, H.coef[l0], n, (T)dx, q, &P->qbits, c->s);
       CK(cudaMemsetAsync(P->acc[1], 0, 16, c->s));
-      launch_dot<T>(p, q, n3, &P->pbits, &P->qbits, P->acc[1], c->s);
+      pcg_dot<T>(c, p, q, n3, &P->pbits, &P->qbits, P->acc[1]);
       launch_pcg_scalar(P, 1, c->s);
       CK(cudaMemsetAsync(&P->rbits, 0, 8, c->s));
       launch_pcg_update<T>(x, r, p, q, n3, &P->alpha, &P->rbits, c->s);
@@ -381,8 +393,8 @@ int pcg_core(mmh_ctx* c, int l0, double dx, T* x, const T* b, T* p, T* q, double
       RET(precond_replay<T>(c, l0, &P->zbits));
       CK(cudaMemsetAsync(P->acc[0], 0, 16, c->s));
       CK(cudaMemsetAsync(P->acc[2], 0, 16, c->s));
-      launch_dot<T>(z, q, n3, &P->zbits, &P->qbits, P->acc[2], c->s);
-      launch_dot<T>(r, z, n3, &P->rbits, &P->zbits, P->acc[0], c->s);
+      pcg_dot<T>(c, z, q, n3, &P->zbits, &P->qbits, P->acc[2]);
+      pcg_dot<T>(c, r, z, n3, &P->rbits, &P->zbits, P->acc[0]);
       launch_pcg_scalar(P, 2, c->s);
       CK(cudaMemsetAsync(&P->pbits, 0, 8, c->s));
       launch_pcg_pupdate<T>(p, z, n3, &P->beta, &P->pbits, c->s);
@@ -985,6 +997,7 @@ int mmh_create(mmh_ctx** out, const mmh_config* cfg) {
       c->u1 = arena + 17 * n3;
     }
   }
+  if (cfg->precision == MMH_MIXED) A(&c->dotpart, kDotBlocks);
   A(&c->sc, 1);
   if (rc == MMH_OK && cudaMallocHost((void**)&c->hsc, sizeof(Scal)) != cudaSuccess) rc = MMH_ERR_NOMEM;
   if (rc == MMH_OK && cudaMemsetAsync(c->sc, 0, sizeof(Scal), c->s) != cudaSuccess) rc = MMH_ERR_CUDA;
