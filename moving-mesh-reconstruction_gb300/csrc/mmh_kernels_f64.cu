@@ -666,8 +666,20 @@ __device__ __forceinline__ double fsign1(double a) { return a >= 0.0 ? 1.0 : -1.
 __device__ __forceinline__ double minmod(double a, double b) {
   const double wslopelim = 1.5, wbee = 1.0;
   double x = fabs(a), y = fabs(b);
-  double lo = ref_min(x, y), hi = ref_max(x, y);
-  double mm = bexp(lo) < 2047 ? ref_min(wslopelim * lo, hi) : ref_min(wslopelim * lo, wbee * hi + (1.0 - wbee) * lo);
+  // Without a NaN operand (an integer test of the bits), fmin/fmax of these
+  // non-negative values equal compare-and-select; with one, the restatement's
+  // compare-and-select decides which value propagates.
+  const unsigned long long inf_bits = 0x7FF0000000000000ull;
+  double lo, hi, mm;
+  if (abs_bits(a) <= inf_bits && abs_bits(b) <= inf_bits) {
+    lo = fmin(x, y);
+    hi = fmax(x, y);
+    mm = bexp(lo) < 2047 ? fmin(wslopelim * lo, hi) : fmin(wslopelim * lo, wbee * hi + (1.0 - wbee) * lo);
+  } else {
+    lo = ref_min(x, y);
+    hi = ref_max(x, y);
+    mm = bexp(lo) < 2047 ? ref_min(wslopelim * lo, hi) : ref_min(wslopelim * lo, wbee * hi + (1.0 - wbee) * lo);
+  }
   if (bexp(mm) < 2046) {
     const bool pa = a >= 0.0, pb = b >= 0.0;
     return pa != pb ? 0.0 : (pa ? mm : -mm);
