@@ -6,6 +6,9 @@
 // restatement and reproduce it bit for bit; the FP32 unit (mixed-precision
 // inner V-cycle) keeps FMA contraction.
 //
+// Divisions by powers of two are written as multiplications by the exact
+// reciprocal: both round the same exact quotient, so the bits are the same.
+//
 // Layout: a(i,j,k) of the Fortran arrays is a[i + n*(j + n*k)] (0-based),
 // periodic in all three directions.  Metric coefficients are 6 planes of n^3
 // (structure of arrays).
@@ -181,9 +184,9 @@ __global__ void k_metric(const T* __restrict__ def, const T* __restrict__ rho, i
   T phixx = (def[IDX(ip, j, k, n)] - T(2) * c + def[IDX(im, j, k, n)]) * di2;
   T phiyy = (def[IDX(i, jp, k, n)] - T(2) * c + def[IDX(i, jm, k, n)]) * di2;
   T phizz = (def[IDX(i, j, kp, n)] - T(2) * c + def[IDX(i, j, km, n)]) * di2;
-  T phixy = (def[IDX(ip, jp, k, n)] - def[IDX(im, jp, k, n)] - def[IDX(ip, jm, k, n)] + def[IDX(im, jm, k, n)]) * di2 / T(4);
-  T phiyz = (def[IDX(i, jp, kp, n)] - def[IDX(i, jp, km, n)] - def[IDX(i, jm, kp, n)] + def[IDX(i, jm, km, n)]) * di2 / T(4);
-  T phixz = (def[IDX(ip, j, kp, n)] - def[IDX(im, j, kp, n)] - def[IDX(ip, j, km, n)] + def[IDX(im, j, km, n)]) * di2 / T(4);
+  T phixy = (def[IDX(ip, jp, k, n)] - def[IDX(im, jp, k, n)] - def[IDX(ip, jm, k, n)] + def[IDX(im, jm, k, n)]) * di2 * T(0.25);
+  T phiyz = (def[IDX(i, jp, kp, n)] - def[IDX(i, jp, km, n)] - def[IDX(i, jm, kp, n)] + def[IDX(i, jm, km, n)]) * di2 * T(0.25);
+  T phixz = (def[IDX(ip, j, kp, n)] - def[IDX(im, j, kp, n)] - def[IDX(ip, j, km, n)] + def[IDX(im, j, km, n)]) * di2 * T(0.25);
   T a11 = T(1) + phixx, a12 = phixy, a13 = phixz, a22 = T(1) + phiyy, a23 = phiyz, a33 = T(1) + phizz;
   T det = a11 * a22 * a33 + T(2) * a12 * a13 * a23 - a13 * a13 * a22 - a11 * (a23 * a23) - a12 * a12 * a33;
   T b11 = (a22 * a33 - a23 * a23);
@@ -231,12 +234,12 @@ struct Stencil {
 // tdiag, t1 (face terms) and t2 (cross terms) in the reference's operand order.
 template <class T>
 __device__ __forceinline__ void op_eval(const Stencil<T>& s, T& tdiag, T& t1, T& t2) {
-  T b11p = (s.f1ip + s.f1c) / T(2);
-  T b11m = (s.f1im + s.f1c) / T(2);
-  T b22p = (s.f4jp + s.f4c) / T(2);
-  T b22m = (s.f4jm + s.f4c) / T(2);
-  T b33p = (s.f6kp + s.f6c) / T(2);
-  T b33m = (s.f6km + s.f6c) / T(2);
+  T b11p = (s.f1ip + s.f1c) * T(0.5);
+  T b11m = (s.f1im + s.f1c) * T(0.5);
+  T b22p = (s.f4jp + s.f4c) * T(0.5);
+  T b22m = (s.f4jm + s.f4c) * T(0.5);
+  T b33p = (s.f6kp + s.f6c) * T(0.5);
+  T b33m = (s.f6km + s.f6c) * T(0.5);
   tdiag = -(b11p + b11m + b22p + b22m + b33p + b33m);
   t1 = (b11p * s.ip + b11m * s.im + b22p * s.jp + b22m * s.jm + b33p * s.kp + b33m * s.km);
   t2 = ((s.ppk - s.mpk) * s.f2jp
@@ -250,7 +253,7 @@ __device__ __forceinline__ void op_eval(const Stencil<T>& s, T& tdiag, T& t1, T&
         + (s.ipkp - s.imkp) * s.f3kp
         - (s.ipkm - s.imkm) * s.f3km
         + (s.ipkp - s.ipkm) * s.f3ip
-        - (s.imkp - s.imkm) * s.f3im) / T(4);
+        - (s.imkp - s.imkm) * s.f3im) * T(0.25);
 }
 
 // Gather the stencil of cell (i,j,k) from global memory.
@@ -687,14 +690,14 @@ __global__ void k_restrict_resid(const T* __restrict__ r, int n, int special, T*
   int jb = 2 * J, jbp = (jb + 1) % n, jbm = (jb + n - 1) % n;
   int kb = 2 * K, kbp = kb + 1, kl = (kb + n - 1) % n;
 #define R_(x, y, z) r[IDX(x, y, z, n)]
-  T lower_a = R_(ib, jb, kl) / T(16);
-  T lower_b = (R_(ibp, jb, kl) + R_(ibm, jb, kl) + R_(ib, jbp, kl) + R_(ib, jbm, kl)) / T(32);
-  T lower_c = (R_(ibp, jbp, kl) + R_(ibp, jbm, kl) + R_(ibm, jbp, kl) + R_(ibm, jbm, kl)) / T(64);
-  T main_a = R_(ib, jb, kb) / T(8);
-  T main_b = (R_(ibp, jb, kb) + R_(ibm, jb, kb) + R_(ib, jbp, kb) + R_(ib, jbm, kb) + R_(ib, jb, kbp)) / T(16);
+  T lower_a = R_(ib, jb, kl) * T(0.0625);
+  T lower_b = (R_(ibp, jb, kl) + R_(ibm, jb, kl) + R_(ib, jbp, kl) + R_(ib, jbm, kl)) * T(0.03125);
+  T lower_c = (R_(ibp, jbp, kl) + R_(ibp, jbm, kl) + R_(ibm, jbp, kl) + R_(ibm, jbm, kl)) * T(0.015625);
+  T main_a = R_(ib, jb, kb) * T(0.125);
+  T main_b = (R_(ibp, jb, kb) + R_(ibm, jb, kb) + R_(ib, jbp, kb) + R_(ib, jbm, kb) + R_(ib, jb, kbp)) * T(0.0625);
   T main_c = (R_(ibp, jbp, kb) + R_(ibp, jbm, kb) + R_(ibm, jbp, kb) + R_(ibm, jbm, kb) + R_(ibp, jb, kbp) +
-              R_(ibm, jb, kbp) + R_(ib, jbp, kbp) + R_(ib, jbm, kbp)) / T(32);
-  T main_d = (R_(ibp, jbp, kbp) + R_(ibp, jbm, kbp) + R_(ibm, jbp, kbp) + R_(ibm, jbm, kbp)) / T(64);
+              R_(ibm, jb, kbp) + R_(ib, jbp, kbp) + R_(ib, jbm, kbp)) * T(0.03125);
+  T main_d = (R_(ibp, jbp, kbp) + R_(ibp, jbm, kbp) + R_(ibm, jbp, kbp) + R_(ibm, jbm, kbp)) * T(0.015625);
 #undef R_
   T acc = T(0);
   if (K == special) {
@@ -713,12 +716,12 @@ template <class T>
 __device__ __forceinline__ T smooth27(const T* __restrict__ a, int n, int i, int j, int k) {
   int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
 #define A_(x, y, z) a[IDX(x, y, z, n)]
-  return A_(i, j, k) / T(8) +
-         (A_(ip, j, k) + A_(im, j, k) + A_(i, jp, k) + A_(i, jm, k) + A_(i, j, kp) + A_(i, j, km)) / T(16) +
+  return A_(i, j, k) * T(0.125) +
+         (A_(ip, j, k) + A_(im, j, k) + A_(i, jp, k) + A_(i, jm, k) + A_(i, j, kp) + A_(i, j, km)) * T(0.0625) +
          (A_(ip, jp, k) + A_(ip, jm, k) + A_(im, jp, k) + A_(im, jm, k) + A_(ip, j, kp) + A_(ip, j, km) +
-          A_(im, j, kp) + A_(im, j, km) + A_(i, jp, kp) + A_(i, jp, km) + A_(i, jm, kp) + A_(i, jm, km)) / T(32) +
+          A_(im, j, kp) + A_(im, j, km) + A_(i, jp, kp) + A_(i, jp, km) + A_(i, jm, kp) + A_(i, jm, km)) * T(0.03125) +
          (A_(ip, jp, kp) + A_(ip, jp, km) + A_(ip, jm, kp) + A_(ip, jm, km) + A_(im, jp, kp) + A_(im, jp, km) +
-          A_(im, jm, kp) + A_(im, jm, km)) / T(64);
+          A_(im, jm, kp) + A_(im, jm, km)) * T(0.015625);
 #undef A_
 }
 
@@ -758,7 +761,7 @@ __global__ void k_prolong_add(T* __restrict__ u, const T* __restrict__ uh, int n
   if (kbh >= nh) kbh = 0;
 #define H_(x, y, z) uh[IDX(x, y, z, nh)]
   u[t] = u[t] + (H_(ibl, jbl, kbl) + H_(ibl, jbl, kbh) + H_(ibl, jbh, kbl) + H_(ibl, jbh, kbh) + H_(ibh, jbh, kbl) +
-                 H_(ibh, jbh, kbh) + H_(ibh, jbl, kbl) + H_(ibh, jbl, kbh)) / T(8);
+                 H_(ibh, jbh, kbh) + H_(ibh, jbl, kbl) + H_(ibh, jbl, kbh)) * T(0.125);
 #undef H_
 }
 
@@ -789,9 +792,9 @@ __global__ void k_det(const T* __restrict__ def, int n, T di2, T* __restrict__ d
   T phixx = (def[IDX(ip, j, k, n)] - T(2) * c + def[IDX(im, j, k, n)]) * di2;
   T phiyy = (def[IDX(i, jp, k, n)] - T(2) * c + def[IDX(i, jm, k, n)]) * di2;
   T phizz = (def[IDX(i, j, kp, n)] - T(2) * c + def[IDX(i, j, km, n)]) * di2;
-  T phixy = (def[IDX(ip, jp, k, n)] - def[IDX(im, jp, k, n)] - def[IDX(ip, jm, k, n)] + def[IDX(im, jm, k, n)]) * di2 / T(4);
-  T phiyz = (def[IDX(i, jp, kp, n)] - def[IDX(i, jp, km, n)] - def[IDX(i, jm, kp, n)] + def[IDX(i, jm, km, n)]) * di2 / T(4);
-  T phixz = (def[IDX(ip, j, kp, n)] - def[IDX(im, j, kp, n)] - def[IDX(ip, j, km, n)] + def[IDX(im, j, km, n)]) * di2 / T(4);
+  T phixy = (def[IDX(ip, jp, k, n)] - def[IDX(im, jp, k, n)] - def[IDX(ip, jm, k, n)] + def[IDX(im, jm, k, n)]) * di2 * T(0.25);
+  T phiyz = (def[IDX(i, jp, kp, n)] - def[IDX(i, jp, km, n)] - def[IDX(i, jm, kp, n)] + def[IDX(i, jm, km, n)]) * di2 * T(0.25);
+  T phixz = (def[IDX(ip, j, kp, n)] - def[IDX(im, j, kp, n)] - def[IDX(ip, j, km, n)] + def[IDX(im, j, km, n)]) * di2 * T(0.25);
   T a11 = T(1) + phixx, a12 = phixy, a13 = phixz, a22 = T(1) + phiyy, a23 = phiyz, a33 = T(1) + phizz;
   det[t] = (a11 * a22 * a33 + T(2) * a12 * a13 * a23 - a13 * a13 * a22 - a11 * (a23 * a23) - a12 * a12 * a33);
 }

@@ -314,15 +314,15 @@ __global__ void __launch_bounds__(256) k_limiter_mask(double* __restrict__ defpl
     double phixx = (P_(ip, j, k) - 2.0 * P_(i, j, k) + P_(im, j, k)) * dtold;
     double phiyy = (P_(i, jp, k) - 2.0 * P_(i, j, k) + P_(i, jm, k)) * dtold;
     double phizz = (P_(i, j, kp) - 2.0 * P_(i, j, k) + P_(i, j, km)) * dtold;
-    double phixy = (P_(ip, jp, k) - P_(im, jp, k) - P_(ip, jm, k) + P_(im, jm, k)) / 4.0 * dtold;
-    double phiyz = (P_(i, jp, kp) - P_(i, jp, km) - P_(i, jm, kp) + P_(i, jm, km)) / 4.0 * dtold;
-    double phixz = (P_(ip, j, kp) - P_(im, j, kp) - P_(ip, j, km) + P_(im, j, km)) / 4.0 * dtold;
+    double phixy = (P_(ip, jp, k) - P_(im, jp, k) - P_(ip, jm, k) + P_(im, jm, k)) * 0.25 * dtold;
+    double phiyz = (P_(i, jp, kp) - P_(i, jp, km) - P_(i, jm, kp) + P_(i, jm, km)) * 0.25 * dtold;
+    double phixz = (P_(ip, j, kp) - P_(im, j, kp) - P_(ip, j, km) + P_(im, j, km)) * 0.25 * dtold;
     phixx = phixx + (D_(ip, j, k) - 2.0 * D_(i, j, k) + D_(im, j, k));
     phiyy = phiyy + (D_(i, jp, k) - 2.0 * D_(i, j, k) + D_(i, jm, k));
     phizz = phizz + (D_(i, j, kp) - 2.0 * D_(i, j, k) + D_(i, j, km));
-    phixy = phixy + (D_(ip, jp, k) - D_(im, jp, k) - D_(ip, jm, k) + D_(im, jm, k)) / 4.0;
-    phiyz = phiyz + (D_(i, jp, kp) - D_(i, jp, km) - D_(i, jm, kp) + D_(i, jm, km)) / 4.0;
-    phixz = phixz + (D_(ip, j, kp) - D_(im, j, kp) - D_(ip, j, km) + D_(im, j, km)) / 4.0;
+    phixy = phixy + (D_(ip, jp, k) - D_(im, jp, k) - D_(ip, jm, k) + D_(im, jm, k)) * 0.25;
+    phiyz = phiyz + (D_(i, jp, kp) - D_(i, jp, km) - D_(i, jm, kp) + D_(i, jm, km)) * 0.25;
+    phixz = phixz + (D_(ip, j, kp) - D_(im, j, kp) - D_(ip, j, km) + D_(im, j, km)) * 0.25;
 #undef P_
 #undef D_
     c[0] = 1.0 + phixx; c[1] = phixy; c[2] = phixz; c[3] = 1.0 + phiyy; c[4] = phiyz; c[5] = 1.0 + phizz;
@@ -536,12 +536,12 @@ __device__ __forceinline__ double ref_max(double a, double b) { return (a < b) ?
 // are computed once here: sd[a] = (u + w_a)/2, sd[3 + a] = (u - w_a)/2.
 __device__ __forceinline__ void store_sd(double* __restrict__ sd, i64 n3, i64 t, double u0, double wx, double wy,
                                          double wz) {
-  sd[0 * n3 + t] = (u0 + wx) / 2.0;
-  sd[1 * n3 + t] = (u0 + wy) / 2.0;
-  sd[2 * n3 + t] = (u0 + wz) / 2.0;
-  sd[3 * n3 + t] = (u0 - wx) / 2.0;
-  sd[4 * n3 + t] = (u0 - wy) / 2.0;
-  sd[5 * n3 + t] = (u0 - wz) / 2.0;
+  sd[0 * n3 + t] = (u0 + wx) * 0.5;
+  sd[1 * n3 + t] = (u0 + wy) * 0.5;
+  sd[2 * n3 + t] = (u0 + wz) * 0.5;
+  sd[3 * n3 + t] = (u0 - wx) * 0.5;
+  sd[4 * n3 + t] = (u0 - wy) * 0.5;
+  sd[5 * n3 + t] = (u0 - wz) * 0.5;
 }
 
 // stage 1: calcbaj + cflkeuler + flux of u at every cell.
@@ -572,7 +572,7 @@ __global__ void k_relax_stage1(const double* __restrict__ rho, const double* __r
   double c;
   // cflkeuler (relaxing.f90:1097-1135)
   {
-    double pdx = (dxp - dxm) / 2.0, pdy = (dyp - dym) / 2.0, pdz = (dzp - dzm) / 2.0;
+    double pdx = (dxp - dxm) * 0.5, pdy = (dyp - dym) * 0.5, pdz = (dzp - dzm) * 0.5;
     double det = m.det;
     double vx = zdiv(u0), vy = vx, vz = vx;
     double v1 = vx - pdx, v2 = vy - pdy, v3 = vz - pdz;
@@ -589,7 +589,7 @@ __global__ void k_relax_stage1(const double* __restrict__ rho, const double* __r
       c = ref_max(ref_max(fabs(vv1), fabs(vv2)), fabs(vv3));
     } else {
       double rhoc = u0 / det;
-      double kin = rhoc * (vx * vx + vy * vy + vz * vz) / 2.0;
+      double kin = rhoc * (vx * vx + vy * vy + vz * vz) * 0.5;
       double edn = zdiv(det) - kin;
       double pressure = (gamma - 1.0) * edn;
       double cs = sqrt(gamma * fabs(pressure / rhoc));
@@ -604,9 +604,9 @@ __global__ void k_relax_stage1(const double* __restrict__ rho, const double* __r
   {
     double rg = m.det;
     double mx = zdiv(rg), my = mx, mz = mx;
-    double pdxg = (dxp - dxm) / 2.0 / rg;
-    double pdyg = (dyp - dym) / 2.0 / rg;
-    double pdzg = (dzp - dzm) / 2.0 / rg;
+    double pdxg = (dxp - dxm) * 0.5 / rg;
+    double pdyg = (dyp - dym) * 0.5 / rg;
+    double pdzg = (dzp - dzm) * 0.5 / rg;
     double b11 = m.b11 * rg, b12 = m.b12 * rg, b13 = m.b13 * rg, b22 = m.b22 * rg, b23 = m.b23 * rg, b33 = m.b33 * rg;
     double vtt1 = mx - u0 * pdxg;
     double vtt2 = my - u0 * pdyg;
@@ -638,9 +638,9 @@ __global__ void k_relax_flux(const double* __restrict__ u1, const double* __rest
   double u0 = u1[t];
   double c = cc[t];
   double mx = zdiv(rg), my = mx, mz = mx;
-  double pdxg = (defp[IDX(ip, j, k, n)] - defp[IDX(im, j, k, n)]) / 2.0 / rg;
-  double pdyg = (defp[IDX(i, jp, k, n)] - defp[IDX(i, jm, k, n)]) / 2.0 / rg;
-  double pdzg = (defp[IDX(i, j, kp, n)] - defp[IDX(i, j, km, n)]) / 2.0 / rg;
+  double pdxg = (defp[IDX(ip, j, k, n)] - defp[IDX(im, j, k, n)]) * 0.5 / rg;
+  double pdyg = (defp[IDX(i, jp, k, n)] - defp[IDX(i, jm, k, n)]) * 0.5 / rg;
+  double pdzg = (defp[IDX(i, j, kp, n)] - defp[IDX(i, j, km, n)]) * 0.5 / rg;
   double b11 = baj[0 * n3 + t] * rg, b12 = baj[1 * n3 + t] * rg, b13 = baj[2 * n3 + t] * rg;
   double b22 = baj[3 * n3 + t] * rg, b23 = baj[4 * n3 + t] * rg, b33 = baj[5 * n3 + t] * rg;
   double vtt1 = mx - u0 * pdxg;
@@ -684,7 +684,7 @@ __device__ __forceinline__ double minmod(double a, double b) {
     const bool pa = a >= 0.0, pb = b >= 0.0;
     return pa != pb ? 0.0 : (pa ? mm : -mm);
   }
-  return (fsign1(a) + fsign1(b)) * mm / 2.0;
+  return (fsign1(a) + fsign1(b)) * mm * 0.5;
 }
 // wphalf (relaxing.f90) from the half sums s = (u+w)/2 at the cells -1, 0, +1
 // and the half differences d = (u-w)/2 at the cells 0, +1, +2 of the face.
@@ -693,10 +693,10 @@ __device__ __forceinline__ double wphalf_sd(double sm, double s0, double sp, dou
   double b = dp;
   double da = sp - a;
   double dam = a - sm;
-  double ap = a + minmod(dam, da) / 2.0;
+  double ap = a + minmod(dam, da) * 0.5;
   double db = dpp - b;
   double dbm = b - d0;
-  double bp = b - minmod(db, dbm) / 2.0;
+  double bp = b - minmod(db, dbm) * 0.5;
   return ap - bp;
 }
 
@@ -720,7 +720,7 @@ __global__ void k_relax_faces(const double* __restrict__ sd, const double* __res
     const double* S = sd;
     const double* D = sd + 3 * n3;
     double fl = wphalf_sd(S[a], S[t], S[b], D[t], D[b], D[d]);
-    g[t] = (cc[b] + c0) / 2.0 * fl;
+    g[t] = (cc[b] + c0) * 0.5 * fl;
   }
   {
     int jm = wm(j, n), jp = wp(j, n), jpp = wp(jp, n);
@@ -728,7 +728,7 @@ __global__ void k_relax_faces(const double* __restrict__ sd, const double* __res
     const double* S = sd + n3;
     const double* D = sd + 4 * n3;
     double fl = wphalf_sd(S[a], S[t], S[b], D[t], D[b], D[d]);
-    g[n3 + t] = (cc[b] + c0) / 2.0 * fl;
+    g[n3 + t] = (cc[b] + c0) * 0.5 * fl;
   }
   {
     int km = wm(k, n), kp = wp(k, n), kpp = wp(kp, n);
@@ -736,7 +736,7 @@ __global__ void k_relax_faces(const double* __restrict__ sd, const double* __res
     const double* S = sd + 2 * n3;
     const double* D = sd + 5 * n3;
     double fl = wphalf_sd(S[a], S[t], S[b], D[t], D[b], D[d]);
-    g[2 * n3 + t] = (cc[b] + c0) / 2.0 * fl;
+    g[2 * n3 + t] = (cc[b] + c0) * 0.5 * fl;
   }
 }
 

@@ -23,9 +23,9 @@ __device__ __forceinline__ LimM lim_metric(const double* __restrict__ def, int n
   m.phixx = (def[IDX(ip, j, k, n)] - 2.0 * c + def[IDX(im, j, k, n)]);
   m.phiyy = (def[IDX(i, jp, k, n)] - 2.0 * c + def[IDX(i, jm, k, n)]);
   m.phizz = (def[IDX(i, j, kp, n)] - 2.0 * c + def[IDX(i, j, km, n)]);
-  m.phixy = (def[IDX(ip, jp, k, n)] - def[IDX(im, jp, k, n)] - def[IDX(ip, jm, k, n)] + def[IDX(im, jm, k, n)]) / 4.0;
-  m.phiyz = (def[IDX(i, jp, kp, n)] - def[IDX(i, jp, km, n)] - def[IDX(i, jm, kp, n)] + def[IDX(i, jm, km, n)]) / 4.0;
-  m.phixz = (def[IDX(ip, j, kp, n)] - def[IDX(im, j, kp, n)] - def[IDX(ip, j, km, n)] + def[IDX(im, j, km, n)]) / 4.0;
+  m.phixy = (def[IDX(ip, jp, k, n)] - def[IDX(im, jp, k, n)] - def[IDX(ip, jm, k, n)] + def[IDX(im, jm, k, n)]) * 0.25;
+  m.phiyz = (def[IDX(i, jp, kp, n)] - def[IDX(i, jp, km, n)] - def[IDX(i, jm, kp, n)] + def[IDX(i, jm, km, n)]) * 0.25;
+  m.phixz = (def[IDX(ip, j, kp, n)] - def[IDX(im, j, kp, n)] - def[IDX(ip, j, km, n)] + def[IDX(im, j, km, n)]) * 0.25;
   double a11 = 1.0 + m.phixx, a12 = m.phixy, a13 = m.phixz, a22 = 1.0 + m.phiyy, a23 = m.phiyz, a33 = 1.0 + m.phizz;
   double det = a11 * a22 * a33 + 2.0 * a12 * a13 * a23 - a13 * a13 * a22 - a11 * (a23 * a23) - a12 * a12 * a33;
   m.det = det;
