@@ -412,17 +412,17 @@ __device__ __forceinline__ double2 spec_mode(double2 x, int kx, int ky, int kz, 
     else kk = (kz + 1 <= n / 2 + 1) ? (double)kz : (double)(kz - n);
     double r2 = re * 0.0 - im * kk;
     double i2 = re * kk + im * 0.0;
-    r2 = r2 / n * 2. * pi;
-    i2 = i2 / n * 2. * pi;
+    r2 = r2 * (1.0 / n) * 2. * pi;  // n is a power of two: exact reciprocal
+    i2 = i2 * (1.0 / n) * 2. * pi;
     return make_double2(r2, i2);
   } else if (mode == 3) {
     // *(k1^2 + k2^2 + k3^2)  (reconstruct.f90:88-110)
     double k3 = (kz + 1 <= n / 2 + 1) ? (double)kz : (double)(kz - n);
-    k3 = k3 / n * 2. * pi;
+    k3 = k3 * (1.0 / n) * 2. * pi;
     double k2 = (ky + 1 <= n / 2 + 1) ? (double)ky : (double)(ky - n);
-    k2 = k2 / n * 2. * pi;
+    k2 = k2 * (1.0 / n) * 2. * pi;
     double k1 = (double)kx;
-    k1 = k1 / n * 2. * pi;
+    k1 = k1 * (1.0 / n) * 2. * pi;
     double f = k1 * k1 + k2 * k2 + k3 * k3;
     return make_double2(re * f, im * f);
   } else {
@@ -494,8 +494,9 @@ __global__ void k_spec_unpack(const double2* __restrict__ z, int n, double* __re
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= tot) return;
   double2 v = z[t];
-  double a = v.x * 2. / n / n / n;
-  double b = v.y * 2. / n / n / n;
+  const double rn = 1.0 / n;  // n is a power of two: exact reciprocal
+  double a = v.x * 2. * rn * rn * rn;
+  double b = v.y * 2. * rn * rn * rn;
   i64 o0 = 2 * t, o1 = 2 * t + 1;
   if (add) {
     out[o0] = out[o0] + a;
