@@ -128,8 +128,9 @@ class ClockSampler:
         smax = [num(r[1]) for r in rows if num(r[1]) is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[q] for r in rows for q in range(4) if r[4 + q].lower() == "active"})
+        pw = [num(r[2]) for r in rows if num(r[2]) is not None]
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "power_w": statistics.median(pw) if pw else None}
 
 
 # ---------------------------------------------------------------------------
@@ -392,7 +393,10 @@ def main():
     gradh = as_np(grad_host, (n, n, n, 3))
     deltah = as_np(delta_host, (n, n, n))
     e2e_ms = None
+    e2e_clk = None
     if args.e2e_steps > 0:
+        e2e_clocks = ClockSampler(local)
+        e2e_clocks.start()
         barrier()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -407,6 +411,7 @@ def main():
         e1.synchronize()
         barrier()
         e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.e2e_steps, dev)
+        e2e_clk = e2e_clocks.stop()
     ctx.close()
 
     # ---- FP64 form ----
@@ -455,7 +460,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "config": workload_config(args),
         "e2e": {"value": (e2e_ms / 1000.0 / world) if e2e_ms else None, "unit": UNIT,
-                "h2d_bytes_per_step": 8 * n3, "d2h_bytes_per_step": 8 * 5 * n3},
+                "h2d_bytes_per_step": 8 * n3, "d2h_bytes_per_step": 8 * 5 * n3, "clocks": e2e_clk},
         "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
         "fp64": fp64, "mixed_vs_fp64_speedup": (fp64["value"] / (ms_mixed / 1000.0)) if fp64 else None,
         "solve": {"vcycles_last": diags[-1]["vcycles"], "resid_rel_last": diags[-1]["resid_rel"],
