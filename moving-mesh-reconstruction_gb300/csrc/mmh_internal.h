@@ -103,4 +103,13 @@ constexpr int kDotBlocks = 152 * 8;
 void launch_dot_fast(const float* a, const float* b, i64 count, const unsigned long long* abits,
                      const unsigned long long* bbits, unsigned long long* acc, double* part, cudaStream_t s);
 
+// calcdefp adjoint pieces (mmh_adjoint.cu)
+void launch_adj_pass1(double* y, const double* t, const uint8_t* maskx, const uint8_t* maskc, double dtaumesh,
+                      i64 n3, cudaStream_t s);
+void launch_adj_rhs(double* y, const double* rho, double dtold, i64 n3, cudaStream_t s);
+void launch_adj_contract(const double* lam, const double* u, const double* cf, int n, double* out, cudaStream_t s);
+void launch_box27(const double* in, int n, double* out, cudaStream_t s);
+void launch_adj_mul(const double* a, const double* b, double* out, i64 n3, cudaStream_t s);
+void launch_adj_sub(const double* a, const double* b, double* out, i64 n3, cudaStream_t s);
+
 }  // namespace mmh

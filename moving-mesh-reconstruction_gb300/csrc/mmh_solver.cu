@@ -648,6 +648,93 @@ int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t
   return st;
 }
 
+// Device scratch of one call, released on the context's stream at scope exit.
+struct DevTemp {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  ~DevTemp() {
+    if (p) cudaFreeAsync(p, s);
+  }
+};
+
+// Gradient of J = w^T defp with respect to the density for one calcdefp
+// increment on the resident def and rho (no counterpart in the reference).
+// def is held fixed and the limiter's branch choices are those of this
+// forward pass; calls whose final compression test limits a cell return
+// MMH_ERR_UNSUPPORTED (that correction is not transposed).  w (device, n^3)
+// is overwritten; grho (device, n^3) receives the gradient.  defp is defined
+// up to a constant, so the gradient is that of w minus its mean.
+int calcdefp_adjoint_dev(mmh_ctx* c, double dtold, double dtaumesh, double* w, double* grho, mmh_diag* d) {
+  if (c->cfg.schedule == MMH_SCHED_REF) return MMH_ERR_UNSUPPORTED;  // one V-cycle is no solve
+  int n = c->n;
+  i64 n3 = c->n3;
+  if (dtold < 1.e-8) dtold = 1.0;
+  DevTemp buf;
+  buf.s = c->s;
+  if (cudaMallocAsync(&buf.p, sizeof(double) * 9 * n3 + 2 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
+  double* pre = (double*)buf.p;  // pass-1 input S^3 g
+  double* uf = pre + n3;         // forward solution before the last two smoothings
+  double* y = uf + n3;
+  double* cf = y + n3;  // C_f = cof/det, 6 n^3
+  uint8_t* mk = (uint8_t*)(cf + 6 * n3);
+  double* tmp = c->tmp();
+  double* defp = c->defp();
+  // forward pass (calcdefp_dev), keeping the pass-1 input, masks and solution
+  launch_calcdefp_rhs(tmp, c->rho, n, dtold, c->s);
+  launch_smooth27<double>(tmp, n, c->scr, c->s);
+  launch_smooth27<double>(c->scr, n, tmp, c->s);
+  launch_smooth27<double>(tmp, n, c->scr, c->s);
+  CK(cudaMemcpyAsync(pre, c->scr, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  launch_lim_reset(&c->sc->lim, c->s);
+  launch_limiter_pass1(c->scr, c->def, c->rho, n, dtold, dtaumesh, &c->sc->lim, mk, mk + n3, c->s);
+  launch_smooth27<double>(c->scr, n, tmp, c->s);
+  launch_fill<double>(defp, n3, 0.0, c->s);
+  int st = multigrid_level(c, 0, 1.0, d);
+  if (st != MMH_OK) return st;
+  CK(cudaMemcpyAsync(uf, defp, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  launch_smooth27<double>(defp, n, c->scr, c->s);
+  launch_smooth27<double>(c->scr, n, defp, c->s);
+  launch_limiter_mask(c->defplim, c->def, defp, n, dtold, &c->sc->lim, nullptr, c->s);
+  RET(pull_scal(c));
+  lim_to_diag(c->hsc->lim, d);
+  if (c->hsc->lim.ncompress) return MMH_ERR_UNSUPPORTED;
+  // adjoint solve L lam = S^2 w - mean (L symmetric)
+  launch_smooth27<double>(w, n, c->scr, c->s);
+  launch_smooth27<double>(c->scr, n, tmp, c->s);
+  RET(zerosum<double>(c, tmp, n3));
+  launch_fill<double>(defp, n3, 0.0, c->s);
+  mmh_diag da{};
+  st = multigrid_level(c, 0, 1.0, &da);
+  if (st != MMH_OK) return st;
+  const double* lam = defp;
+  // right-hand-side path: g' . S^3 (D . S (P^T lam)),
+  // P^T lam = lam - (det^T lam) / sum det
+  launch_det<double>(c->def, n, 1.0, c->det, c->s);
+  launch_adj_mul(c->det, lam, y, n3, c->s);
+  CK(cudaMemsetAsync(c->sc->acc[0], 0, 32, c->s));
+  launch_fxsum<double>(c->det, n3, c->sc->acc[0], &c->sc->bad, c->s);
+  launch_fxsum<double>(y, n3, c->sc->acc[1], &c->sc->bad, c->s);
+  launch_fx_ratio(c->sc->acc[1], c->sc->acc[0], &c->sc->ratio, c->s);
+  CK(cudaMemcpyAsync(y, lam, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  launch_sub_mean<double>(y, n3, &c->sc->ratio, c->s);
+  launch_smooth27<double>(y, n, c->scr, c->s);
+  launch_adj_pass1(c->scr, pre, mk, mk + n3, dtaumesh, n3, c->s);
+  launch_smooth27<double>(c->scr, n, y, c->s);
+  launch_smooth27<double>(y, n, c->scr, c->s);
+  launch_smooth27<double>(c->scr, n, y, c->s);
+  launch_adj_rhs(y, c->rho, dtold, n3, c->s);
+  // operator path: - B27( sum_f C_f G_f(lam, u) ), C_f from the metric of a unit density
+  launch_fill<double>(pre, n3, 1.0, c->s);
+  launch_metric<double>(c->def, pre, n, 1.0, cf, c->s);
+  launch_adj_contract(lam, uf, cf, n, c->scr, c->s);
+  launch_box27(c->scr, n, pre, c->s);
+  launch_adj_sub(y, pre, grho, n3, c->s);
+  RET(pull_scal(c));
+  if (c->hsc->bad) return MMH_ERR_RANGE;
+  if (d) d->vcycles += da.vcycles;
+  return MMH_OK;
+}
+
 // relaxing(u, def, defp, cmax, dt, 5) on the resident density.
 int relaxing_dev(mmh_ctx* c, double dt) {
   int n = c->n;
@@ -1031,6 +1118,24 @@ int mmh_calcdefp(mmh_ctx* c, float* defp, float* tmp, float* tmp2, const float* 
 int mmh_calcdefp_f64(mmh_ctx* c, double* defp, double* tmp, double* tmp2, const double* def, const double* u,
                      double dtold1, double dtaumesh, int nfluid, mmh_diag* d) {
   return calcdefp_host<double>(c, defp, tmp, tmp2, def, u, dtold1, dtaumesh, nfluid, d);
+}
+int mmh_calcdefp_adjoint_f64(mmh_ctx* c, const double* def, const double* u, int nfluid, double dtold1,
+                             double dtaumesh, const double* w, double* grho, mmh_diag* d) {
+  if (!c || !def || !u || !w || !grho) return MMH_ERR_ARG;
+  i64 n3 = c->n3;
+  RET(upload(c, def, c->def, n3));
+  RET(upload_density(c, u, nfluid, n3, c->rho));
+  DevTemp buf;
+  buf.s = c->s;
+  if (cudaMallocAsync(&buf.p, sizeof(double) * 2 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
+  double* dw = (double*)buf.p;
+  RET(upload(c, w, dw, n3));
+  mmh_diag dd{};
+  int st = calcdefp_adjoint_dev(c, dtold1, dtaumesh, dw, dw + n3, &dd);
+  dd.status = st;
+  if (d) *d = dd;
+  RET(st);
+  return download(c, dw + n3, grho, n3);
 }
 int mmh_multigrid(mmh_ctx* c, float* u, float* rhs, const float* defpot, const float* ubig, float dx, int nx, int ny,
                   int nz, int nu, int nred, int iopt, mmh_diag* d) {

@@ -28,6 +28,7 @@ MMH_SCHED_VCYCLE = 2   # plain repeated V-cycles
 
 MMH_OK = 0
 MMH_ERR_DIVERGED = -6
+MMH_ERR_UNSUPPORTED = -7
 
 # every entry point of include/mmh.h
 EXPORTS = (
@@ -38,7 +39,7 @@ EXPORTS = (
     "mmh_rgzerosum_f64", "mmh_nsmooth_f64", "mmh_limiter_pass1_f64", "mmh_limiter_mask_f64",
     "mmh_limiter_poisson_f64", "mmh_load_f64", "mmh_load_dev", "mmh_iterate", "mmh_store_f64",
     "mmh_outputs_f64", "mmh_outputs_dev", "mmh_state_dev", "mmh_profile_start", "mmh_profile_stop",
-    "mmh_relax_noalloc_f64", "mmh_batch_run",
+    "mmh_relax_noalloc_f64", "mmh_batch_run", "mmh_calcdefp_adjoint_f64",
 )
 
 # kernel kinds for the timing hooks
@@ -194,6 +195,18 @@ class Context:
                 int(nfluid), C.byref(d))
         _chk(rc, "calcdefp", allow_diverged=True)
         return d.as_dict()
+
+    def calcdefp_adjoint(self, defpot, u, w, dtold1=1.0, dtaumesh=1.0, nfluid=5):
+        """Gradient of sum(w * defp) with respect to the density for the defp
+        that calcdefp(..., defpot, u, dtold1, dtaumesh, nfluid) computes, with
+        defpot fixed and the limiter branches frozen.  Returns (grho, diag)."""
+        for a in (defpot, u, w):
+            _farr(a, np.float64)
+        grho = np.zeros(defpot.shape, dtype=np.float64, order="F")
+        d = Diag()
+        _chk(lib().mmh_calcdefp_adjoint_f64(self._h, _p(defpot), _p(u), int(nfluid), C.c_double(dtold1),
+                                            C.c_double(dtaumesh), _p(w), _p(grho), C.byref(d)), "calcdefp_adjoint")
+        return grho, d.as_dict()
 
     def multigrid(self, u, rhs, defpot, ubig, dx, nx, ny, nz, nu, nred=1, iopt=2):
         """multigrid(u,rhs,defpot,ubig,dx,nx,ny,nz,nu,nred,iopt)  (mmh/multigrid.f90:16)."""

@@ -1,0 +1,111 @@
+"""calcdefp adjoint (no counterpart in the reference): the density gradient of
+J = sum(w * defp) from mmh_calcdefp_adjoint_f64 against central finite
+differences of J through mmh_calcdefp_f64 on the same inputs.
+
+The limiter's branch choices are frozen in the adjoint, so each case checks,
+on the CPU, that the finite-difference steps stay clear of every branch edge
+(the +-1/dtaumesh flux clamps, the density clip at |1 - rho| = 2); the
+expansion and compression masks depend on def alone."""
+import numpy as np
+import pytest
+
+from conftest import smooth_field
+
+
+def _s3(a):
+    """The 27-point smoother (mmh/limiter.f90:677-781): [1,2,1]/4 along each axis."""
+    for ax in range(3):
+        a = 0.25 * np.roll(a, 1, ax) + 0.5 * a + 0.25 * np.roll(a, -1, ax)
+    return a
+
+
+def _max_hessian(g):
+    d2 = [np.roll(g, 1, ax) - 2 * g + np.roll(g, -1, ax) for ax in range(3)]
+    return max(np.abs(x).max() for x in d2)
+
+
+def _bump(n, kappa, width):
+    """-A exp(-r^2 / 2 width^2) at the box centre: centre curvature kappa (an
+    expanding region, det > 10 for kappa > 1.16), rim curvature >= -0.45 kappa."""
+    x = np.arange(n) - n / 2
+    r2 = x[:, None, None] ** 2 + x[None, :, None] ** 2 + x[None, None, :] ** 2
+    return np.asfortranarray(-kappa * width * width * np.exp(-r2 / (2.0 * width * width)))
+
+
+def _gap_threshold(t, lo=0.55, hi=0.85):
+    """A flux-clamp level 1/dtaumesh in the widest gap of sorted |t| between
+    quantiles lo and hi (some cells clamped, none near the edge)."""
+    s = np.sort(np.abs(t).ravel())
+    a, b = int(lo * s.size), int(hi * s.size)
+    q = a + int(np.argmax(np.diff(s[a:b])))
+    return 0.5 * (s[q] + s[q + 1]), 0.5 * (s[q + 1] - s[q])
+
+
+CASES = {
+    # 16^3, gentle def, clamps and the density clip active
+    "clamps": dict(n=16, sigma=0.6, seed=31, kind="smooth", clamp=True),
+    # 32^3, an expanding bump: expansion mask active, strongly curved metric
+    "expansion": dict(n=32, sigma=0.4, seed=57, kind="bump", clamp=False),
+}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_calcdefp_adjoint_matches_finite_differences(mmh, fields, case):
+    p = CASES[case]
+    n, dtold = p["n"], 0.5
+    rho = fields.lognormal_density(n, sigma=p["sigma"], seed=p["seed"])
+    if p["kind"] == "bump":
+        defpot = _bump(n, kappa=1.3, width=3.0)
+    else:
+        g = smooth_field(n, 1.0, p["seed"] + 1)
+        defpot = np.asfortranarray(g * (0.3 / _max_hessian(g)))
+    rng = np.random.default_rng(p["seed"] + 2)
+    w = _s3(rng.standard_normal((n, n, n)))
+    w = np.asfortranarray(w - w.mean())
+    dirs = [np.asfortranarray(_s3(rng.standard_normal((n, n, n)))) for _ in range(2)]
+    h = 1e-4
+
+    # pass-1 input S^3 g (limiter.f90:153-166) and the branch edges
+    t = _s3(_s3(_s3(np.clip(1.0 - rho, -2.0, 2.0) / 30.0 / dtold)))
+    dt_max = max(h * np.abs(_s3(_s3(_s3(v)))).max() / 30.0 / dtold for v in dirs)
+    if p["clamp"]:
+        level, margin = _gap_threshold(t)
+        assert margin > 20 * dt_max, (margin, dt_max)
+        dtaumesh = 1.0 / level
+        assert (np.abs(t) > level).sum() > 0
+    else:
+        dtaumesh = 1e-6
+    edge = np.abs(np.abs(1.0 - rho) - 2.0).min()
+    assert edge > 20 * h * max(np.abs(v).max() for v in dirs)
+    if p["clamp"]:
+        assert (np.abs(1.0 - rho) > 2.0).sum() > 0  # the clip is exercised
+
+    with mmh.Context(n, precision=mmh.MMH_FP64, schedule=mmh.MMH_SCHED_TOL, tol=1e-13, max_cycles=400) as ctx:
+        grho, d = ctx.calcdefp_adjoint(defpot, rho, w, dtold, dtaumesh, nfluid=1)
+        assert d["ncompress"] == 0
+        if p["kind"] == "bump":
+            assert d["nexpand"] > 0
+
+        def J(r):
+            defp = np.zeros((n, n, n), order="F")
+            ctx.calcdefp(defp, None, None, defpot, np.asfortranarray(r), dtold, dtaumesh, nfluid=1)
+            return float(np.sum(w * defp))
+
+        for v in dirs:
+            fd = (J(rho + h * v) - J(rho - h * v)) / (2 * h)
+            ad = float(np.sum(grho * v))
+            scale = float(np.sum(np.abs(grho * v)))
+            print(f"{case}: fd {fd:.12e} adjoint {ad:.12e} rel {abs(fd - ad) / abs(ad):.2e}")
+            assert abs(fd - ad) <= 2e-6 * max(abs(ad), 1e-3 * scale), (fd, ad)
+
+
+@pytest.mark.gpu
+def test_calcdefp_adjoint_needs_a_solving_schedule(mmh, fields):
+    n = 16
+    rho = fields.lognormal_density(n, sigma=0.5, seed=3)
+    z = np.zeros((n, n, n), order="F")
+    with mmh.Context(n, precision=mmh.MMH_FP64, schedule=mmh.MMH_SCHED_REF) as ctx:
+        with pytest.raises(mmh.MMHError) as e:
+            ctx.calcdefp_adjoint(z, rho, z, 1.0, 1.0, nfluid=1)
+        assert e.value.code == mmh.MMH_ERR_UNSUPPORTED
