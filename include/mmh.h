@@ -206,17 +206,18 @@ int mmh_relax_noalloc_f64(const double* d_deformpot, const double* d_rho, double
                           double dx, int n, int nrelax, int iopt, double* rinf, void* stream);
 
 /* ---- calcdefp adjoint (no counterpart in the reference) ----------------- */
-/* grho(n,n,n) = dJ/d rho for J = sum w*defp, defp the increment that
- * mmh_calcdefp_f64 computes from the same def and u (u(2:nfluid) == 0):
- * def held fixed, the limiter's branch choices (expansion and compression
- * masks, flux clamps, the density clip) frozen where this forward pass took
- * them.  defp is defined up to a constant, so w counts through its deviation
- * from its mean.  Needs a solving schedule (MMH_SCHED_TOL or
- * MMH_SCHED_VCYCLE; MMH_SCHED_REF gives MMH_ERR_UNSUPPORTED), and returns
- * MMH_ERR_UNSUPPORTED when the final compression test limits a cell.  The
- * diag is that of the forward pass; vcycles adds the adjoint solve's. */
+/* grho(n,n,n) = dJ/d rho and gdef(n,n,n) = dJ/d def (either may be NULL) for
+ * J = sum w*defp, defp the increment that mmh_calcdefp_f64 computes from the
+ * same def and u (u(2:nfluid) == 0), with the limiter's branch choices
+ * (expansion and compression masks, flux clamps, the density clip, the
+ * metric's tangle fallback) frozen where this forward pass took them.  defp
+ * is defined up to a constant, so w counts through its deviation from its
+ * mean.  Needs a solving schedule (MMH_SCHED_TOL or MMH_SCHED_VCYCLE;
+ * MMH_SCHED_REF gives MMH_ERR_UNSUPPORTED), and returns MMH_ERR_UNSUPPORTED
+ * when the final compression test limits a cell.  The diag is that of the
+ * forward pass; vcycles adds the adjoint solve's. */
 int mmh_calcdefp_adjoint_f64(mmh_ctx* ctx, const double* def, const double* u, int nfluid, double dtold1,
-                             double dtaumesh, const double* w, double* grho, mmh_diag* diag);
+                             double dtaumesh, const double* w, double* grho, double* gdef, mmh_diag* diag);
 
 /* ---- kernel timing (no counterpart in the reference) -------------------- */
 /* Arm CUDA-event timing of one kernel kind (MMH_K_* | MMH_K_F32 for the FP32

@@ -111,5 +111,8 @@ void launch_adj_contract(const double* lam, const double* u, const double* cf, i
 void launch_box27(const double* in, int n, double* out, cudaStream_t s);
 void launch_adj_mul(const double* a, const double* b, double* out, i64 n3, cudaStream_t s);
 void launch_adj_sub(const double* a, const double* b, double* out, i64 n3, cudaStream_t s);
+void launch_adj_metric(const double* def, const double* lam, const double* u, const double* urg, const double* y,
+                       const double* rptr, int n, double* abar, cudaStream_t s);
+void launch_adj_hess(const double* abar, int n, double* out, int add, cudaStream_t s);
 
 }  // namespace mmh

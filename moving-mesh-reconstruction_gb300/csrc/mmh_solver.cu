@@ -657,26 +657,29 @@ struct DevTemp {
   }
 };
 
-// Gradient of J = w^T defp with respect to the density for one calcdefp
-// increment on the resident def and rho (no counterpart in the reference).
-// def is held fixed and the limiter's branch choices are those of this
-// forward pass; calls whose final compression test limits a cell return
+// Gradients of J = w^T defp with respect to the density and to def for one
+// calcdefp increment on the resident def and rho (no counterpart in the
+// reference).  The limiter's branch choices are those of this forward pass;
+// calls whose final compression test limits a cell return
 // MMH_ERR_UNSUPPORTED (that correction is not transposed).  w (device, n^3)
-// is overwritten; grho (device, n^3) receives the gradient.  defp is defined
-// up to a constant, so the gradient is that of w minus its mean.
-int calcdefp_adjoint_dev(mmh_ctx* c, double dtold, double dtaumesh, double* w, double* grho, mmh_diag* d) {
+// is overwritten; grho and gdef (device, n^3, either may be null) receive the
+// gradients.  defp is defined up to a constant, so the gradients are those of
+// w minus its mean.
+int calcdefp_adjoint_dev(mmh_ctx* c, double dtold, double dtaumesh, double* w, double* grho, double* gdef,
+                         mmh_diag* d) {
   if (c->cfg.schedule == MMH_SCHED_REF) return MMH_ERR_UNSUPPORTED;  // one V-cycle is no solve
   int n = c->n;
   i64 n3 = c->n3;
   if (dtold < 1.e-8) dtold = 1.0;
   DevTemp buf;
   buf.s = c->s;
-  if (cudaMallocAsync(&buf.p, sizeof(double) * 9 * n3 + 2 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
+  if (cudaMallocAsync(&buf.p, sizeof(double) * (9 * n3 + 1) + 2 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
   double* pre = (double*)buf.p;  // pass-1 input S^3 g
   double* uf = pre + n3;         // forward solution before the last two smoothings
   double* y = uf + n3;
-  double* cf = y + n3;  // C_f = cof/det, 6 n^3
-  uint8_t* mk = (uint8_t*)(cf + 6 * n3);
+  double* cf = y + n3;           // C_f = cof/det, or the adjoint of A = I + Hess(def); 6 n^3
+  double* rslot = cf + 6 * n3;   // the forward rgzerosum ratio sum(b) / sum(det)
+  uint8_t* mk = (uint8_t*)(rslot + 1);
   double* tmp = c->tmp();
   double* defp = c->defp();
   // forward pass (calcdefp_dev), keeping the pass-1 input, masks and solution
@@ -691,6 +694,7 @@ int calcdefp_adjoint_dev(mmh_ctx* c, double dtold, double dtaumesh, double* w, d
   launch_fill<double>(defp, n3, 0.0, c->s);
   int st = multigrid_level(c, 0, 1.0, d);
   if (st != MMH_OK) return st;
+  CK(cudaMemcpyAsync(rslot, &c->sc->ratio, sizeof(double), cudaMemcpyDeviceToDevice, c->s));
   CK(cudaMemcpyAsync(uf, defp, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
   launch_smooth27<double>(defp, n, c->scr, c->s);
   launch_smooth27<double>(c->scr, n, defp, c->s);
@@ -707,8 +711,7 @@ int calcdefp_adjoint_dev(mmh_ctx* c, double dtold, double dtaumesh, double* w, d
   st = multigrid_level(c, 0, 1.0, &da);
   if (st != MMH_OK) return st;
   const double* lam = defp;
-  // right-hand-side path: g' . S^3 (D . S (P^T lam)),
-  // P^T lam = lam - (det^T lam) / sum det
+  // y = P^T lam = lam - (det^T lam) / sum det
   launch_det<double>(c->def, n, 1.0, c->det, c->s);
   launch_adj_mul(c->det, lam, y, n3, c->s);
   CK(cudaMemsetAsync(c->sc->acc[0], 0, 32, c->s));
@@ -717,18 +720,27 @@ int calcdefp_adjoint_dev(mmh_ctx* c, double dtold, double dtaumesh, double* w, d
   launch_fx_ratio(c->sc->acc[1], c->sc->acc[0], &c->sc->ratio, c->s);
   CK(cudaMemcpyAsync(y, lam, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
   launch_sub_mean<double>(y, n3, &c->sc->ratio, c->s);
-  launch_smooth27<double>(y, n, c->scr, c->s);
-  launch_adj_pass1(c->scr, pre, mk, mk + n3, dtaumesh, n3, c->s);
-  launch_smooth27<double>(c->scr, n, y, c->s);
-  launch_smooth27<double>(y, n, c->scr, c->s);
-  launch_smooth27<double>(c->scr, n, y, c->s);
-  launch_adj_rhs(y, c->rho, dtold, n3, c->s);
-  // operator path: - B27( sum_f C_f G_f(lam, u) ), C_f from the metric of a unit density
-  launch_fill<double>(pre, n3, 1.0, c->s);
-  launch_metric<double>(c->def, pre, n, 1.0, cf, c->s);
-  launch_adj_contract(lam, uf, cf, n, c->scr, c->s);
-  launch_box27(c->scr, n, pre, c->s);
-  launch_adj_sub(y, pre, grho, n3, c->s);
+  if (gdef) {
+    // def enters through C_f(A) and the rgzerosum weights det(A), A = I + Hess(def)
+    launch_box27(c->rho, n, c->scr, c->s);
+    launch_adj_metric(c->def, lam, uf, c->scr, y, rslot, n, cf, c->s);
+    launch_adj_hess(cf, n, gdef, 0, c->s);
+  }
+  if (grho) {
+    // right-hand-side path: g' . S^3 (D . S y)
+    launch_smooth27<double>(y, n, c->scr, c->s);
+    launch_adj_pass1(c->scr, pre, mk, mk + n3, dtaumesh, n3, c->s);
+    launch_smooth27<double>(c->scr, n, y, c->s);
+    launch_smooth27<double>(y, n, c->scr, c->s);
+    launch_smooth27<double>(c->scr, n, y, c->s);
+    launch_adj_rhs(y, c->rho, dtold, n3, c->s);
+    // operator path: - B27( sum_f C_f G_f(lam, u) ), C_f from the metric of a unit density
+    launch_fill<double>(pre, n3, 1.0, c->s);
+    launch_metric<double>(c->def, pre, n, 1.0, cf, c->s);
+    launch_adj_contract(lam, uf, cf, n, c->scr, c->s);
+    launch_box27(c->scr, n, pre, c->s);
+    launch_adj_sub(y, pre, grho, n3, c->s);
+  }
   RET(pull_scal(c));
   if (c->hsc->bad) return MMH_ERR_RANGE;
   if (d) d->vcycles += da.vcycles;
@@ -1120,22 +1132,24 @@ int mmh_calcdefp_f64(mmh_ctx* c, double* defp, double* tmp, double* tmp2, const 
   return calcdefp_host<double>(c, defp, tmp, tmp2, def, u, dtold1, dtaumesh, nfluid, d);
 }
 int mmh_calcdefp_adjoint_f64(mmh_ctx* c, const double* def, const double* u, int nfluid, double dtold1,
-                             double dtaumesh, const double* w, double* grho, mmh_diag* d) {
-  if (!c || !def || !u || !w || !grho) return MMH_ERR_ARG;
+                             double dtaumesh, const double* w, double* grho, double* gdef, mmh_diag* d) {
+  if (!c || !def || !u || !w || (!grho && !gdef)) return MMH_ERR_ARG;
   i64 n3 = c->n3;
   RET(upload(c, def, c->def, n3));
   RET(upload_density(c, u, nfluid, n3, c->rho));
   DevTemp buf;
   buf.s = c->s;
-  if (cudaMallocAsync(&buf.p, sizeof(double) * 2 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
+  if (cudaMallocAsync(&buf.p, sizeof(double) * 3 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
   double* dw = (double*)buf.p;
   RET(upload(c, w, dw, n3));
   mmh_diag dd{};
-  int st = calcdefp_adjoint_dev(c, dtold1, dtaumesh, dw, dw + n3, &dd);
+  int st = calcdefp_adjoint_dev(c, dtold1, dtaumesh, dw, grho ? dw + n3 : nullptr, gdef ? dw + 2 * n3 : nullptr, &dd);
   dd.status = st;
   if (d) *d = dd;
   RET(st);
-  return download(c, dw + n3, grho, n3);
+  if (grho) RET(download(c, dw + n3, grho, n3));
+  if (gdef) RET(download(c, dw + 2 * n3, gdef, n3));
+  return MMH_OK;
 }
 int mmh_multigrid(mmh_ctx* c, float* u, float* rhs, const float* defpot, const float* ubig, float dx, int nx, int ny,
                   int nz, int nu, int nred, int iopt, mmh_diag* d) {

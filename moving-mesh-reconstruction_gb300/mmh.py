@@ -197,16 +197,18 @@ class Context:
         return d.as_dict()
 
     def calcdefp_adjoint(self, defpot, u, w, dtold1=1.0, dtaumesh=1.0, nfluid=5):
-        """Gradient of sum(w * defp) with respect to the density for the defp
-        that calcdefp(..., defpot, u, dtold1, dtaumesh, nfluid) computes, with
-        defpot fixed and the limiter branches frozen.  Returns (grho, diag)."""
+        """Gradients of sum(w * defp) with respect to the density and to defpot
+        for the defp that calcdefp(..., defpot, u, dtold1, dtaumesh, nfluid)
+        computes, with the limiter branches frozen.  Returns (grho, gdef, diag)."""
         for a in (defpot, u, w):
             _farr(a, np.float64)
         grho = np.zeros(defpot.shape, dtype=np.float64, order="F")
+        gdef = np.zeros(defpot.shape, dtype=np.float64, order="F")
         d = Diag()
         _chk(lib().mmh_calcdefp_adjoint_f64(self._h, _p(defpot), _p(u), int(nfluid), C.c_double(dtold1),
-                                            C.c_double(dtaumesh), _p(w), _p(grho), C.byref(d)), "calcdefp_adjoint")
-        return grho, d.as_dict()
+                                            C.c_double(dtaumesh), _p(w), _p(grho), _p(gdef), C.byref(d)),
+             "calcdefp_adjoint")
+        return grho, gdef, d.as_dict()
 
     def multigrid(self, u, rhs, defpot, ubig, dx, nx, ny, nz, nu, nred=1, iopt=2):
         """multigrid(u,rhs,defpot,ubig,dx,nx,ny,nz,nu,nred,iopt)  (mmh/multigrid.f90:16)."""

@@ -1,11 +1,11 @@
-"""calcdefp adjoint (no counterpart in the reference): the density gradient of
-J = sum(w * defp) from mmh_calcdefp_adjoint_f64 against central finite
-differences of J through mmh_calcdefp_f64 on the same inputs.
+"""calcdefp adjoint (no counterpart in the reference): the density and def
+gradients of J = sum(w * defp) from mmh_calcdefp_adjoint_f64 against central
+finite differences of J through mmh_calcdefp_f64 on the same inputs.
 
 The limiter's branch choices are frozen in the adjoint, so each case checks,
-on the CPU, that the finite-difference steps stay clear of every branch edge
-(the +-1/dtaumesh flux clamps, the density clip at |1 - rho| = 2); the
-expansion and compression masks depend on def alone."""
+on the CPU, that the finite-difference steps stay clear of every branch edge:
+the +-1/dtaumesh flux clamps and the density clip at |1 - rho| = 2 (density
+steps), the expansion mask det > 10 (def steps)."""
 import numpy as np
 import pytest
 
@@ -22,6 +22,20 @@ def _s3(a):
 def _max_hessian(g):
     d2 = [np.roll(g, 1, ax) - 2 * g + np.roll(g, -1, ax) for ax in range(3)]
     return max(np.abs(x).max() for x in d2)
+
+
+def _det(d):
+    """det(I + Hess(def)) as the metric computes it (gauss1.f90:1107-1210)."""
+    r = np.roll
+    a11 = 1 + r(d, -1, 0) - 2 * d + r(d, 1, 0)
+    a22 = 1 + r(d, -1, 1) - 2 * d + r(d, 1, 1)
+    a33 = 1 + r(d, -1, 2) - 2 * d + r(d, 1, 2)
+
+    def cross(p, q):
+        return 0.25 * (r(r(d, -1, p), -1, q) - r(r(d, 1, p), -1, q) - r(r(d, -1, p), 1, q) + r(r(d, 1, p), 1, q))
+
+    a12, a23, a13 = cross(0, 1), cross(1, 2), cross(0, 2)
+    return a11 * a22 * a33 + 2 * a12 * a13 * a23 - a13 * a13 * a22 - a11 * a23 * a23 - a12 * a12 * a33
 
 
 def _bump(n, kappa, width):
@@ -64,6 +78,10 @@ def test_calcdefp_adjoint_matches_finite_differences(mmh, fields, case):
     w = _s3(rng.standard_normal((n, n, n)))
     w = np.asfortranarray(w - w.mean())
     dirs = [np.asfortranarray(_s3(rng.standard_normal((n, n, n)))) for _ in range(2)]
+    ddirs = []
+    for q in range(2):
+        v = smooth_field(n, 1.0, p["seed"] + 10 + q)
+        ddirs.append(np.asfortranarray(v / _max_hessian(v)))
     h = 1e-4
 
     # pass-1 input S^3 g (limiter.f90:153-166) and the branch edges
@@ -80,24 +98,32 @@ def test_calcdefp_adjoint_matches_finite_differences(mmh, fields, case):
     assert edge > 20 * h * max(np.abs(v).max() for v in dirs)
     if p["clamp"]:
         assert (np.abs(1.0 - rho) > 2.0).sum() > 0  # the clip is exercised
+    det = _det(defpot)
+    for v in ddirs:
+        for sgn in (-1, 1):
+            assert np.array_equal(det > 10.0, _det(defpot + sgn * 20 * h * v) > 10.0)
 
     with mmh.Context(n, precision=mmh.MMH_FP64, schedule=mmh.MMH_SCHED_TOL, tol=1e-13, max_cycles=400) as ctx:
-        grho, d = ctx.calcdefp_adjoint(defpot, rho, w, dtold, dtaumesh, nfluid=1)
+        grho, gdef, d = ctx.calcdefp_adjoint(defpot, rho, w, dtold, dtaumesh, nfluid=1)
         assert d["ncompress"] == 0
         if p["kind"] == "bump":
             assert d["nexpand"] > 0
 
-        def J(r):
+        def J(dp, r):
             defp = np.zeros((n, n, n), order="F")
-            ctx.calcdefp(defp, None, None, defpot, np.asfortranarray(r), dtold, dtaumesh, nfluid=1)
+            ctx.calcdefp(defp, None, None, np.asfortranarray(dp), np.asfortranarray(r), dtold, dtaumesh, nfluid=1)
             return float(np.sum(w * defp))
 
-        for v in dirs:
-            fd = (J(rho + h * v) - J(rho - h * v)) / (2 * h)
-            ad = float(np.sum(grho * v))
-            scale = float(np.sum(np.abs(grho * v)))
-            print(f"{case}: fd {fd:.12e} adjoint {ad:.12e} rel {abs(fd - ad) / abs(ad):.2e}")
-            assert abs(fd - ad) <= 2e-6 * max(abs(ad), 1e-3 * scale), (fd, ad)
+        for name, g, vs in (("rho", grho, dirs), ("def", gdef, ddirs)):
+            for v in vs:
+                if name == "rho":
+                    fd = (J(defpot, rho + h * v) - J(defpot, rho - h * v)) / (2 * h)
+                else:
+                    fd = (J(defpot + h * v, rho) - J(defpot - h * v, rho)) / (2 * h)
+                ad = float(np.sum(g * v))
+                scale = float(np.sum(np.abs(g * v)))
+                print(f"{case} d/d{name}: fd {fd:.12e} adjoint {ad:.12e} rel {abs(fd - ad) / abs(ad):.2e}")
+                assert abs(fd - ad) <= 1e-7 * max(abs(ad), 1e-3 * scale), (name, fd, ad)
 
 
 @pytest.mark.gpu
