@@ -219,6 +219,14 @@ int mmh_relax_noalloc_f64(const double* d_deformpot, const double* d_rho, double
 int mmh_calcdefp_adjoint_f64(mmh_ctx* ctx, const double* def, const double* u, int nfluid, double dtold1,
                              double dtaumesh, const double* w, double* grho, double* gdef, mmh_diag* diag);
 
+/* gu(n,n,n) = dJ/d rho, gdef = dJ/d def, gdefp = dJ/d defp (the last two may
+ * be NULL) for J = sum w*u'(1,:,:,:), u' the density that mmh_relaxing_f64
+ * computes from the same u, def, defp and dt (u(2:nfluidcmp) == 0), with the
+ * minmod slopes and the cflkeuler maximum frozen where this forward pass took
+ * them.  Assumes a finite non-zero density and det in every cell. */
+int mmh_relaxing_adjoint_f64(mmh_ctx* ctx, const double* u, const double* def, const double* defp, double dt,
+                             int nfluidcmp, const double* w, double* gu, double* gdef, double* gdefp);
+
 /* ---- kernel timing (no counterpart in the reference) -------------------- */
 /* Arm CUDA-event timing of one kernel kind (MMH_K_* | MMH_K_F32 for the FP32
  * instantiation) on the stream it is launched on; mmh_profile_stop returns the

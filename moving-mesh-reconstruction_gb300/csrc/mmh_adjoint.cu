@@ -14,6 +14,7 @@
 // where L lam = S^2 w - mean, D the frozen pass-1 derivative, B27 the box
 // mean and G_f the bilinear form of coefficient f (k_adj_contract).
 #include "mmh_launch.cuh"
+#include "mmh_phys.cuh"
 
 namespace mmh {
 
@@ -92,6 +93,21 @@ __global__ void k_box27(const double* __restrict__ in, int n, double* __restrict
   out[t] = s / 27.0;
 }
 
+// Adjoint of A = I + Hess(def) (6 planes a11, a12, a13, a22, a23, a33; a12
+// stands for both off-diagonal entries) from the adjoint detb of det(A) and
+// the adjoints c_f of the cofactors cof_f(A).
+__device__ __forceinline__ void adj_cofdet(double a11, double a12, double a13, double a22, double a23, double a33,
+                                           double b11, double b12, double b13, double b22, double b23, double b33,
+                                           double detb, double c11, double c12, double c13, double c22, double c23,
+                                           double c33, double* __restrict__ abar, i64 t, i64 n3) {
+  abar[t] = detb * b11 + c22 * a33 - c23 * a23 + c33 * a22;
+  abar[n3 + t] = 2.0 * detb * b12 - c12 * a33 + c13 * a23 + c23 * a13 - 2.0 * c33 * a12;
+  abar[2 * n3 + t] = 2.0 * detb * b13 + c12 * a23 - c13 * a22 - 2.0 * c22 * a13 + c23 * a12;
+  abar[3 * n3 + t] = detb * b22 + c11 * a33 - c13 * a13 + c33 * a11;
+  abar[4 * n3 + t] = 2.0 * detb * b23 - 2.0 * c11 * a23 + c12 * a13 + c13 * a12 - c23 * a11;
+  abar[5 * n3 + t] = detb * b33 + c11 * a22 - c12 * a12 + c22 * a11;
+}
+
 // Gradient with respect to the entries of A = I + Hess(def) of
 //   - sum_f urg G_f C_f(A)   (the operator path, C_f = cof_f / det with the
 //                              tangle fallback det <= 1e-5 of cbajraw)
@@ -137,13 +153,8 @@ __global__ void k_adj_metric(const double* __restrict__ def, const double* __res
     detb -= (g11 * b11 + g12 * b12 + g13 * b13 + g22 * b22 + g23 * b23 + g33 * b33) / det;
     c11 = g11; c12 = g12; c13 = g13; c22 = g22; c23 = g23; c33 = g33;
   }
-  // d det / d a and d cof / d a (symmetric A: a12 stands for both off-diagonal entries)
-  abar[t] = detb * b11 + c22 * a33 - c23 * a23 + c33 * a22;
-  abar[n3 + t] = 2.0 * detb * b12 - c12 * a33 + c13 * a23 + c23 * a13 - 2.0 * c33 * a12;
-  abar[2 * n3 + t] = 2.0 * detb * b13 + c12 * a23 - c13 * a22 - 2.0 * c22 * a13 + c23 * a12;
-  abar[3 * n3 + t] = detb * b22 + c11 * a33 - c13 * a13 + c33 * a11;
-  abar[4 * n3 + t] = 2.0 * detb * b23 - 2.0 * c11 * a23 + c12 * a13 + c13 * a12 - c23 * a11;
-  abar[5 * n3 + t] = detb * b33 + c11 * a22 - c12 * a12 + c22 * a11;
+  adj_cofdet(a11, a12, a13, a22, a23, a33, b11, b12, b13, b22, b23, b33, detb, c11, c12, c13, c22, c23, c33, abar,
+             t, n3);
 }
 
 // out (+)= Hess^T abar: the second differences of the metric are symmetric
@@ -172,6 +183,204 @@ __global__ void k_adj_pair(const double* __restrict__ a, const double* __restric
   i64 q = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n3) return;
   out[q] = op ? a[q] * b[q] : a[q] - b[q];
+}
+
+// ---------------------------------------------------------------------------
+// relaxing adjoint (relaxing.f90, density-only state at rest)
+//
+// Forward map, restated: per cell the flux ratios alpha_a = vv_a / c with
+// vv = b (0 - grad defp), b = cof/det of I + Hess(def), c = max_a |vv_a|
+// (cflkeuler, the branch of a finite non-zero density and det); the half sums
+// S_a = x (1 + alpha_a) / 2 and differences D_a = x (1 - alpha_a) / 2; the
+// face flux F_a(f) = (c(f) + c(f+a)) / 2 * wphalf(S_a, D_a) with the minmod
+// slopes; R(x) = sum_a F_a(e) - F_a(e-a).  TVD RK2: x1 = u - dt/2 R(u),
+// u' = u - dt R(x1), both stages with the alpha and c of u's stage.
+// ---------------------------------------------------------------------------
+
+// minmod with wslopelim 1.5 (relaxing.f90): value and the partial
+// derivatives in a and b on the branch it takes.
+__device__ __forceinline__ double mm_branch(double a, double b, double& da, double& db) {
+  double x = fabs(a), y = fabs(b);
+  da = 0.0;
+  db = 0.0;
+  if ((a >= 0.0) != (b >= 0.0)) return 0.0;
+  double s = a >= 0.0 ? 1.0 : -1.0;
+  double lo = fmin(x, y), hi = fmax(x, y);
+  if (1.5 * lo <= hi) {
+    if (x <= y) da = 1.5; else db = 1.5;
+    return s * 1.5 * lo;
+  }
+  if (x >= y) da = 1.0; else db = 1.0;
+  return s * hi;
+}
+
+// Face f -> fp along one axis (cells fm, f, fp, fpp): the adjoints P of the
+// six half sums and differences it reads and Q of each of its two speeds,
+// for the output adjoint rbar scaled by `scale`.
+struct FaceAdj {
+  double p0, p1, p2, p3, p4, p5, q;
+};
+__device__ __forceinline__ FaceAdj face_adj(const double* __restrict__ S, const double* __restrict__ D,
+                                            const double* __restrict__ cc, const double* __restrict__ rbar,
+                                            double scale, i64 fm, i64 f, i64 fp, i64 fpp) {
+  double sm = S[fm], s0 = S[f], sp = S[fp], d0 = D[f], dp = D[fp], dpp = D[fpp];
+  double mu1, mu2, nu1, nu2;
+  double ma = mm_branch(s0 - sm, sp - s0, mu1, mu2);
+  double mb = mm_branch(dpp - dp, dp - d0, nu1, nu2);
+  double wph = (s0 + ma * 0.5) - (dp - mb * 0.5);
+  double fb = scale * (rbar[f] - rbar[fp]);
+  double wb = fb * (cc[fp] + cc[f]) * 0.5;
+  FaceAdj r;
+  r.p0 = wb * (-0.5 * mu1);
+  r.p1 = wb * (1.0 + 0.5 * mu1 - 0.5 * mu2);
+  r.p2 = wb * (0.5 * mu2);
+  r.p3 = -wb * (1.0 + 0.5 * nu1 - 0.5 * nu2);
+  r.p4 = wb * (0.5 * nu1);
+  r.p5 = -wb * (0.5 * nu2);
+  r.q = fb * wph * 0.5;
+  return r;
+}
+
+// flux ratios alpha_a = vv_a / c of stage 1 (3 planes)
+__global__ void k_adj_alpha(const double* __restrict__ baj, const double* __restrict__ defp,
+                            const double* __restrict__ cc, int n, double* __restrict__ alpha) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  int i, j, k;
+  cell_of(t, n, i, j, k);
+  double v1 = 0.0 - (defp[IDX(wp(i, n), j, k, n)] - defp[IDX(wm(i, n), j, k, n)]) * 0.5;
+  double v2 = 0.0 - (defp[IDX(i, wp(j, n), k, n)] - defp[IDX(i, wm(j, n), k, n)]) * 0.5;
+  double v3 = 0.0 - (defp[IDX(i, j, wp(k, n), n)] - defp[IDX(i, j, wm(k, n), n)]) * 0.5;
+  double b11 = baj[t], b12 = baj[n3 + t], b13 = baj[2 * n3 + t], b22 = baj[3 * n3 + t], b23 = baj[4 * n3 + t],
+         b33 = baj[5 * n3 + t];
+  double c = cc[t];
+  alpha[t] = (b11 * v1 + b12 * v2 + b13 * v3) / c;
+  alpha[n3 + t] = (b12 * v1 + b22 * v2 + b23 * v3) / c;
+  alpha[2 * n3 + t] = (b13 * v1 + b23 * v2 + b33 * v3) / c;
+}
+
+// Adjoint of one dpv evaluation x -> scale * R(x) against rbar: xbar = the
+// state adjoint (written), alphabar and cbar accumulated.  sd holds the half
+// sums and differences of x as the forward pass formed them (their minmod
+// branches are the forward's).
+__global__ void k_adj_dpv(const double* __restrict__ sd, const double* __restrict__ cc,
+                          const double* __restrict__ alpha, const double* __restrict__ x,
+                          const double* __restrict__ rbar, double scale, int n, double* __restrict__ xbar,
+                          double* __restrict__ alphabar, double* __restrict__ cbar) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  int ijk[3];
+  cell_of(t, n, ijk[0], ijk[1], ijk[2]);
+  double xb = 0.0, cb = 0.0;
+  const double xe = x[t];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    // cells e-3a .. e+3a along axis a
+    i64 at[7];
+#pragma unroll
+    for (int o = -3; o <= 3; ++o) {
+      int c3[3] = {ijk[0], ijk[1], ijk[2]};
+      int v = c3[a] + o;
+      v = v < 0 ? v + n : (v >= n ? v - n : v);
+      c3[a] = v;
+      at[o + 3] = IDX(c3[0], c3[1], c3[2], n);
+    }
+    const double* S = sd + a * n3;
+    const double* D = sd + (3 + a) * n3;
+    FaceAdj up = face_adj(S, D, cc, rbar, scale, at[3], at[4], at[5], at[6]);  // face e+a
+    FaceAdj f0 = face_adj(S, D, cc, rbar, scale, at[2], at[3], at[4], at[5]);  // face e
+    FaceAdj m1 = face_adj(S, D, cc, rbar, scale, at[1], at[2], at[3], at[4]);  // face e-a
+    FaceAdj m2 = face_adj(S, D, cc, rbar, scale, at[0], at[1], at[2], at[3]);  // face e-2a
+    double sb = up.p0 + f0.p1 + m1.p2;
+    double db = f0.p5 + m1.p3 + m2.p4;
+    cb += f0.q + m1.q;
+    double al = alpha[a * n3 + t];
+    xb += sb * (1.0 + al) * 0.5 + db * (1.0 - al) * 0.5;
+    alphabar[a * n3 + t] += (sb - db) * xe * 0.5;
+  }
+  xbar[t] = xb;
+  cbar[t] += cb;
+}
+
+// From alphabar and cbar to the adjoints of A = I + Hess(def) (6 planes) and
+// of the centred differences pd_a = (defp(e+a) - defp(e-a)) / 2 (3 planes).
+__global__ void k_adj_relax_geom(const double* __restrict__ def, const double* __restrict__ defp,
+                                 const double* __restrict__ cc, const double* __restrict__ alphabar,
+                                 const double* __restrict__ cbar, int n, double* __restrict__ abar,
+                                 double* __restrict__ pdbar) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  int i, j, k;
+  cell_of(t, n, i, j, k);
+  LimM m = lim_metric(def, n, i, j, k);
+  double pd1 = (defp[IDX(wp(i, n), j, k, n)] - defp[IDX(wm(i, n), j, k, n)]) * 0.5;
+  double pd2 = (defp[IDX(i, wp(j, n), k, n)] - defp[IDX(i, wm(j, n), k, n)]) * 0.5;
+  double pd3 = (defp[IDX(i, j, wp(k, n), n)] - defp[IDX(i, j, wm(k, n), n)]) * 0.5;
+  double v1 = 0.0 - pd1, v2 = 0.0 - pd2, v3 = 0.0 - pd3;
+  double vv[3] = {m.b11 * v1 + m.b12 * v2 + m.b13 * v3, m.b12 * v1 + m.b22 * v2 + m.b23 * v3,
+                  m.b13 * v1 + m.b23 * v2 + m.b33 * v3};
+  // the maximum cflkeuler takes: max(max(|vv1|, |vv2|), |vv3|), first on ties
+  int as = fabs(vv[0]) < fabs(vv[1]) ? 1 : 0;
+  as = fabs(vv[as]) < fabs(vv[2]) ? 2 : as;
+  double c = cc[t];
+  double ab[3] = {alphabar[t], alphabar[n3 + t], alphabar[2 * n3 + t]};
+  // alpha_a = vv_a / c, c = |vv_as|
+  double cb = cbar[t] - (ab[0] * vv[0] + ab[1] * vv[1] + ab[2] * vv[2]) / (c * c);
+  double vb[3] = {ab[0] / c, ab[1] / c, ab[2] / c};
+  vb[as] += cb * (vv[as] > 0.0 ? 1.0 : (vv[as] < 0.0 ? -1.0 : 0.0));
+  // vv = b v, v = -pd; b = cof / det
+  double g11 = vb[0] * v1, g22 = vb[1] * v2, g33 = vb[2] * v3;
+  double g12 = vb[0] * v2 + vb[1] * v1, g13 = vb[0] * v3 + vb[2] * v1, g23 = vb[1] * v3 + vb[2] * v2;
+  pdbar[t] = -(m.b11 * vb[0] + m.b12 * vb[1] + m.b13 * vb[2]);
+  pdbar[n3 + t] = -(m.b12 * vb[0] + m.b22 * vb[1] + m.b23 * vb[2]);
+  pdbar[2 * n3 + t] = -(m.b13 * vb[0] + m.b23 * vb[1] + m.b33 * vb[2]);
+  double a11 = 1.0 + m.phixx, a22 = 1.0 + m.phiyy, a33 = 1.0 + m.phizz, a12 = m.phixy, a13 = m.phixz, a23 = m.phiyz;
+  double det = m.det;
+  double c11 = a22 * a33 - a23 * a23, c12 = a13 * a23 - a12 * a33, c13 = a12 * a23 - a13 * a22;
+  double c22 = a11 * a33 - a13 * a13, c23 = a12 * a13 - a11 * a23, c33 = a11 * a22 - a12 * a12;
+  g11 /= det; g12 /= det; g13 /= det; g22 /= det; g23 /= det; g33 /= det;
+  double detb = -(g11 * c11 + g12 * c12 + g13 * c13 + g22 * c22 + g23 * c23 + g33 * c33) / det;
+  adj_cofdet(a11, a12, a13, a22, a23, a33, c11, c12, c13, c22, c23, c33, detb, g11, g12, g13, g22, g23, g33, abar,
+             t, n3);
+}
+
+// out (+)= the transpose of the centred differences pd_a of defp
+__global__ void k_adj_grad_t(const double* __restrict__ pdbar, int n, double* __restrict__ out, int add) {
+  i64 n3 = (i64)n * n * n;
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  int i, j, k;
+  cell_of(t, n, i, j, k);
+  double r = (pdbar[IDX(wm(i, n), j, k, n)] - pdbar[IDX(wp(i, n), j, k, n)]) * 0.5 +
+             (pdbar[n3 + IDX(i, wm(j, n), k, n)] - pdbar[n3 + IDX(i, wp(j, n), k, n)]) * 0.5 +
+             (pdbar[2 * n3 + IDX(i, j, wm(k, n), n)] - pdbar[2 * n3 + IDX(i, j, wp(k, n), n)]) * 0.5;
+  out[t] = add ? out[t] + r : r;
+}
+
+void launch_adj_alpha(const double* baj, const double* defp, const double* cc, int n, double* alpha, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  k_adj_alpha<<<grid_of(n3, kBlock), kBlock, 0, s>>>(baj, defp, cc, n, alpha);
+  count_launch();
+}
+void launch_adj_dpv(const double* sd, const double* cc, const double* alpha, const double* x, const double* rbar,
+                    double scale, int n, double* xbar, double* alphabar, double* cbar, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  k_adj_dpv<<<grid_of(n3, kBlock), kBlock, 0, s>>>(sd, cc, alpha, x, rbar, scale, n, xbar, alphabar, cbar);
+  count_launch();
+}
+void launch_adj_relax_geom(const double* def, const double* defp, const double* cc, const double* alphabar,
+                           const double* cbar, int n, double* abar, double* pdbar, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  k_adj_relax_geom<<<grid_of(n3, kBlock), kBlock, 0, s>>>(def, defp, cc, alphabar, cbar, n, abar, pdbar);
+  count_launch();
+}
+void launch_adj_grad_t(const double* pdbar, int n, double* out, int add, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  k_adj_grad_t<<<grid_of(n3, kBlock), kBlock, 0, s>>>(pdbar, n, out, add);
+  count_launch();
 }
 
 void launch_adj_pass1(double* y, const double* t, const uint8_t* maskx, const uint8_t* maskc, double dtaumesh,

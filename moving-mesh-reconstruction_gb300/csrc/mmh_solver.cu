@@ -747,6 +747,51 @@ int calcdefp_adjoint_dev(mmh_ctx* c, double dtold, double dtaumesh, double* w, d
   return MMH_OK;
 }
 
+// Gradients of J = ubar^T u' for u' = relaxing(u, def, defp, dt) on the
+// resident rho, def and defp (no counterpart in the reference), with the
+// minmod slopes and the cflkeuler maximum frozen where the forward pass took
+// them: gu, gdef, gdefp (device, n^3; gdef and gdefp may be null) receive the
+// gradients with respect to the density, def and defp.  ubar (device) is read.
+int relaxing_adjoint_dev(mmh_ctx* c, double dt, const double* ubar, double* gu, double* gdef, double* gdefp) {
+  int n = c->n;
+  i64 n3 = c->n3;
+  DevTemp buf;
+  buf.s = c->s;
+  if (cudaMallocAsync(&buf.p, sizeof(double) * 33 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
+  double* baj = (double*)buf.p;  // 7 planes
+  double* cc = baj + 7 * n3;
+  double* sd0 = cc + n3;         // half sums and differences at u (6 planes)
+  double* sd1 = sd0 + 6 * n3;    // ... at the half step (6 planes)
+  double* gface = sd1 + 6 * n3;  // 3 planes
+  double* u1 = gface + 3 * n3;
+  double* alpha = u1 + n3;       // 3 planes
+  double* alphabar = alpha + 3 * n3;
+  double* cbar = alphabar + 3 * n3;
+  double* u1bar = cbar + n3;
+  double* xbar = u1bar + n3;
+  double* defp = c->defp();
+  // forward pass (relaxing_dev) with both stages' half sums kept
+  launch_relax_stage1(c->rho, c->def, defp, n, baj, cc, sd0, c->s);
+  launch_adj_alpha(baj, defp, cc, n, alpha, c->s);
+  launch_relax_dpv(sd0, cc, n, c->rho, dt / 2.0, u1, gface, c->s);
+  launch_relax_flux(u1, defp, baj, cc, n, sd1, c->s);
+  // stage 2 (u' = u - dt R(u1)), then stage 1 (u1 = u - dt/2 R(u))
+  CK(cudaMemsetAsync(alphabar, 0, sizeof(double) * 4 * n3, c->s));
+  launch_adj_dpv(sd1, cc, alpha, u1, ubar, -dt, n, u1bar, alphabar, cbar, c->s);
+  launch_adj_dpv(sd0, cc, alpha, c->rho, u1bar, -dt / 2.0, n, xbar, alphabar, cbar, c->s);
+  CK(cudaMemcpyAsync(gu, ubar, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  launch_add(gu, u1bar, n3, c->s);
+  launch_add(gu, xbar, n3, c->s);
+  // the flux ratios and speeds back to def and defp (sd0, sd1 are free)
+  double* abar = sd0;
+  double* pdbar = sd1;
+  launch_adj_relax_geom(c->def, defp, cc, alphabar, cbar, n, abar, pdbar, c->s);
+  if (gdef) launch_adj_hess(abar, n, gdef, 0, c->s);
+  if (gdefp) launch_adj_grad_t(pdbar, n, gdefp, 0, c->s);
+  CK(cudaGetLastError());
+  return MMH_OK;
+}
+
 // relaxing(u, def, defp, cmax, dt, 5) on the resident density.
 int relaxing_dev(mmh_ctx* c, double dt) {
   int n = c->n;
@@ -1149,6 +1194,24 @@ int mmh_calcdefp_adjoint_f64(mmh_ctx* c, const double* def, const double* u, int
   RET(st);
   if (grho) RET(download(c, dw + n3, grho, n3));
   if (gdef) RET(download(c, dw + 2 * n3, gdef, n3));
+  return MMH_OK;
+}
+int mmh_relaxing_adjoint_f64(mmh_ctx* c, const double* u, const double* def, const double* defp, double dt,
+                             int nfluidcmp, const double* w, double* gu, double* gdef, double* gdefp) {
+  if (!c || !u || !def || !defp || !w || !gu) return MMH_ERR_ARG;
+  i64 n3 = c->n3;
+  RET(upload(c, def, c->def, n3));
+  RET(upload(c, defp, c->defp(), n3));
+  RET(upload_density(c, u, nfluidcmp, n3, c->rho));
+  DevTemp buf;
+  buf.s = c->s;
+  if (cudaMallocAsync(&buf.p, sizeof(double) * 4 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
+  double* dw = (double*)buf.p;
+  RET(upload(c, w, dw, n3));
+  RET(relaxing_adjoint_dev(c, dt, dw, dw + n3, gdef ? dw + 2 * n3 : nullptr, gdefp ? dw + 3 * n3 : nullptr));
+  RET(download(c, dw + n3, gu, n3));
+  if (gdef) RET(download(c, dw + 2 * n3, gdef, n3));
+  if (gdefp) RET(download(c, dw + 3 * n3, gdefp, n3));
   return MMH_OK;
 }
 int mmh_multigrid(mmh_ctx* c, float* u, float* rhs, const float* defpot, const float* ubig, float dx, int nx, int ny,

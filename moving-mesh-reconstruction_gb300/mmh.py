@@ -40,6 +40,7 @@ EXPORTS = (
     "mmh_limiter_poisson_f64", "mmh_load_f64", "mmh_load_dev", "mmh_iterate", "mmh_store_f64",
     "mmh_outputs_f64", "mmh_outputs_dev", "mmh_state_dev", "mmh_profile_start", "mmh_profile_stop",
     "mmh_relax_noalloc_f64", "mmh_batch_run", "mmh_calcdefp_adjoint_f64",
+    "mmh_relaxing_adjoint_f64",
 )
 
 # kernel kinds for the timing hooks
@@ -209,6 +210,16 @@ class Context:
                                             C.c_double(dtaumesh), _p(w), _p(grho), _p(gdef), C.byref(d)),
              "calcdefp_adjoint")
         return grho, gdef, d.as_dict()
+
+    def relaxing_adjoint(self, u, defpot, defp, w, dt=1.0, nfluidcmp=5):
+        """Gradients of sum(w * u'[density]) for u' = relaxing(u, defpot, defp,
+        dt) with the minmod slopes frozen.  Returns (gu, gdef, gdefp)."""
+        for a in (u, defpot, defp, w):
+            _farr(a, np.float64)
+        g = [np.zeros(defpot.shape, dtype=np.float64, order="F") for _ in range(3)]
+        _chk(lib().mmh_relaxing_adjoint_f64(self._h, _p(u), _p(defpot), _p(defp), C.c_double(dt), int(nfluidcmp),
+                                            _p(w), _p(g[0]), _p(g[1]), _p(g[2])), "relaxing_adjoint")
+        return tuple(g)
 
     def multigrid(self, u, rhs, defpot, ubig, dx, nx, ny, nz, nu, nred=1, iopt=2):
         """multigrid(u,rhs,defpot,ubig,dx,nx,ny,nz,nu,nred,iopt)  (mmh/multigrid.f90:16)."""

@@ -135,3 +135,43 @@ def test_calcdefp_adjoint_needs_a_solving_schedule(mmh, fields):
         with pytest.raises(mmh.MMHError) as e:
             ctx.calcdefp_adjoint(z, rho, z, 1.0, 1.0, nfluid=1)
         assert e.value.code == mmh.MMH_ERR_UNSUPPORTED
+
+
+@pytest.mark.gpu
+def test_relaxing_adjoint_matches_finite_differences(mmh, fields):
+    """relaxing adjoint against central differences of relaxing.f90's density
+    update, on the state of the first deformation iteration (def = defp =
+    calcdefp's increment from def = 0, as main.f90:95-101 calls them)."""
+    n, dt = 16, 1.0
+    rho = fields.lognormal_density(n, sigma=0.6, seed=21)
+    z = np.zeros((n, n, n), order="F")
+    rng = np.random.default_rng(22)
+    w = np.asfortranarray(_s3(rng.standard_normal((n, n, n))))
+    with mmh.Context(n, precision=mmh.MMH_FP64, schedule=mmh.MMH_SCHED_TOL, tol=1e-12) as ctx:
+        defp = np.zeros((n, n, n), order="F")
+        ctx.calcdefp(defp, None, None, z, rho, 1.0, 1.0, nfluid=1)
+        defpot = defp.copy(order="F")
+        gu, gdef, gdefp = ctx.relaxing_adjoint(rho, defpot, defp, w, dt, nfluidcmp=1)
+
+        def J(r, dpot, dp):
+            u = np.asfortranarray(r.copy())
+            ctx.relaxing(u, np.asfortranarray(dpot), np.asfortranarray(dp), 1.0, dt, nfluidcmp=1)
+            return float(np.sum(w * u))
+
+        amp = np.abs(defp).max()
+        checks = []
+        for q in range(2):
+            checks.append(("rho", gu, np.asfortranarray(_s3(rng.standard_normal((n, n, n))))))
+            checks.append(("def", gdef, smooth_field(n, amp, 40 + q)))
+            checks.append(("defp", gdefp, smooth_field(n, amp, 50 + q)))
+        for name, g, v in checks:
+            h = 1e-6 / max(np.abs(v).max(), 1e-300)
+            args_p = [rho, defpot, defp]
+            args_m = [rho, defpot, defp]
+            k = ("rho", "def", "defp").index(name)
+            args_p[k] = args_p[k] + h * v
+            args_m[k] = args_m[k] - h * v
+            fd = (J(*args_p) - J(*args_m)) / (2 * h)
+            ad = float(np.sum(g * v))
+            print(f"relaxing d/d{name}: fd {fd:.12e} adjoint {ad:.12e} rel {abs(fd - ad) / abs(ad):.2e}")
+            assert abs(fd - ad) <= 1e-6 * abs(ad), (name, fd, ad)
