@@ -227,6 +227,17 @@ int mmh_calcdefp_adjoint_f64(mmh_ctx* ctx, const double* def, const double* u, i
 int mmh_relaxing_adjoint_f64(mmh_ctx* ctx, const double* u, const double* def, const double* defp, double dt,
                              int nfluidcmp, const double* w, double* gu, double* gdef, double* gdefp);
 
+/* Adjoint of a whole reconstruction: niter deformation iterations of
+ * mmh_iterate from the loaded state (def_0, rho_0), then grho = dJ/d rho_0 and
+ * gdef = dJ/d def_0 (NULL: not returned) for
+ *   J = sum wdef*def_N + sum wdelta*delta,  delta = defp2delta(def_N),
+ * (wdef, wdelta: n^3 host arrays, NULL: zero), the limiter and slope-limiter
+ * branches frozen as above.  The forward states are kept every
+ * checkpoint_every iterations and the others recomputed as the adjoint walks
+ * back.  Needs a solving schedule; the state ends as after mmh_iterate(niter). */
+int mmh_iterate_adjoint_f64(mmh_ctx* ctx, int niter, int checkpoint_every, const double* wdef, const double* wdelta,
+                            double* grho, double* gdef, mmh_diag* diag);
+
 /* ---- kernel timing (no counterpart in the reference) -------------------- */
 /* Arm CUDA-event timing of one kernel kind (MMH_K_* | MMH_K_F32 for the FP32
  * instantiation) on the stream it is launched on; mmh_profile_stop returns the

@@ -648,6 +648,33 @@ int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t
   return st;
 }
 
+// relaxing(u, def, defp, cmax, dt, 5) on the resident density.
+int relaxing_dev(mmh_ctx* c, double dt) {
+  int n = c->n;
+  launch_relax_stage1(c->rho, c->def, c->defp(), n, c->baj, c->cc, c->vt, c->s);
+  launch_relax_dpv(c->vt, c->cc, n, c->rho, dt / 2.0, c->u1, c->gface, c->s);
+  launch_relax_flux(c->u1, c->defp(), c->baj, c->cc, n, c->vt, c->s);
+  launch_relax_dpv(c->vt, c->cc, n, c->rho, dt, c->rho, c->gface, c->s);
+  return MMH_OK;
+}
+
+// spectral outputs of src into host/device buffers (grad: 3 planes of n^3)
+int spectral_outputs(mmh_ctx* c, const double* src, double* d_grad, double* d_delta) {
+  RET(make_plans(c));
+  CKF(cufftExecD2Z(c->pd2z, (cufftDoubleReal*)src, (cufftDoubleComplex*)c->Xc));
+  for (int ax = 0; ax < 3 && d_grad; ++ax) {
+    launch_spec_pack(c->Xc, c->n, ax, c->Z, &c->sc->lim, c->spectab, c->s);
+    CKF(cufftExecZ2Z(c->pz2z, (cufftDoubleComplex*)c->Z, (cufftDoubleComplex*)c->Z, CUFFT_FORWARD));
+    launch_spec_unpack(c->Z, c->n, d_grad + ax * c->n3, 1, 0, &c->sc->lim, c->s);
+  }
+  if (d_delta) {
+    launch_spec_pack(c->Xc, c->n, 3, c->Z, &c->sc->lim, c->spectab, c->s);
+    CKF(cufftExecZ2Z(c->pz2z, (cufftDoubleComplex*)c->Z, (cufftDoubleComplex*)c->Z, CUFFT_FORWARD));
+    launch_spec_unpack(c->Z, c->n, d_delta, 1, 0, &c->sc->lim, c->s);
+  }
+  return MMH_OK;
+}
+
 // Device scratch of one call, released on the context's stream at scope exit.
 struct DevTemp {
   void* p = nullptr;
@@ -792,30 +819,110 @@ int relaxing_adjoint_dev(mmh_ctx* c, double dt, const double* ubar, double* gu, 
   return MMH_OK;
 }
 
-// relaxing(u, def, defp, cmax, dt, 5) on the resident density.
-int relaxing_dev(mmh_ctx* c, double dt) {
-  int n = c->n;
-  launch_relax_stage1(c->rho, c->def, c->defp(), n, c->baj, c->cc, c->vt, c->s);
-  launch_relax_dpv(c->vt, c->cc, n, c->rho, dt / 2.0, c->u1, c->gface, c->s);
-  launch_relax_flux(c->u1, c->defp(), c->baj, c->cc, n, c->vt, c->s);
-  launch_relax_dpv(c->vt, c->cc, n, c->rho, dt, c->rho, c->gface, c->s);
-  return MMH_OK;
-}
-
-// spectral outputs of src into host/device buffers (grad: 3 planes of n^3)
-int spectral_outputs(mmh_ctx* c, const double* src, double* d_grad, double* d_delta) {
-  RET(make_plans(c));
-  CKF(cufftExecD2Z(c->pd2z, (cufftDoubleReal*)src, (cufftDoubleComplex*)c->Xc));
-  for (int ax = 0; ax < 3 && d_grad; ++ax) {
-    launch_spec_pack(c->Xc, c->n, ax, c->Z, &c->sc->lim, c->spectab, c->s);
-    CKF(cufftExecZ2Z(c->pz2z, (cufftDoubleComplex*)c->Z, (cufftDoubleComplex*)c->Z, CUFFT_FORWARD));
-    launch_spec_unpack(c->Z, c->n, d_grad + ax * c->n3, 1, 0, &c->sc->lim, c->s);
+// niter deformation iterations of mmh_iterate on the resident (def_0, rho_0)
+// followed by their adjoint (no counterpart in the reference): for
+// J = wdef^T def_N + wdelta^T defp2delta(def_N), grho = dJ/d rho_0 and
+// gdef = dJ/d def_0 (device, n^3; wdef, wdelta, gdef may be null).  The
+// forward states are kept every `every` iterations and the iterations between
+// two of them recomputed, segment by segment, as the adjoint walks back.  The
+// resident state ends as (def_N, rho_N); the defp buffer is scratch.
+int iterate_adjoint_dev(mmh_ctx* c, int niter, int every, const double* wdef, const double* wdelta, double* grho,
+                        double* gdef, mmh_diag* d) {
+  if (c->cfg.schedule == MMH_SCHED_REF) return MMH_ERR_UNSUPPORTED;
+  if (niter < 0 || every < 1) return MMH_ERR_ARG;
+  const i64 n3 = c->n3;
+  const size_t f = sizeof(double) * (size_t)n3;
+  const int ncp = niter > 0 ? (niter + every - 1) / every : 0;
+  const int seg = std::min(every, std::max(niter, 1));
+  DevTemp buf;
+  buf.s = c->s;
+  // checkpoints (def, rho) | segment states (def, rho, defp) | final state |
+  // rhobar, rhobar_next, defbar, and four gradient parts
+  const i64 words = (2 * (i64)ncp + 3 * (i64)seg + 2 + 7) * n3;
+  if (cudaMallocAsync(&buf.p, sizeof(double) * words, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
+  double* ckpt = (double*)buf.p;
+  double* segst = ckpt + 2 * (i64)ncp * n3;
+  double* fin = segst + 3 * (i64)seg * n3;
+  double* rbar = fin + 2 * n3;
+  double* rbar2 = rbar + n3;
+  double* dbar = rbar2 + n3;
+  double* ga = dbar + n3;
+  double* gb = ga + n3;
+  double* gc = gb + n3;
+  double* gd = gc + n3;
+  double* defp = c->defp();
+  auto step = [&](mmh_diag* dd) -> int {
+    int st = calcdefp_dev(c, 1.0, 1.0, nullptr, nullptr, nullptr, dd);
+    if (st != MMH_OK) return st;
+    launch_add(c->def, defp, n3, c->s);
+    return relaxing_dev(c, 1.0);
+  };
+  // forward pass with checkpoints
+  for (int k = 0; k < niter; ++k) {
+    if (k % every == 0) {
+      CK(cudaMemcpyAsync(ckpt + 2 * (i64)(k / every) * n3, c->def, f, cudaMemcpyDeviceToDevice, c->s));
+      CK(cudaMemcpyAsync(ckpt + (2 * (i64)(k / every) + 1) * n3, c->rho, f, cudaMemcpyDeviceToDevice, c->s));
+    }
+    mmh_diag dd{};
+    RET(step(&dd));
+    if (d) *d = dd;
   }
-  if (d_delta) {
-    launch_spec_pack(c->Xc, c->n, 3, c->Z, &c->sc->lim, c->spectab, c->s);
-    CKF(cufftExecZ2Z(c->pz2z, (cufftDoubleComplex*)c->Z, (cufftDoubleComplex*)c->Z, CUFFT_FORWARD));
-    launch_spec_unpack(c->Z, c->n, d_delta, 1, 0, &c->sc->lim, c->s);
+  CK(cudaMemcpyAsync(fin, c->def, f, cudaMemcpyDeviceToDevice, c->s));
+  CK(cudaMemcpyAsync(fin + n3, c->rho, f, cudaMemcpyDeviceToDevice, c->s));
+  // seeds: defbar_N = wdef + defp2delta(wdelta) (defp2delta is symmetric)
+  launch_fill<double>(rbar, n3, 0.0, c->s);
+  if (wdelta) {
+    RET(spectral_outputs(c, wdelta, nullptr, dbar));
+    if (wdef) launch_add(dbar, wdef, n3, c->s);
+  } else if (wdef) {
+    CK(cudaMemcpyAsync(dbar, wdef, f, cudaMemcpyDeviceToDevice, c->s));
+  } else {
+    launch_fill<double>(dbar, n3, 0.0, c->s);
   }
+  for (int s = ncp - 1; s >= 0; --s) {
+    const int k0 = s * every, k1 = std::min(k0 + every, niter);
+    CK(cudaMemcpyAsync(c->def, ckpt + 2 * (i64)s * n3, f, cudaMemcpyDeviceToDevice, c->s));
+    CK(cudaMemcpyAsync(c->rho, ckpt + (2 * (i64)s + 1) * n3, f, cudaMemcpyDeviceToDevice, c->s));
+    for (int k = k0; k < k1; ++k) {
+      double* sk = segst + 3 * (i64)(k - k0) * n3;
+      CK(cudaMemcpyAsync(sk, c->def, f, cudaMemcpyDeviceToDevice, c->s));
+      CK(cudaMemcpyAsync(sk + n3, c->rho, f, cudaMemcpyDeviceToDevice, c->s));
+      if (k + 1 < k1) {
+        RET(step(nullptr));
+        CK(cudaMemcpyAsync(sk + 2 * n3, defp, f, cudaMemcpyDeviceToDevice, c->s));
+      } else {
+        // the last iteration of the segment needs only its defp
+        int st = calcdefp_dev(c, 1.0, 1.0, nullptr, nullptr, nullptr, nullptr);
+        if (st != MMH_OK) return st;
+        CK(cudaMemcpyAsync(sk + 2 * n3, defp, f, cudaMemcpyDeviceToDevice, c->s));
+      }
+    }
+    for (int k = k1 - 1; k >= k0; --k) {
+      const double* sk = segst + 3 * (i64)(k - k0) * n3;
+      // relaxing: rho_{k+1} = relaxing(rho_k, def_{k+1}, defp_k)
+      CK(cudaMemcpyAsync(c->def, sk, f, cudaMemcpyDeviceToDevice, c->s));
+      launch_add(c->def, sk + 2 * n3, n3, c->s);
+      CK(cudaMemcpyAsync(c->rho, sk + n3, f, cudaMemcpyDeviceToDevice, c->s));
+      CK(cudaMemcpyAsync(defp, sk + 2 * n3, f, cudaMemcpyDeviceToDevice, c->s));
+      RET(relaxing_adjoint_dev(c, 1.0, rbar, rbar2, ga, gb));
+      std::swap(rbar, rbar2);
+      // def_{k+1} = def_k + defp_k: defbar_k = defbar_{k+1} + relaxing's part,
+      // defpbar_k = the same + relaxing's defp part
+      launch_add(dbar, ga, n3, c->s);
+      launch_add(gb, dbar, n3, c->s);
+      // calcdefp: defp_k = calcdefp(def_k, rho_k)
+      CK(cudaMemcpyAsync(c->def, sk, f, cudaMemcpyDeviceToDevice, c->s));
+      RET(calcdefp_adjoint_dev(c, 1.0, 1.0, gb, gc, gd, nullptr));
+      launch_add(rbar, gc, n3, c->s);
+      launch_add(dbar, gd, n3, c->s);
+    }
+  }
+  CK(cudaMemcpyAsync(grho, rbar, f, cudaMemcpyDeviceToDevice, c->s));
+  if (gdef) CK(cudaMemcpyAsync(gdef, dbar, f, cudaMemcpyDeviceToDevice, c->s));
+  CK(cudaMemcpyAsync(c->def, fin, f, cudaMemcpyDeviceToDevice, c->s));
+  CK(cudaMemcpyAsync(c->rho, fin + n3, f, cudaMemcpyDeviceToDevice, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  CK(cudaGetLastError());
   return MMH_OK;
 }
 
@@ -1212,6 +1319,26 @@ int mmh_relaxing_adjoint_f64(mmh_ctx* c, const double* u, const double* def, con
   RET(download(c, dw + n3, gu, n3));
   if (gdef) RET(download(c, dw + 2 * n3, gdef, n3));
   if (gdefp) RET(download(c, dw + 3 * n3, gdefp, n3));
+  return MMH_OK;
+}
+int mmh_iterate_adjoint_f64(mmh_ctx* c, int niter, int checkpoint_every, const double* wdef, const double* wdelta,
+                            double* grho, double* gdef, mmh_diag* d) {
+  if (!c || !grho) return MMH_ERR_ARG;
+  i64 n3 = c->n3;
+  DevTemp buf;
+  buf.s = c->s;
+  if (cudaMallocAsync(&buf.p, sizeof(double) * 4 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
+  double* dw = (double*)buf.p;
+  if (wdef) RET(upload(c, wdef, dw, n3));
+  if (wdelta) RET(upload(c, wdelta, dw + n3, n3));
+  mmh_diag dd{};
+  int st = iterate_adjoint_dev(c, niter, checkpoint_every, wdef ? dw : nullptr, wdelta ? dw + n3 : nullptr, dw + 2 * n3,
+                               gdef ? dw + 3 * n3 : nullptr, &dd);
+  dd.status = st;
+  if (d) *d = dd;
+  RET(st);
+  RET(download(c, dw + 2 * n3, grho, n3));
+  if (gdef) RET(download(c, dw + 3 * n3, gdef, n3));
   return MMH_OK;
 }
 int mmh_multigrid(mmh_ctx* c, float* u, float* rhs, const float* defpot, const float* ubig, float dx, int nx, int ny,

@@ -40,7 +40,7 @@ EXPORTS = (
     "mmh_limiter_poisson_f64", "mmh_load_f64", "mmh_load_dev", "mmh_iterate", "mmh_store_f64",
     "mmh_outputs_f64", "mmh_outputs_dev", "mmh_state_dev", "mmh_profile_start", "mmh_profile_stop",
     "mmh_relax_noalloc_f64", "mmh_batch_run", "mmh_calcdefp_adjoint_f64",
-    "mmh_relaxing_adjoint_f64",
+    "mmh_relaxing_adjoint_f64", "mmh_iterate_adjoint_f64",
 )
 
 # kernel kinds for the timing hooks
@@ -220,6 +220,21 @@ class Context:
         _chk(lib().mmh_relaxing_adjoint_f64(self._h, _p(u), _p(defpot), _p(defp), C.c_double(dt), int(nfluidcmp),
                                             _p(w), _p(g[0]), _p(g[1]), _p(g[2])), "relaxing_adjoint")
         return tuple(g)
+
+    def iterate_adjoint(self, niter, wdef=None, wdelta=None, checkpoint_every=4):
+        """niter iterations from the loaded state, then the gradients of
+        sum(wdef * def_N) + sum(wdelta * defp2delta(def_N)) with respect to the
+        loaded density and def.  Returns (grho, gdef, diag)."""
+        for a in (wdef, wdelta):
+            if a is not None:
+                _farr(a, np.float64)
+        shape = (self.n,) * 3
+        grho = np.zeros(shape, dtype=np.float64, order="F")
+        gdef = np.zeros(shape, dtype=np.float64, order="F")
+        d = Diag()
+        _chk(lib().mmh_iterate_adjoint_f64(self._h, int(niter), int(checkpoint_every), _p(wdef), _p(wdelta),
+                                           _p(grho), _p(gdef), C.byref(d)), "iterate_adjoint")
+        return grho, gdef, d.as_dict()
 
     def multigrid(self, u, rhs, defpot, ubig, dx, nx, ny, nz, nu, nred=1, iopt=2):
         """multigrid(u,rhs,defpot,ubig,dx,nx,ny,nz,nu,nred,iopt)  (mmh/multigrid.f90:16)."""

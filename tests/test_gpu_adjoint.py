@@ -164,8 +164,11 @@ def test_relaxing_adjoint_matches_finite_differences(mmh, fields):
             checks.append(("rho", gu, np.asfortranarray(_s3(rng.standard_normal((n, n, n))))))
             checks.append(("def", gdef, smooth_field(n, amp, 40 + q)))
             checks.append(("defp", gdefp, smooth_field(n, amp, 50 + q)))
+        # The map is piecewise smooth (cflkeuler's maximum and the minmod
+        # branches switch at kinks; at 16^3 some lie ~1e-5 away in these
+        # directions), so the steps are small enough to stay on one piece.
         for name, g, v in checks:
-            h = 1e-6 / max(np.abs(v).max(), 1e-300)
+            h = 1e-7 / max(np.abs(v).max(), 1e-300)
             args_p = [rho, defpot, defp]
             args_m = [rho, defpot, defp]
             k = ("rho", "def", "defp").index(name)
