@@ -176,5 +176,10 @@ def test_relaxing_adjoint_matches_finite_differences(mmh, fields):
             args_m[k] = args_m[k] - h * v
             fd = (J(*args_p) - J(*args_m)) / (2 * h)
             ad = float(np.sum(g * v))
-            print(f"relaxing d/d{name}: fd {fd:.12e} adjoint {ad:.12e} rel {abs(fd - ad) / abs(ad):.2e}")
-            assert abs(fd - ad) <= 1e-6 * abs(ad), (name, fd, ad)
+            # bound relative to the summed per-cell contributions: in some def
+            # directions the derivative is a cancellation of many cells and
+            # the differences' round-off (~1e-14 / h) dominates |ad|
+            scale = float(np.sum(np.abs(g * v)))
+            print(f"relaxing d/d{name}: fd {fd:.12e} adjoint {ad:.12e} rel {abs(fd - ad) / abs(ad):.2e} "
+                  f"of sum {abs(fd - ad) / scale:.2e}")
+            assert abs(fd - ad) <= 1e-6 * max(abs(ad), scale), (name, fd, ad)
