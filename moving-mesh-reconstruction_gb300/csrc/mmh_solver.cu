@@ -684,61 +684,70 @@ struct DevTemp {
   }
 };
 
-// Gradients of J = w^T defp with respect to the density and to def for one
-// calcdefp increment on the resident def and rho (no counterpart in the
-// reference).  The limiter's branch choices are those of this forward pass;
-// calls whose final compression test limits a cell return
-// MMH_ERR_UNSUPPORTED (that correction is not transposed).  w (device, n^3)
-// is overwritten; grho and gdef (device, n^3, either may be null) receive the
-// gradients.  defp is defined up to a constant, so the gradients are those of
-// w minus its mean.
-int calcdefp_adjoint_dev(mmh_ctx* c, double dtold, double dtaumesh, double* w, double* grho, double* gdef,
-                         mmh_diag* d) {
-  if (c->cfg.schedule == MMH_SCHED_REF) return MMH_ERR_UNSUPPORTED;  // one V-cycle is no solve
+// What the calcdefp adjoint needs from its forward pass: the pass-1 input
+// S^3 g, the expansion and compression masks (2 n^3 bytes), the solution
+// before the last two smoothings and the rgzerosum ratio sum(b) / sum(det).
+struct CalcKeep {
+  double* pre;
+  double* uf;
+  uint8_t* mk;
+  double* ratio;
+};
+
+// calcdefp_dev on the resident def and rho, keeping what the adjoint needs.
+// MMH_ERR_UNSUPPORTED when the final compression test limits a cell (that
+// correction is not transposed); defp is then not corrected either.
+int calcdefp_fwd_keep(mmh_ctx* c, double dtold, double dtaumesh, const CalcKeep& kp, mmh_diag* d) {
   int n = c->n;
   i64 n3 = c->n3;
   if (dtold < 1.e-8) dtold = 1.0;
-  DevTemp buf;
-  buf.s = c->s;
-  if (cudaMallocAsync(&buf.p, sizeof(double) * (9 * n3 + 1) + 2 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
-  double* pre = (double*)buf.p;  // pass-1 input S^3 g
-  double* uf = pre + n3;         // forward solution before the last two smoothings
-  double* y = uf + n3;
-  double* cf = y + n3;           // C_f = cof/det, or the adjoint of A = I + Hess(def); 6 n^3
-  double* rslot = cf + 6 * n3;   // the forward rgzerosum ratio sum(b) / sum(det)
-  uint8_t* mk = (uint8_t*)(rslot + 1);
   double* tmp = c->tmp();
   double* defp = c->defp();
-  // forward pass (calcdefp_dev), keeping the pass-1 input, masks and solution
   launch_calcdefp_rhs(tmp, c->rho, n, dtold, c->s);
   launch_smooth27<double>(tmp, n, c->scr, c->s);
   launch_smooth27<double>(c->scr, n, tmp, c->s);
   launch_smooth27<double>(tmp, n, c->scr, c->s);
-  CK(cudaMemcpyAsync(pre, c->scr, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  CK(cudaMemcpyAsync(kp.pre, c->scr, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
   launch_lim_reset(&c->sc->lim, c->s);
-  launch_limiter_pass1(c->scr, c->def, c->rho, n, dtold, dtaumesh, &c->sc->lim, mk, mk + n3, c->s);
+  launch_limiter_pass1(c->scr, c->def, c->rho, n, dtold, dtaumesh, &c->sc->lim, kp.mk, kp.mk + n3, c->s);
   launch_smooth27<double>(c->scr, n, tmp, c->s);
   launch_fill<double>(defp, n3, 0.0, c->s);
   int st = multigrid_level(c, 0, 1.0, d);
   if (st != MMH_OK) return st;
-  CK(cudaMemcpyAsync(rslot, &c->sc->ratio, sizeof(double), cudaMemcpyDeviceToDevice, c->s));
-  CK(cudaMemcpyAsync(uf, defp, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  CK(cudaMemcpyAsync(kp.ratio, &c->sc->ratio, sizeof(double), cudaMemcpyDeviceToDevice, c->s));
+  CK(cudaMemcpyAsync(kp.uf, defp, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
   launch_smooth27<double>(defp, n, c->scr, c->s);
   launch_smooth27<double>(c->scr, n, defp, c->s);
   launch_limiter_mask(c->defplim, c->def, defp, n, dtold, &c->sc->lim, nullptr, c->s);
   RET(pull_scal(c));
   lim_to_diag(c->hsc->lim, d);
   if (c->hsc->lim.ncompress) return MMH_ERR_UNSUPPORTED;
-  // adjoint solve L lam = S^2 w - mean (L symmetric)
+  return MMH_OK;
+}
+
+// The adjoint half: gradients of J = w^T defp with respect to the density
+// and to def (grho, gdef: device n^3, either may be null) on the resident
+// def and rho of the forward pass kp was kept from.  scratch: 8 n^3.
+//   dJ/drho = g' . S^3 (D . S y) - B27( sum_f C_f G_f(lam, u) ),
+//   dJ/ddef = Hess^T( d/dA [ - sum_f urg G_f C_f(A) - r y det(A) ] ),
+// y = P^T lam = lam - (det^T lam) / sum det, L lam = S^2 w - mean (L symmetric).
+int calcdefp_adj_core(mmh_ctx* c, double dtold, double dtaumesh, const CalcKeep& kp, const double* w, double* grho,
+                      double* gdef, double* scratch, mmh_diag* da) {
+  int n = c->n;
+  i64 n3 = c->n3;
+  if (dtold < 1.e-8) dtold = 1.0;
+  double* cf = scratch;    // C_f or the adjoint of A; 6 n^3
+  double* y = cf + 6 * n3;
+  double* z = y + n3;
+  double* tmp = c->tmp();
+  double* defp = c->defp();
   launch_smooth27<double>(w, n, c->scr, c->s);
   launch_smooth27<double>(c->scr, n, tmp, c->s);
   RET(zerosum<double>(c, tmp, n3));
   launch_fill<double>(defp, n3, 0.0, c->s);
-  mmh_diag da{};
-  st = multigrid_level(c, 0, 1.0, &da);
+  int st = multigrid_level(c, 0, 1.0, da);
   if (st != MMH_OK) return st;
   const double* lam = defp;
-  // y = P^T lam = lam - (det^T lam) / sum det
   launch_det<double>(c->def, n, 1.0, c->det, c->s);
   launch_adj_mul(c->det, lam, y, n3, c->s);
   CK(cudaMemsetAsync(c->sc->acc[0], 0, 32, c->s));
@@ -748,28 +757,50 @@ int calcdefp_adjoint_dev(mmh_ctx* c, double dtold, double dtaumesh, double* w, d
   CK(cudaMemcpyAsync(y, lam, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
   launch_sub_mean<double>(y, n3, &c->sc->ratio, c->s);
   if (gdef) {
-    // def enters through C_f(A) and the rgzerosum weights det(A), A = I + Hess(def)
-    launch_box27(c->rho, n, c->scr, c->s);
-    launch_adj_metric(c->def, lam, uf, c->scr, y, rslot, n, cf, c->s);
+    launch_box27(c->rho, n, z, c->s);
+    launch_adj_metric(c->def, lam, kp.uf, z, y, kp.ratio, n, cf, c->s);
     launch_adj_hess(cf, n, gdef, 0, c->s);
   }
   if (grho) {
-    // right-hand-side path: g' . S^3 (D . S y)
     launch_smooth27<double>(y, n, c->scr, c->s);
-    launch_adj_pass1(c->scr, pre, mk, mk + n3, dtaumesh, n3, c->s);
+    launch_adj_pass1(c->scr, kp.pre, kp.mk, kp.mk + n3, dtaumesh, n3, c->s);
     launch_smooth27<double>(c->scr, n, y, c->s);
     launch_smooth27<double>(y, n, c->scr, c->s);
     launch_smooth27<double>(c->scr, n, y, c->s);
     launch_adj_rhs(y, c->rho, dtold, n3, c->s);
-    // operator path: - B27( sum_f C_f G_f(lam, u) ), C_f from the metric of a unit density
-    launch_fill<double>(pre, n3, 1.0, c->s);
-    launch_metric<double>(c->def, pre, n, 1.0, cf, c->s);
-    launch_adj_contract(lam, uf, cf, n, c->scr, c->s);
-    launch_box27(c->scr, n, pre, c->s);
-    launch_adj_sub(y, pre, grho, n3, c->s);
+    launch_fill<double>(z, n3, 1.0, c->s);
+    launch_metric<double>(c->def, z, n, 1.0, cf, c->s);
+    launch_adj_contract(lam, kp.uf, cf, n, c->scr, c->s);
+    launch_box27(c->scr, n, z, c->s);
+    launch_adj_sub(y, z, grho, n3, c->s);
   }
   RET(pull_scal(c));
   if (c->hsc->bad) return MMH_ERR_RANGE;
+  return MMH_OK;
+}
+
+// Gradients of J = w^T defp with respect to the density and to def for one
+// calcdefp increment on the resident def and rho (no counterpart in the
+// reference), the limiter's branch choices those of this forward pass.  w
+// (device, n^3) is read; grho and gdef (device, n^3, either may be null)
+// receive the gradients.  defp is defined up to a constant, so the gradients
+// are those of w minus its mean.
+int calcdefp_adjoint_dev(mmh_ctx* c, double dtold, double dtaumesh, const double* w, double* grho, double* gdef,
+                         mmh_diag* d) {
+  if (c->cfg.schedule == MMH_SCHED_REF) return MMH_ERR_UNSUPPORTED;  // one V-cycle is no solve
+  i64 n3 = c->n3;
+  DevTemp buf;
+  buf.s = c->s;
+  if (cudaMallocAsync(&buf.p, sizeof(double) * (10 * n3 + 1) + 2 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
+  double* scratch = (double*)buf.p;  // 8 n^3
+  CalcKeep kp;
+  kp.pre = scratch + 8 * n3;
+  kp.uf = kp.pre + n3;
+  kp.ratio = kp.uf + n3;
+  kp.mk = (uint8_t*)(kp.ratio + 1);
+  RET(calcdefp_fwd_keep(c, dtold, dtaumesh, kp, d));
+  mmh_diag da{};
+  RET(calcdefp_adj_core(c, dtold, dtaumesh, kp, w, grho, gdef, scratch, &da));
   if (d) d->vcycles += da.vcycles;
   return MMH_OK;
 }
@@ -779,40 +810,42 @@ int calcdefp_adjoint_dev(mmh_ctx* c, double dtold, double dtaumesh, double* w, d
 // minmod slopes and the cflkeuler maximum frozen where the forward pass took
 // them: gu, gdef, gdefp (device, n^3; gdef and gdefp may be null) receive the
 // gradients with respect to the density, def and defp.  ubar (device) is read.
-int relaxing_adjoint_dev(mmh_ctx* c, double dt, const double* ubar, double* gu, double* gdef, double* gdefp) {
+// The forward buffers are relaxing_dev's (the context's shared scratch);
+// `scratch` (15 n^3, null: allocated here) holds the rest.
+int relaxing_adjoint_dev(mmh_ctx* c, double dt, const double* ubar, double* gu, double* gdef, double* gdefp,
+                         double* scratch) {
   int n = c->n;
   i64 n3 = c->n3;
   DevTemp buf;
   buf.s = c->s;
-  if (cudaMallocAsync(&buf.p, sizeof(double) * 33 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
-  double* baj = (double*)buf.p;  // 7 planes
-  double* cc = baj + 7 * n3;
-  double* sd0 = cc + n3;         // half sums and differences at u (6 planes)
-  double* sd1 = sd0 + 6 * n3;    // ... at the half step (6 planes)
-  double* gface = sd1 + 6 * n3;  // 3 planes
-  double* u1 = gface + 3 * n3;
-  double* alpha = u1 + n3;       // 3 planes
+  if (!scratch) {
+    if (cudaMallocAsync(&buf.p, sizeof(double) * 15 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
+    scratch = (double*)buf.p;
+  }
+  double* sd0 = c->vt;            // half sums and differences at u (6 planes)
+  double* sd1 = scratch;          // ... at the half step (6 planes)
+  double* alpha = sd1 + 6 * n3;   // 3 planes
   double* alphabar = alpha + 3 * n3;
   double* cbar = alphabar + 3 * n3;
   double* u1bar = cbar + n3;
   double* xbar = u1bar + n3;
   double* defp = c->defp();
   // forward pass (relaxing_dev) with both stages' half sums kept
-  launch_relax_stage1(c->rho, c->def, defp, n, baj, cc, sd0, c->s);
-  launch_adj_alpha(baj, defp, cc, n, alpha, c->s);
-  launch_relax_dpv(sd0, cc, n, c->rho, dt / 2.0, u1, gface, c->s);
-  launch_relax_flux(u1, defp, baj, cc, n, sd1, c->s);
+  launch_relax_stage1(c->rho, c->def, defp, n, c->baj, c->cc, sd0, c->s);
+  launch_adj_alpha(c->baj, defp, c->cc, n, alpha, c->s);
+  launch_relax_dpv(sd0, c->cc, n, c->rho, dt / 2.0, c->u1, c->gface, c->s);
+  launch_relax_flux(c->u1, defp, c->baj, c->cc, n, sd1, c->s);
   // stage 2 (u' = u - dt R(u1)), then stage 1 (u1 = u - dt/2 R(u))
   CK(cudaMemsetAsync(alphabar, 0, sizeof(double) * 4 * n3, c->s));
-  launch_adj_dpv(sd1, cc, alpha, u1, ubar, -dt, n, u1bar, alphabar, cbar, c->s);
-  launch_adj_dpv(sd0, cc, alpha, c->rho, u1bar, -dt / 2.0, n, xbar, alphabar, cbar, c->s);
+  launch_adj_dpv(sd1, c->cc, alpha, c->u1, ubar, -dt, n, u1bar, alphabar, cbar, c->s);
+  launch_adj_dpv(sd0, c->cc, alpha, c->rho, u1bar, -dt / 2.0, n, xbar, alphabar, cbar, c->s);
   CK(cudaMemcpyAsync(gu, ubar, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
   launch_add(gu, u1bar, n3, c->s);
   launch_add(gu, xbar, n3, c->s);
-  // the flux ratios and speeds back to def and defp (sd0, sd1 are free)
+  // the flux ratios and speeds back to def and defp (sd0 and sd1 are free)
   double* abar = sd0;
   double* pdbar = sd1;
-  launch_adj_relax_geom(c->def, defp, cc, alphabar, cbar, n, abar, pdbar, c->s);
+  launch_adj_relax_geom(c->def, defp, c->cc, alphabar, cbar, n, abar, pdbar, c->s);
   if (gdef) launch_adj_hess(abar, n, gdef, 0, c->s);
   if (gdefp) launch_adj_grad_t(pdbar, n, gdefp, 0, c->s);
   CK(cudaGetLastError());
@@ -836,13 +869,15 @@ int iterate_adjoint_dev(mmh_ctx* c, int niter, int every, const double* wdef, co
   const int seg = std::min(every, std::max(niter, 1));
   DevTemp buf;
   buf.s = c->s;
-  // checkpoints (def, rho) | segment states (def, rho, defp) | final state |
-  // rhobar, rhobar_next, defbar, and four gradient parts
-  const i64 words = (2 * (i64)ncp + 3 * (i64)seg + 2 + 7) * n3;
+  // checkpoints (def, rho) | per segment iteration: def, rho, defp and the
+  // calcdefp forward's pre, uf | final state | rhobar, rhobar_next, defbar,
+  // four gradient parts | adjoint scratch (15: relaxing's, or calcdefp's 8) |
+  // segment ratios and masks
+  const i64 words = (2 * (i64)ncp + 5 * (i64)seg + 2 + 7 + 15) * n3 + seg + (2 * (i64)seg * n3 + 7) / 8;
   if (cudaMallocAsync(&buf.p, sizeof(double) * words, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
   double* ckpt = (double*)buf.p;
   double* segst = ckpt + 2 * (i64)ncp * n3;
-  double* fin = segst + 3 * (i64)seg * n3;
+  double* fin = segst + 5 * (i64)seg * n3;
   double* rbar = fin + 2 * n3;
   double* rbar2 = rbar + n3;
   double* dbar = rbar2 + n3;
@@ -850,12 +885,18 @@ int iterate_adjoint_dev(mmh_ctx* c, int niter, int every, const double* wdef, co
   double* gb = ga + n3;
   double* gc = gb + n3;
   double* gd = gc + n3;
+  double* scratch = gd + n3;
+  double* ratios = scratch + 15 * n3;
+  uint8_t* masks = (uint8_t*)(ratios + seg);
   double* defp = c->defp();
-  auto step = [&](mmh_diag* dd) -> int {
-    int st = calcdefp_dev(c, 1.0, 1.0, nullptr, nullptr, nullptr, dd);
-    if (st != MMH_OK) return st;
-    launch_add(c->def, defp, n3, c->s);
-    return relaxing_dev(c, 1.0);
+  auto keep = [&](int q) {
+    CalcKeep kp;
+    double* sk = segst + 5 * (i64)q * n3;
+    kp.pre = sk + 3 * n3;
+    kp.uf = sk + 4 * n3;
+    kp.ratio = ratios + q;
+    kp.mk = masks + 2 * (i64)q * n3;
+    return kp;
   };
   // forward pass with checkpoints
   for (int k = 0; k < niter; ++k) {
@@ -864,7 +905,11 @@ int iterate_adjoint_dev(mmh_ctx* c, int niter, int every, const double* wdef, co
       CK(cudaMemcpyAsync(ckpt + (2 * (i64)(k / every) + 1) * n3, c->rho, f, cudaMemcpyDeviceToDevice, c->s));
     }
     mmh_diag dd{};
-    RET(step(&dd));
+    int st = calcdefp_dev(c, 1.0, 1.0, nullptr, nullptr, nullptr, &dd);
+    if (st != MMH_OK) return st;
+    if (dd.ncompress) return MMH_ERR_UNSUPPORTED;
+    launch_add(c->def, defp, n3, c->s);
+    RET(relaxing_dev(c, 1.0));
     if (d) *d = dd;
   }
   CK(cudaMemcpyAsync(fin, c->def, f, cudaMemcpyDeviceToDevice, c->s));
@@ -881,30 +926,28 @@ int iterate_adjoint_dev(mmh_ctx* c, int niter, int every, const double* wdef, co
   }
   for (int s = ncp - 1; s >= 0; --s) {
     const int k0 = s * every, k1 = std::min(k0 + every, niter);
+    // recompute the segment, keeping each iteration's state and calcdefp data
     CK(cudaMemcpyAsync(c->def, ckpt + 2 * (i64)s * n3, f, cudaMemcpyDeviceToDevice, c->s));
     CK(cudaMemcpyAsync(c->rho, ckpt + (2 * (i64)s + 1) * n3, f, cudaMemcpyDeviceToDevice, c->s));
     for (int k = k0; k < k1; ++k) {
-      double* sk = segst + 3 * (i64)(k - k0) * n3;
+      double* sk = segst + 5 * (i64)(k - k0) * n3;
       CK(cudaMemcpyAsync(sk, c->def, f, cudaMemcpyDeviceToDevice, c->s));
       CK(cudaMemcpyAsync(sk + n3, c->rho, f, cudaMemcpyDeviceToDevice, c->s));
+      RET(calcdefp_fwd_keep(c, 1.0, 1.0, keep(k - k0), nullptr));
+      CK(cudaMemcpyAsync(sk + 2 * n3, defp, f, cudaMemcpyDeviceToDevice, c->s));
       if (k + 1 < k1) {
-        RET(step(nullptr));
-        CK(cudaMemcpyAsync(sk + 2 * n3, defp, f, cudaMemcpyDeviceToDevice, c->s));
-      } else {
-        // the last iteration of the segment needs only its defp
-        int st = calcdefp_dev(c, 1.0, 1.0, nullptr, nullptr, nullptr, nullptr);
-        if (st != MMH_OK) return st;
-        CK(cudaMemcpyAsync(sk + 2 * n3, defp, f, cudaMemcpyDeviceToDevice, c->s));
+        launch_add(c->def, defp, n3, c->s);
+        RET(relaxing_dev(c, 1.0));
       }
     }
     for (int k = k1 - 1; k >= k0; --k) {
-      const double* sk = segst + 3 * (i64)(k - k0) * n3;
+      const double* sk = segst + 5 * (i64)(k - k0) * n3;
       // relaxing: rho_{k+1} = relaxing(rho_k, def_{k+1}, defp_k)
       CK(cudaMemcpyAsync(c->def, sk, f, cudaMemcpyDeviceToDevice, c->s));
       launch_add(c->def, sk + 2 * n3, n3, c->s);
       CK(cudaMemcpyAsync(c->rho, sk + n3, f, cudaMemcpyDeviceToDevice, c->s));
       CK(cudaMemcpyAsync(defp, sk + 2 * n3, f, cudaMemcpyDeviceToDevice, c->s));
-      RET(relaxing_adjoint_dev(c, 1.0, rbar, rbar2, ga, gb));
+      RET(relaxing_adjoint_dev(c, 1.0, rbar, rbar2, ga, gb, scratch));
       std::swap(rbar, rbar2);
       // def_{k+1} = def_k + defp_k: defbar_k = defbar_{k+1} + relaxing's part,
       // defpbar_k = the same + relaxing's defp part
@@ -912,7 +955,7 @@ int iterate_adjoint_dev(mmh_ctx* c, int niter, int every, const double* wdef, co
       launch_add(gb, dbar, n3, c->s);
       // calcdefp: defp_k = calcdefp(def_k, rho_k)
       CK(cudaMemcpyAsync(c->def, sk, f, cudaMemcpyDeviceToDevice, c->s));
-      RET(calcdefp_adjoint_dev(c, 1.0, 1.0, gb, gc, gd, nullptr));
+      RET(calcdefp_adj_core(c, 1.0, 1.0, keep(k - k0), gb, gc, gd, scratch, nullptr));
       launch_add(rbar, gc, n3, c->s);
       launch_add(dbar, gd, n3, c->s);
     }
@@ -1315,7 +1358,7 @@ int mmh_relaxing_adjoint_f64(mmh_ctx* c, const double* u, const double* def, con
   if (cudaMallocAsync(&buf.p, sizeof(double) * 4 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
   double* dw = (double*)buf.p;
   RET(upload(c, w, dw, n3));
-  RET(relaxing_adjoint_dev(c, dt, dw, dw + n3, gdef ? dw + 2 * n3 : nullptr, gdefp ? dw + 3 * n3 : nullptr));
+  RET(relaxing_adjoint_dev(c, dt, dw, dw + n3, gdef ? dw + 2 * n3 : nullptr, gdefp ? dw + 3 * n3 : nullptr, nullptr));
   RET(download(c, dw + n3, gu, n3));
   if (gdef) RET(download(c, dw + 2 * n3, gdef, n3));
   if (gdefp) RET(download(c, dw + 3 * n3, gdefp, n3));
