@@ -1,0 +1,84 @@
+"""The adjoint at full size (opt-in: MMH_TEST_C5=1; MMH_C5_DIRS directions,
+default 64): a 256^3 lognormal density, 20 deformation iterations with the
+forward states kept every 4, the loss sum_b w_b P_b of the reconstructed
+density's power in 16 log-spaced |k| bands (seeded weights), its gradient
+with respect to the input density from mmh_iterate_adjoint_f64 against central
+finite differences of the loss in smooth random directions.
+
+FP64 solves to 1e-11: the finite differences need a forward map that is
+smooth at the step (1e-7 of the direction's maximum), which the FP32 inner
+solves of the mixed form are not."""
+import os
+import time
+
+import numpy as np
+import pytest
+
+from conftest import smooth_field
+
+pytestmark = pytest.mark.skipif(os.environ.get("MMH_TEST_C5") != "1", reason="256^3 adjoint: set MMH_TEST_C5=1")
+
+
+def band_weights(n, seed):
+    """W(k): seeded weight of the band of |k| (16 log-spaced bands between 1
+    and sqrt(3) n / 2), 0 at k = 0."""
+    k = np.fft.fftfreq(n, d=1.0 / n)
+    kk = np.sqrt(k[:, None, None] ** 2 + k[None, :, None] ** 2 + k[None, None, :] ** 2)
+    edges = np.logspace(0.0, np.log10(np.sqrt(3.0) * n / 2 + 1e-9), 17)
+    band = np.searchsorted(edges, kk, side="right") - 1
+    w = np.random.default_rng(seed).uniform(0.5, 1.5, 16)
+    return np.where((band >= 0) & (band < 16), w[np.clip(band, 0, 15)], 0.0)
+
+
+def band_loss(delta, W):
+    """loss and d loss / d delta for loss = sum_k W(k) |fft(delta)(k)|^2 / n^3."""
+    n = delta.shape[0]
+    F = np.fft.fftn(delta)
+    loss = float(np.sum(W * np.abs(F) ** 2)) / n ** 3
+    seed = 2.0 * np.real(np.fft.ifftn(W * F))
+    return loss, np.asfortranarray(seed)
+
+
+@pytest.mark.gpu
+def test_c5_adjoint_256(mmh, fields):
+    n, niter, every = 256, 20, 4
+    ndirs = int(os.environ.get("MMH_C5_DIRS", "64"))
+    rho0 = fields.lognormal_density(n, sigma=0.5, seed=5)
+    W = band_weights(n, 55)
+    z = np.zeros((n, n, n), order="F")
+
+    def u_of(r):
+        u = np.zeros((5, n, n, n), order="F")
+        u[0] = r
+        return u
+
+    with mmh.Context(n, precision=mmh.MMH_FP64, schedule=mmh.MMH_SCHED_TOL, tol=1e-11, max_cycles=400) as ctx:
+
+        def forward(r):
+            ctx.load(z, u_of(r))
+            d = ctx.iterate(niter)
+            assert d["status"] == 0 and d["ncompress"] == 0
+            delta = np.zeros((n, n, n), order="F")
+            ctx.outputs(None, delta)
+            return delta
+
+        t0 = time.perf_counter()
+        loss, seed = band_loss(forward(rho0), W)
+        t_fwd = time.perf_counter() - t0
+        ctx.load(z, u_of(rho0))
+        t0 = time.perf_counter()
+        grho, _, _ = ctx.iterate_adjoint(niter, wdelta=seed, checkpoint_every=every)
+        t_adj = time.perf_counter() - t0
+        print(f"C5 256^3: loss {loss:.10e}; forward {t_fwd:.2f} s, forward+adjoint {t_adj:.2f} s")
+
+        worst = 0.0
+        for q in range(ndirs):
+            v = smooth_field(n, 1.0, 1000 + q)
+            h = 1e-7 / np.abs(v).max()
+            fd = (band_loss(forward(rho0 + h * v), W)[0] - band_loss(forward(rho0 - h * v), W)[0]) / (2 * h)
+            ad = float(np.sum(grho * v))
+            rel = abs(fd - ad) / abs(ad)
+            worst = max(worst, rel)
+            print(f"  direction {q}: fd {fd:.12e} adjoint {ad:.12e} rel {rel:.2e}", flush=True)
+        print(f"C5 worst relative difference over {ndirs} directions: {worst:.2e}")
+        assert worst <= 1e-6

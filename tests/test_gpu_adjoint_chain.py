@@ -118,3 +118,20 @@ def test_autograd_function_band_power_gradient(mmh, fields):
             ad = float(np.sum(grad * v))
             print(f"band loss: fd {fd:.12e} adjoint {ad:.12e} rel {abs(fd - ad) / abs(ad):.2e}")
             assert abs(fd - ad) <= 1e-6 * abs(ad), (fd, ad)
+
+
+@pytest.mark.gpu
+def test_iterate_adjoint_mixed_matches_fp64(mmh, fields):
+    """The mixed form's gradient (FP32 inner solves, FP64 residual to tol)
+    against the FP64 form's on the same reconstruction."""
+    n, niter = N, 4
+    rho = fields.lognormal_density(n, sigma=0.6, seed=63)
+    wdelta = np.asfortranarray(np.random.default_rng(64).standard_normal((n, n, n)))
+    g = {}
+    for prec in (mmh.MMH_FP64, mmh.MMH_MIXED):
+        with mmh.Context(n, precision=prec, schedule=mmh.MMH_SCHED_TOL, tol=1e-12, max_cycles=400) as ctx:
+            ctx.load(np.zeros((n, n, n), order="F"), _u(rho))
+            g[prec], _, _ = ctx.iterate_adjoint(niter, wdelta=wdelta, checkpoint_every=3)
+    err = np.abs(g[mmh.MMH_MIXED] - g[mmh.MMH_FP64]).max() / np.abs(g[mmh.MMH_FP64]).max()
+    print(f"mixed vs FP64 gradient: {err:.2e}")
+    assert err <= 1e-8
