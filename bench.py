@@ -21,6 +21,9 @@ is one such reconstruction; the metric is seconds per reconstruction.
             measured HBM copy bandwidth.
   cpu_baseline: the CPU oracle (FP64, all host threads) on a bounded sample.
 
+--batch and --adjoint print the batched-realisation line and the adjoint
+line (the density gradient of a band-power loss at 256^3) instead.
+
 Multi-GPU: independent reconstructions, one per rank (replicas; the path has
 no exchange step).  --impl reference times the CPU restatement of the
 reference (the Fortran reference has no compiler on this image).
@@ -75,6 +78,10 @@ def parse():
     ap.add_argument("--profile", default="gs32", choices=["gs32", "gs64", "res64", "res32", "none"])
     ap.add_argument("--batch", action="store_true",
                     help="batched-realisations workload (mmh_batch_run) instead of the headline reconstruction")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="print the C5 adjoint line instead (256^3 density gradient of a band-power loss)")
+    ap.add_argument("--adj-n", type=int, default=256)
+    ap.add_argument("--adj-tol", type=float, default=1e-10)
     ap.add_argument("--batch-workers", type=int, default=8)
     ap.add_argument("--batch-niter", type=int, default=4)
     return ap.parse_args()
@@ -299,12 +306,81 @@ def batch_arm(args):
     return 0
 
 
+def adjoint_arm(args):
+    """C5: the gradient of a band-power loss of the reconstructed density with
+    respect to the input density.  adj_n^3 lognormal field (sigma_lnrho), 20
+    deformation iterations (niter) with the forward states kept every 4, loss
+    sum_b w_b P_b over 16 log-spaced |k| bands with seeded weights; its seed
+    d loss / d delta is formed on the host from one forward run before the
+    timed region.  One step = one mmh_iterate_adjoint_f64 call (checkpointed
+    forward pass + reverse sweep), wall clock around the synchronous call;
+    the forward reconstruction alone is timed the same way for the ratio.
+    Mixed form, and the FP64 form with the gradients' difference."""
+    __import__("importlib").import_module(PKG)
+    import mmh
+    import fields
+    n, niter, every = args.adj_n, args.niter, 4
+    rho = fields.lognormal_density(n, sigma=args.sigma, seed=args.seed)
+    u = np.zeros((5, n, n, n), order="F")
+    u[0] = rho
+    z = np.zeros((n, n, n), order="F")
+    k = np.fft.fftfreq(n, d=1.0 / n)
+    kk = np.sqrt(k[:, None, None] ** 2 + k[None, :, None] ** 2 + k[None, None, :] ** 2)
+    band = np.searchsorted(np.logspace(0.0, np.log10(np.sqrt(3.0) * n / 2 + 1e-9), 17), kk, side="right") - 1
+    wb = np.random.default_rng(args.seed + 1).uniform(0.5, 1.5, 16)
+    W = np.where((band >= 0) & (band < 16), wb[np.clip(band, 0, 15)], 0.0)
+    out, grads = {}, {}
+    for name, prec in (("mixed", mmh.MMH_MIXED), ("fp64", mmh.MMH_FP64)):
+        if name == "fp64" and args.fp64_steps <= 0:
+            continue
+        with mmh.Context(n, precision=prec, schedule=mmh.MMH_SCHED_TOL, tol=args.adj_tol,
+                         max_cycles=args.max_cycles) as ctx:
+            def forward():
+                ctx.load(z, u)
+                ctx.iterate(niter)
+                delta = np.zeros((n, n, n), order="F")
+                ctx.outputs(None, delta)
+                return delta
+            forward()  # warm-up
+            t = time.perf_counter()
+            delta = forward()
+            t_fwd = time.perf_counter() - t
+            F = np.fft.fftn(delta)
+            seed = np.asfortranarray(2.0 * np.real(np.fft.ifftn(W * F)))
+            loss = float(np.sum(W * np.abs(F) ** 2)) / n ** 3
+            times = []
+            for _ in range(max(1, args.steps)):
+                ctx.load(z, u)
+                t = time.perf_counter()
+                g, _, d = ctx.iterate_adjoint(niter, wdelta=seed, checkpoint_every=every)
+                times.append(time.perf_counter() - t)
+            grads[name] = g
+            out[name] = {"gradient_s": statistics.median(times), "forward_s": t_fwd,
+                         "ratio": statistics.median(times) / t_fwd, "loss": loss}
+    line = {
+        "metric": f"s per {n}^3 density gradient of a 16-band power loss (20 iterations, checkpoints every 4)",
+        "value": out["mixed"]["gradient_s"], "unit": "s/gradient", "higher_is_better": False, "n_gpus": 1,
+        "steps": max(1, args.steps), "warmup": 1, "mixed": out["mixed"], "fp64": out.get("fp64"),
+        "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": f"{n}^3 lognormal density, sigma_lnrho {args.sigma}, seed {args.seed}; {niter} "
+                               f"deformation iterations, solves to {args.adj_tol:g}; loss over 16 log-spaced |k| "
+                               f"bands of the reconstructed density", "timing": "wall clock around the host call"},
+    }
+    if "fp64" in grads:
+        line["mixed_vs_fp64_gradient"] = float(np.abs(grads["mixed"] - grads["fp64"]).max()
+                                               / np.abs(grads["fp64"]).max())
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
     if args.batch:
         return batch_arm(args)
+    if args.adjoint:
+        return adjoint_arm(args)
 
     import torch
     __import__("importlib").import_module(PKG)
