@@ -166,6 +166,19 @@ int mmh_outputs_dev(mmh_ctx* ctx, double* d_grad, double* d_delta);
 /* Device pointers of the resident state (n^3 doubles each). */
 int mmh_state_dev(mmh_ctx* ctx, double** d_def, double** d_rho, double** d_defp);
 
+/* The diagnostics main.f90 prints each iteration (main.f90:97-105) and at the
+ * end (main.f90:115-117), from the resident state after mmh_iterate: the mean
+ * and sqrt(mean square) of def and of the last increment defp, the mean of
+ * the density, sqrt(mean (rho-1)^2), its extrema and the count of cells with
+ * rho < 0.  The sums are exact (rounded once); NaN when a term is outside
+ * |x| < 2^32. */
+typedef struct mmh_stats {
+  double def_mean, def_sigma, defp_sigma;
+  double rho_mean, rho_sigma, rho_min, rho_max;
+  long long rho_negative;
+} mmh_stats;
+int mmh_state_stats(mmh_ctx* ctx, mmh_stats* stats);
+
 /* ---- batched realisations (no single call in the reference) ------------ */
 /* One independent reconstruction of mmh/main.f90:83-179: density rho (n^3,
  * Fortran order, host), def = 0, niter deformation iterations, then the

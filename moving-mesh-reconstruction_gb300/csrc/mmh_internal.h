@@ -103,6 +103,17 @@ constexpr int kDotBlocks = 152 * 8;
 void launch_dot_fast(const float* a, const float* b, i64 count, const unsigned long long* abits,
                      const unsigned long long* bbits, unsigned long long* acc, double* part, cudaStream_t s);
 
+// main.f90's iteration diagnostics: exact sums (def, def^2, defp^2, rho,
+// (rho-1)^2), ord_of-encoded extrema of rho, count of rho < 0, range flag
+struct StatsDev {
+  unsigned long long acc[5][2];
+  unsigned long long rmin, rmax, nneg;
+  int flag;
+  int pad;
+};
+void launch_state_stats(const double* def, const double* defp, const double* rho, i64 n3, StatsDev* st,
+                        cudaStream_t s);
+
 // calcdefp adjoint pieces (mmh_adjoint.cu)
 void launch_adj_pass1(double* y, const double* t, const uint8_t* maskx, const uint8_t* maskc, double dtaumesh,
                       i64 n3, cudaStream_t s);

@@ -1,6 +1,7 @@
 // FP64 kernels of the MMH hot path.  Compiled with --fmad=false: every
 // expression rounds as written, so results match the CPU restatement bit for
 // bit (except where a libm function -- acos, cos -- is involved).
+#include <algorithm>
 #include <atomic>
 #include <vector>
 
@@ -393,6 +394,49 @@ __global__ void k_lim_reset(LimDev* st) {
   st->rho2[1] = 0;
   st->flag = 0;
 }
+// Diagnostics of main.f90's iteration loop (main.f90:97-105, 115-117, 181-182):
+// exact sums of def, def^2, defp^2, rho and (rho-1)^2, the extrema of rho and
+// the count of rho < 0.  st is zeroed by the caller except rmin (all ones).
+__global__ void k_state_stats(const double* __restrict__ def, const double* __restrict__ defp,
+                              const double* __restrict__ rho, i64 n3, StatsDev* st) {
+  __int128 s[5] = {0, 0, 0, 0, 0};
+  bool bad = false;
+  unsigned long long neg = 0, omin = ~0ull, omax = 0;
+  for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < n3; t += (i64)gridDim.x * blockDim.x) {
+    double d = def[t], p = defp[t], r = rho[t];
+    double v[5] = {d, d * d, p * p, r, (r - 1.0) * (r - 1.0)};
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      if (!(fabs(v[q]) < 4294967296.0)) bad = true;
+      else s[q] += fx_of(v[q]);
+    }
+    if (r < 0.0) ++neg;
+    unsigned long long o = ord_of(r);
+    omin = o < omin ? o : omin;
+    omax = o > omax ? o : omax;
+  }
+  __shared__ unsigned long long s_buf[32];
+  unsigned long long v;
+  v = block_u64(neg, s_buf, 0);
+  if (threadIdx.x == 0 && v) atomicAdd(&st->nneg, v);
+  v = block_u64(omin, s_buf, 2);
+  if (threadIdx.x == 0) atomicMin(&st->rmin, v);
+  v = block_u64(omax, s_buf, 1);
+  if (threadIdx.x == 0) atomicMax(&st->rmax, v);
+  if (bad) atomicOr(&st->flag, 1);
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    __syncthreads();
+    fx_block_commit(s[q], st->acc[q]);
+  }
+}
+void launch_state_stats(const double* def, const double* defp, const double* rho, i64 n3, StatsDev* st,
+                        cudaStream_t s) {
+  i64 blocks = std::min<i64>((n3 + kBlock - 1) / kBlock, 152 * 8);
+  k_state_stats<<<(unsigned)blocks, kBlock, 0, s>>>(def, defp, rho, n3, st);
+  count_launch();
+}
+
 void launch_lim_reset(LimDev* st, cudaStream_t s) {
   k_lim_reset<<<1, 1, 0, s>>>(st);
   count_launch();

@@ -1384,6 +1384,30 @@ int mmh_iterate_adjoint_f64(mmh_ctx* c, int niter, int checkpoint_every, const d
   if (gdef) RET(download(c, dw + 3 * n3, gdef, n3));
   return MMH_OK;
 }
+int mmh_state_stats(mmh_ctx* c, mmh_stats* out) {
+  if (!c || !out) return MMH_ERR_ARG;
+  StatsDev* st = nullptr;
+  CK(cudaMallocAsync((void**)&st, sizeof(StatsDev), c->s));
+  CK(cudaMemsetAsync(st, 0, sizeof(StatsDev), c->s));
+  CK(cudaMemsetAsync(&st->rmin, 0xff, sizeof(unsigned long long), c->s));
+  launch_state_stats(c->def, c->defp(), c->rho, c->n3, st, c->s);
+  StatsDev h;
+  CK(cudaMemcpyAsync(&h, st, sizeof(StatsDev), cudaMemcpyDeviceToHost, c->s));
+  CK(cudaFreeAsync(st, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  const double n3 = (double)c->n3;
+  double sum[5];
+  for (int q = 0; q < 5; ++q) sum[q] = h.flag ? NAN : fx_host(h.acc[q]);
+  out->def_mean = sum[0] / n3;
+  out->def_sigma = std::sqrt(sum[1] / n3);
+  out->defp_sigma = std::sqrt(sum[2] / n3);
+  out->rho_mean = sum[3] / n3;
+  out->rho_sigma = std::sqrt(sum[4] / n3);
+  out->rho_min = ord_to_double(h.rmin);
+  out->rho_max = ord_to_double(h.rmax);
+  out->rho_negative = (long long)h.nneg;
+  return MMH_OK;
+}
 int mmh_multigrid(mmh_ctx* c, float* u, float* rhs, const float* defpot, const float* ubig, float dx, int nx, int ny,
                   int nz, int nu, int nred, int iopt, mmh_diag* d) {
   return multigrid_host<float>(c, u, rhs, defpot, ubig, dx, nx, ny, nz, nu, nred, iopt, d);

@@ -40,7 +40,7 @@ EXPORTS = (
     "mmh_limiter_poisson_f64", "mmh_load_f64", "mmh_load_dev", "mmh_iterate", "mmh_store_f64",
     "mmh_outputs_f64", "mmh_outputs_dev", "mmh_state_dev", "mmh_profile_start", "mmh_profile_stop",
     "mmh_relax_noalloc_f64", "mmh_batch_run", "mmh_calcdefp_adjoint_f64",
-    "mmh_relaxing_adjoint_f64", "mmh_iterate_adjoint_f64",
+    "mmh_relaxing_adjoint_f64", "mmh_iterate_adjoint_f64", "mmh_state_stats",
 )
 
 # kernel kinds for the timing hooks
@@ -57,6 +57,15 @@ class MMHError(RuntimeError):
     def __init__(self, code, what=""):
         self.code = code
         super().__init__(f"{what}: {strerror(code)} ({code})" if what else f"{strerror(code)} ({code})")
+
+
+class Stats(C.Structure):
+    _fields_ = [("def_mean", C.c_double), ("def_sigma", C.c_double), ("defp_sigma", C.c_double),
+                ("rho_mean", C.c_double), ("rho_sigma", C.c_double), ("rho_min", C.c_double),
+                ("rho_max", C.c_double), ("rho_negative", C.c_longlong)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Config(C.Structure):
@@ -346,6 +355,12 @@ class Context:
         d = Diag()
         _chk(lib().mmh_iterate(self._h, int(niter), C.byref(d)), "iterate", allow_diverged=True)
         return d.as_dict()
+
+    def stats(self):
+        """main.f90's iteration diagnostics of the resident state (mmh_state_stats)."""
+        st = Stats()
+        _chk(lib().mmh_state_stats(self._h, C.byref(st)), "state_stats")
+        return st.as_dict()
 
     def store(self, defpot=None, u=None):
         nf = u.shape[0] if u is not None else 5
