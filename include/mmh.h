@@ -179,6 +179,18 @@ typedef struct mmh_stats {
 } mmh_stats;
 int mmh_state_stats(mmh_ctx* ctx, mmh_stats* stats);
 
+/* Binned power spectrum of a (n^3, host) -- or the cross spectrum with b (NULL:
+ * auto) -- in the bins of the reference's Fisher inputs: nbins (<= 128) bins
+ * log-spaced in |k| from 1 to n/2 fundamental modes, bin i holding
+ * (n/2)^(i/nbins) <= |k| < (n/2)^((i+1)/nbins) (calcfisherinfo.f90 reads 48 of
+ * them and skips the six that hold no mode at 128^3).  power[i] = mean over
+ * the bin's modes of |A(k)|^2 / n^3 (Re(A conj(B)) / n^3), A the unnormalised
+ * DFT (so unit white noise has power 1); kmean[i] = their mean |k| in
+ * fundamental units (the bin's geometric centre, power 0, when it is empty);
+ * modes[i] (may be NULL) their number.  Exact sums, independent of order. */
+int mmh_power_spectrum_f64(mmh_ctx* ctx, const double* a, const double* b, int nbins, double* kmean, double* power,
+                           long long* modes);
+
 /* ---- batched realisations (no single call in the reference) ------------ */
 /* One independent reconstruction of mmh/main.f90:83-179: density rho (n^3,
  * Fortran order, host), def = 0, niter deformation iterations, then the

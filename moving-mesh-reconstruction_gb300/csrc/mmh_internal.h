@@ -114,6 +114,16 @@ struct StatsDev {
 void launch_state_stats(const double* def, const double* defp, const double* rho, i64 n3, StatsDev* st,
                         cudaStream_t s);
 
+// binned power spectrum accumulators (fixed-point sums of power and |k|, mode counts)
+constexpr int kPowMaxBins = 128;
+struct PowDev {
+  unsigned long long p[kPowMaxBins][2], k[kPowMaxBins][2], cnt[kPowMaxBins];
+  int flag;
+  int pad;
+};
+void launch_power_bins(const void* A, const void* B, int n, int nb, const double* e2, double scale, PowDev* acc,
+                       cudaStream_t s);
+
 // calcdefp adjoint pieces (mmh_adjoint.cu)
 void launch_adj_pass1(double* y, const double* t, const uint8_t* maskx, const uint8_t* maskc, double dtaumesh,
                       i64 n3, cudaStream_t s);

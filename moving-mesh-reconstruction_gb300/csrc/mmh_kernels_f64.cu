@@ -437,6 +437,75 @@ void launch_state_stats(const double* def, const double* defp, const double* rho
   count_launch();
 }
 
+// Binned power spectrum of the half spectrum A (cuFFT D2Z layout, (n/2+1) x n
+// x n, x fastest): |A|^2 (or Re(A conj(B))) * scale over the modes of each
+// |k| bin.  Bin b holds e2[b] <= |k|^2 < e2[b+1] (squared edges, exact where
+// an edge is a power of two); half-spectrum modes with 0 < kx < n/2 stand for
+// two modes.  Per-block fixed-point histograms in shared memory, committed
+// with 128-bit carries: the sums are exact and independent of order.
+__device__ __forceinline__ void fx_atomic_add(unsigned long long* acc, __int128 v) {
+  unsigned long long lo = (unsigned long long)v, hi = (unsigned long long)((unsigned __int128)v >> 64);
+  unsigned long long old = atomicAdd(&acc[0], lo);
+  atomicAdd(&acc[1], hi + ((old + lo < old) ? 1ull : 0ull));
+}
+__global__ void __launch_bounds__(256) k_power_bins(const double2* __restrict__ A, const double2* __restrict__ B,
+                                                    int n, int nb, const double* __restrict__ e2, double scale,
+                                                    PowDev* acc) {
+  __shared__ unsigned long long sp[kPowMaxBins][2], sk[kPowMaxBins][2], sc[kPowMaxBins];
+  __shared__ double se2[kPowMaxBins + 1];
+  for (int q = threadIdx.x; q < kPowMaxBins; q += blockDim.x) {
+    sp[q][0] = sp[q][1] = sk[q][0] = sk[q][1] = sc[q] = 0ull;
+  }
+  for (int q = threadIdx.x; q <= nb; q += blockDim.x) se2[q] = e2[q];
+  __syncthreads();
+  const int nh = n / 2 + 1;
+  const i64 tot = (i64)nh * n * n;
+  bool bad = false;
+  for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (i64)gridDim.x * blockDim.x) {
+    int i = (int)(t % nh);
+    i64 r = t / nh;
+    int j = (int)(r % n), k = (int)(r / n);
+    long long ky = j <= n / 2 ? j : j - n, kz = k <= n / 2 ? k : k - n;
+    long long K2 = (long long)i * i + ky * ky + kz * kz;
+    double kk2 = (double)K2;
+    if (K2 == 0 || kk2 < se2[0] || !(kk2 < se2[nb])) continue;
+    int lo = 0, hi = nb - 1;  // the largest b with se2[b] <= kk2
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (se2[mid] <= kk2) lo = mid;
+      else hi = mid - 1;
+    }
+    const double w = (i == 0 || 2 * i == n) ? 1.0 : 2.0;
+    double2 a = A[t];
+    double p = B ? (a.x * B[t].x + a.y * B[t].y) : (a.x * a.x + a.y * a.y);
+    double pv = w * (p * scale), kv = w * sqrt(kk2);
+    if (!(fabs(pv) < 4294967296.0) || !(kv < 4294967296.0)) {
+      bad = true;
+      continue;
+    }
+    fx_atomic_add(sp[lo], fx_of(pv));
+    fx_atomic_add(sk[lo], fx_of(kv));
+    atomicAdd(&sc[lo], (unsigned long long)w);
+  }
+  if (bad) atomicOr(&acc->flag, 1);
+  __syncthreads();
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+    if (sc[q] == 0) continue;
+    __int128 vp = (__int128)(((unsigned __int128)sp[q][1] << 64) | (unsigned __int128)sp[q][0]);
+    __int128 vk = (__int128)(((unsigned __int128)sk[q][1] << 64) | (unsigned __int128)sk[q][0]);
+    fx_atomic_add(acc->p[q], vp);
+    fx_atomic_add(acc->k[q], vk);
+    atomicAdd(&acc->cnt[q], sc[q]);
+  }
+}
+void launch_power_bins(const void* A, const void* B, int n, int nb, const double* e2, double scale, PowDev* acc,
+                       cudaStream_t s) {
+  i64 tot = (i64)(n / 2 + 1) * n * n;
+  i64 blocks = std::min<i64>((tot + 255) / 256, 152 * 4);
+  k_power_bins<<<(unsigned)blocks, 256, 0, s>>>((const double2*)A, (const double2*)B, n, nb, e2, scale, acc);
+  count_launch();
+}
+
 void launch_lim_reset(LimDev* st, cudaStream_t s) {
   k_lim_reset<<<1, 1, 0, s>>>(st);
   count_launch();

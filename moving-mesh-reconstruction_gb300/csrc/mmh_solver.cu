@@ -1408,6 +1408,48 @@ int mmh_state_stats(mmh_ctx* c, mmh_stats* out) {
   out->rho_negative = (long long)h.nneg;
   return MMH_OK;
 }
+int mmh_power_spectrum_f64(mmh_ctx* c, const double* a, const double* b, int nbins, double* kmean, double* power,
+                           long long* modes) {
+  if (!c || !a || !kmean || !power || nbins < 1 || nbins > kPowMaxBins) return MMH_ERR_ARG;
+  const int n = c->n;
+  const i64 n3 = c->n3, nc = (i64)(n / 2 + 1) * n * n;
+  RET(make_plans(c));
+  // squared bin edges (n/2)^(2i/nbins): exact where the exponent makes a power of two
+  int m = 0;
+  while ((2 << m) < n) ++m;  // n/2 = 2^m
+  std::vector<double> e2(nbins + 1);
+  for (int i = 0; i <= nbins; ++i) {
+    const int num = 2 * m * i;
+    e2[i] = num % nbins == 0 ? std::ldexp(1.0, num / nbins) : std::exp2((double)num / nbins);
+  }
+  DevTemp buf;
+  buf.s = c->s;
+  const size_t bytes = sizeof(double) * (b ? 2 * nc : 0) + sizeof(double) * (nbins + 1) + sizeof(PowDev);
+  if (cudaMallocAsync(&buf.p, bytes, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
+  double* Bc = (double*)buf.p;
+  double* de2 = Bc + (b ? 2 * nc : 0);
+  PowDev* acc = (PowDev*)(de2 + nbins + 1);
+  CK(cudaMemcpyAsync(de2, e2.data(), sizeof(double) * (nbins + 1), cudaMemcpyHostToDevice, c->s));
+  CK(cudaMemsetAsync(acc, 0, sizeof(PowDev), c->s));
+  RET(upload(c, a, c->scr, n3));
+  CKF(cufftExecD2Z(c->pd2z, (cufftDoubleReal*)c->scr, (cufftDoubleComplex*)c->Xc));
+  if (b) {
+    RET(upload(c, b, c->scr, n3));
+    CKF(cufftExecD2Z(c->pd2z, (cufftDoubleReal*)c->scr, (cufftDoubleComplex*)Bc));
+  }
+  launch_power_bins(c->Xc, b ? Bc : nullptr, n, nbins, de2, 1.0 / (double)n3, acc, c->s);
+  PowDev h;
+  CK(cudaMemcpyAsync(&h, acc, sizeof(PowDev), cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  if (h.flag) return MMH_ERR_RANGE;
+  for (int q = 0; q < nbins; ++q) {
+    const double cnt = (double)h.cnt[q];
+    kmean[q] = h.cnt[q] ? fx_host(h.k[q]) / cnt : std::sqrt(std::sqrt(e2[q] * e2[q + 1]));
+    power[q] = h.cnt[q] ? fx_host(h.p[q]) / cnt : 0.0;
+    if (modes) modes[q] = (long long)h.cnt[q];
+  }
+  return MMH_OK;
+}
 int mmh_multigrid(mmh_ctx* c, float* u, float* rhs, const float* defpot, const float* ubig, float dx, int nx, int ny,
                   int nz, int nu, int nred, int iopt, mmh_diag* d) {
   return multigrid_host<float>(c, u, rhs, defpot, ubig, dx, nx, ny, nz, nu, nred, iopt, d);

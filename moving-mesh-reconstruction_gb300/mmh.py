@@ -41,6 +41,7 @@ EXPORTS = (
     "mmh_outputs_f64", "mmh_outputs_dev", "mmh_state_dev", "mmh_profile_start", "mmh_profile_stop",
     "mmh_relax_noalloc_f64", "mmh_batch_run", "mmh_calcdefp_adjoint_f64",
     "mmh_relaxing_adjoint_f64", "mmh_iterate_adjoint_f64", "mmh_state_stats",
+    "mmh_power_spectrum_f64",
 )
 
 # kernel kinds for the timing hooks
@@ -51,6 +52,14 @@ K_F32 = 256
 def K_AT(n):
     """Grid filter for profile_start: time only the launches on the n^3 level."""
     return int(n) << 12
+
+
+def write_spectrum(path, k, p):
+    """One bin per line, "k P(k)": the layout calcfisherinfo.f90:41-49 reads
+    (list-directed, tmp(:, 1, bin) = k, tmp(:, 2, bin) = P)."""
+    with open(path, "w") as f:
+        for kv, pv in zip(k, p):
+            f.write(f"{kv:.16e} {pv:.16e}\n")
 
 
 class MMHError(RuntimeError):
@@ -355,6 +364,18 @@ class Context:
         d = Diag()
         _chk(lib().mmh_iterate(self._h, int(niter), C.byref(d)), "iterate", allow_diverged=True)
         return d.as_dict()
+
+    def power_spectrum(self, a, b=None, nbins=48):
+        """Binned (cross) power spectrum of n^3 fields (mmh_power_spectrum_f64):
+        returns (kmean in fundamental units, power, modes) per bin."""
+        for x in (a, b):
+            if x is not None:
+                _farr(x, np.float64)
+        k = np.zeros(nbins)
+        p = np.zeros(nbins)
+        m = np.zeros(nbins, dtype=np.int64)
+        _chk(lib().mmh_power_spectrum_f64(self._h, _p(a), _p(b), int(nbins), _p(k), _p(p), _p(m)), "power_spectrum")
+        return k, p, m
 
     def stats(self):
         """main.f90's iteration diagnostics of the resident state (mmh_state_stats)."""
