@@ -11,7 +11,14 @@
 //             [--fndelta delta512/] [--fndisp disp512/] [--restart STEP]
 //             [--no-def] [--no-gradient] [--no-density] [--no-checkpoint]
 //             [--real8] [--precision fp64|mixed] [--schedule ref|tol|vcycle]
-//             [--tol T] [--print-names]
+//             [--tol T] [--ps-dir DIR/] [--print-names]
+//
+// --ps-dir writes the power spectra the reference's Fisher script reads
+// (calcfisherinfo.f90:26-27): ps48bins_<NG><id>.txt of the input density
+// contrast and ps48bins_def_<NG><id>.txt of def, one "k P(k)" line per bin of
+// 48, k in radians per cell (the units of defp2delta's |k|^2, so k^4 P_def is
+// the reconstructed density's power, as calcfisherinfo.f90:66 forms it) and P
+// in grid units (mean |DFT|^2 / n^3).
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -28,6 +35,7 @@ struct Opts {
   int ng = 0, niter = 300, restart = -1;
   std::string workdir = "./", z = "0.000", inf = "den", id = "_2", prefix = ".bin";
   std::string fnu = "u512/", fndef = "def512/", fndelta = "delta512/", fndisp = "disp512/";
+  std::string psdir;
   bool flag_def = true, flag_gradient = true, flag_density = true, flag_check = true;
   bool real8 = false, print_names = false;
   int precision = MMH_FP64, schedule = MMH_SCHED_REF;
@@ -67,7 +75,8 @@ int usage(const char* msg) {
                "usage: mmh_recon --ng N [--niter K] [--workdir DIR/] [--z S] [--inf S] [--id S] [--prefix S]\n"
                "       [--fnu S] [--fndef S] [--fndelta S] [--fndisp S] [--restart STEP] [--no-def]\n"
                "       [--no-gradient] [--no-density] [--no-checkpoint] [--real8]\n"
-               "       [--precision fp64|mixed] [--schedule ref|tol|vcycle] [--tol T] [--print-names]\n");
+               "       [--precision fp64|mixed] [--schedule ref|tol|vcycle] [--tol T] [--ps-dir DIR/]\n"
+               "       [--print-names]\n");
   return 2;
 }
 
@@ -92,6 +101,7 @@ bool parse(int argc, char** argv, Opts& o) {
     else if (k == "--fndef") { if (!val(o.fndef)) return false; }
     else if (k == "--fndelta") { if (!val(o.fndelta)) return false; }
     else if (k == "--fndisp") { if (!val(o.fndisp)) return false; }
+    else if (k == "--ps-dir") { if (!val(o.psdir)) return false; }
     else if (k == "--no-def") o.flag_def = false;
     else if (k == "--no-gradient") o.flag_gradient = false;
     else if (k == "--no-density") o.flag_density = false;
@@ -157,6 +167,18 @@ double rms_about(const std::vector<double>& a, double c) {
   return std::sqrt(s / (double)a.size());
 }
 
+// The 48-bin power spectrum of a field in the Fisher script's layout.
+bool write_spectrum(mmh_ctx* ctx, const std::string& fn, const double* a, int n) {
+  const int nb = 48;
+  double k[nb], p[nb];
+  if (mmh_power_spectrum_f64(ctx, a, nullptr, nb, k, p, nullptr) != MMH_OK) return false;
+  FILE* f = std::fopen(fn.c_str(), "w");
+  if (!f) return false;
+  const double unit = 2.0 * 3.14159265358979323846 / n;
+  for (int q = 0; q < nb; ++q) std::fprintf(f, "%.16e %.16e\n", k[q] * unit, p[q]);
+  return std::fclose(f) == 0;
+}
+
 int write_failed() {
   std::fprintf(stderr, "mmh_recon: write failed\n");
   return 1;
@@ -207,6 +229,11 @@ int main(int argc, char** argv) {
     return 1;
   }
   std::printf(" u mean= %.7g\n u sigma= %.7g\n \n BEGIN MULTIGRID\n", umean, rms_about(rho, 1.0));
+  std::vector<double> contrast;
+  if (!o.psdir.empty()) {
+    contrast.resize(n3);
+    for (size_t q = 0; q < n3; ++q) contrast[q] = rho[q] - 1.0;
+  }
   int begin = 1;
   if (o.restart >= 0) {
     // readrestart (main.f90:184-200)
@@ -278,6 +305,12 @@ int main(int argc, char** argv) {
       std::printf(" \n time consumed for defp2delta: %g seconds\n delta:\n avg= %.7g\n sigma= %.7g\n", now() - t1,
                   mean_of(delta), rms_about(delta, 0.0));
     }
+  }
+  if (!o.psdir.empty()) {
+    const std::string tag = std::to_string(n) + o.id + ".txt";
+    const std::string f1 = o.psdir + "ps48bins_" + tag, f2 = o.psdir + "ps48bins_def_" + tag;
+    std::printf(" writing: %s\n writing: %s\n", f1.c_str(), f2.c_str());
+    if (!write_spectrum(ctx, f1, contrast.data(), n) || !write_spectrum(ctx, f2, def.data(), n)) return write_failed();
   }
   mmh_destroy(ctx);
   return 0;

@@ -75,7 +75,7 @@ def test_driver_matches_binding(exe, mmh, fields, tmp_path):
     n, niter = 32, 3
     rho = fields.lognormal_density(n, sigma=0.8, seed=77).astype(np.float32).astype(np.float64)
     wd = _setup(tmp_path, rho)
-    r = run(exe, "--ng", n, "--niter", niter, "--workdir", wd)
+    r = run(exe, "--ng", n, "--niter", niter, "--workdir", wd, "--ps-dir", wd)
     assert r.returncode == 0, r.stderr + r.stdout
     assert r.stdout.count(" iter=") == niter
     u = np.zeros((5, n, n, n), order="F")
@@ -90,6 +90,14 @@ def test_driver_matches_binding(exe, mmh, fields, tmp_path):
         grad = np.zeros((n, n, n, 3), order="F")
         delta = np.zeros((n, n, n), order="F")
         ctx.outputs(grad, delta)
+        spectra = {"ps48bins_": ctx.power_spectrum(np.asfortranarray(rho - 1.0)),
+                   "ps48bins_def_": ctx.power_spectrum(d.astype(np.float32).astype(np.float64))}
+    # the Fisher script's inputs (calcfisherinfo.f90:26-27): "k P" per bin, k in rad/cell
+    for stem, (k, p, _) in spectra.items():
+        got = np.loadtxt(wd + f"{stem}{n}_2.txt")
+        assert got.shape == (48, 2)
+        np.testing.assert_allclose(got[:, 0], k * 2 * np.pi / n, rtol=1e-15)
+        np.testing.assert_allclose(got[:, 1], p, rtol=1e-15)
     f32 = np.float32
     assert np.array_equal(_load(wd + f"def512/0.000def_2{n:04d}.bin", n), d.astype(f32))
     for a, ax in enumerate("xyz"):
