@@ -91,7 +91,7 @@ def test_driver_matches_binding(exe, mmh, fields, tmp_path):
         delta = np.zeros((n, n, n), order="F")
         ctx.outputs(grad, delta)
         spectra = {"ps48bins_": ctx.power_spectrum(np.asfortranarray(rho - 1.0)),
-                   "ps48bins_def_": ctx.power_spectrum(d.astype(np.float32).astype(np.float64))}
+                   "ps48bins_def_": ctx.power_spectrum(d)}
     # the Fisher script's inputs (calcfisherinfo.f90:26-27): "k P" per bin, k in rad/cell
     for stem, (k, p, _) in spectra.items():
         got = np.loadtxt(wd + f"{stem}{n}_2.txt")
