@@ -191,6 +191,22 @@ int mmh_state_stats(mmh_ctx* ctx, mmh_stats* stats);
 int mmh_power_spectrum_f64(mmh_ctx* ctx, const double* a, const double* b, int nbins, double* kmean, double* power,
                            long long* modes);
 
+/* ---- input preparation (the reference's haloden.f90, from1024to512.f90) -- */
+/* Particle density assignment of haloden.f90:87-189: x(3,np) particle
+ * positions in fine-cell units (x, y, z fastest; nf fine cells per dimension,
+ * wrapped periodically), the ng^3 density (Fortran order, 4-byte reals) with
+ * every particle's cell counting it and every empty cell given to the nearest
+ * particle of the first non-empty cube shell around it, each particle's unit
+ * mass shared equally by its cells, normalised to mean 1.  raw (ng^3, may be
+ * NULL) receives the density before normalisation, wp (np, may be NULL) the
+ * cells of each particle.  ng <= 1024, np < 2^31.  MMH_ERR_RANGE when a
+ * position falls outside the grid after the wrap.  No context: the call
+ * allocates and frees its own device memory on the current device. */
+int mmh_haloden(const float* x, long long np, int nf, int ng, float* den, float* raw, int* wp);
+/* from1024to512.f90: ncoarse halvings of an ng^3 density by 2x2x2 block sums,
+ * then scaled to mean 1 (the sum taken exactly, then rounded to 4 bytes). */
+int mmh_coarsen(const float* den, int ng, int ncoarse, float* out);
+
 /* ---- batched realisations (no single call in the reference) ------------ */
 /* One independent reconstruction of mmh/main.f90:83-179: density rho (n^3,
  * Fortran order, host), def = 0, niter deformation iterations, then the

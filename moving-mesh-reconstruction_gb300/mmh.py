@@ -41,7 +41,7 @@ EXPORTS = (
     "mmh_outputs_f64", "mmh_outputs_dev", "mmh_state_dev", "mmh_profile_start", "mmh_profile_stop",
     "mmh_relax_noalloc_f64", "mmh_batch_run", "mmh_calcdefp_adjoint_f64",
     "mmh_relaxing_adjoint_f64", "mmh_iterate_adjoint_f64", "mmh_state_stats",
-    "mmh_power_spectrum_f64",
+    "mmh_power_spectrum_f64", "mmh_haloden", "mmh_coarsen",
 )
 
 # kernel kinds for the timing hooks
@@ -60,6 +60,30 @@ def write_spectrum(path, k, p):
     with open(path, "w") as f:
         for kv, pv in zip(k, p):
             f.write(f"{kv:.16e} {pv:.16e}\n")
+
+
+def haloden(x, nf, ng):
+    """Particle density assignment (haloden.f90) on the GPU: x (3, np) float32
+    positions in fine-cell units.  Returns (den, raw, wp)."""
+    xc = np.ascontiguousarray(np.asarray(x, dtype=np.float32).T)  # component fastest
+    np_ = xc.shape[0]
+    den = np.zeros((ng, ng, ng), dtype=np.float32, order="F")
+    raw = np.zeros_like(den, order="F")
+    wp = np.zeros(np_, dtype=np.int32)
+    L = lib()
+    L.mmh_haloden.argtypes = [C.c_void_p, C.c_longlong, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    _chk(L.mmh_haloden(_p(xc), np_, int(nf), int(ng), _p(den), _p(raw), _p(wp)), "haloden")
+    return den, raw, wp
+
+
+def coarsen(den, ncoarse=1):
+    """from1024to512.f90's coarsening on the GPU: ncoarse 2x2x2 halvings, mean 1."""
+    den = np.asfortranarray(den, dtype=np.float32)
+    ng = den.shape[0]
+    nc = ng >> ncoarse
+    out = np.zeros((nc, nc, nc), dtype=np.float32, order="F")
+    _chk(lib().mmh_coarsen(_p(den), int(ng), int(ncoarse), _p(out)), "coarsen")
+    return out
 
 
 class MMHError(RuntimeError):

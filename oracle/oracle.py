@@ -47,8 +47,8 @@ def build():
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(
-                os.path.join(_HERE, "mmh_oracle.cpp")):
+        srcs = [os.path.join(_HERE, f) for f in ("mmh_oracle.cpp", "prep_oracle.cpp")]
+        if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < max(map(os.path.getmtime, srcs)):
             build()
         _lib = C.CDLL(_LIB_PATH)
     return _lib
@@ -272,3 +272,33 @@ def r1lax_trace(na3, nrelax, iopt):
     buf = (C.c_int * cap)()
     cnt = lib().orc_r1lax_trace(int(na3), int(nrelax), int(iopt), buf, cap)
     return list(buf[:cnt])
+
+
+def haloden(x, nf, ng):
+    """haloden.f90:87-189: x (3, np) float32 positions in fine-cell units.
+    Returns (den, raw, wp): the normalised and raw ng^3 densities (Fortran
+    order, float32) and the cells per particle."""
+    x = np.asarray(x, dtype=np.float32)
+    np_ = x.shape[1]
+    xc = np.ascontiguousarray(x.T)  # component fastest, as xp(3, np)
+    den = np.zeros((ng, ng, ng), dtype=np.float32, order="F")
+    raw = np.zeros_like(den, order="F")
+    wp = np.zeros(np_, dtype=np.int32)
+    L = lib()
+    L.orc_haloden.argtypes = [C.c_void_p, C.c_longlong, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    rc = L.orc_haloden(_p(xc), np_, nf, ng, _p(den), _p(raw), _p(wp))
+    if rc != 0:
+        raise ValueError("orc_haloden failed")
+    return den, raw, wp
+
+
+def coarsen(den, ncoarse=1):
+    """from1024to512.f90: ncoarse 2x2x2 halvings, normalised to mean 1."""
+    den = np.asfortranarray(den, dtype=np.float32)
+    ng = den.shape[0]
+    nf = ng >> ncoarse
+    out = np.zeros((nf, nf, nf), dtype=np.float32, order="F")
+    L = lib()
+    L.orc_coarsen.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    L.orc_coarsen(_p(den), ng, ncoarse, _p(out))
+    return out
