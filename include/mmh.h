@@ -207,6 +207,22 @@ int mmh_haloden(const float* x, long long np, int nf, int ng, float* den, float*
  * then scaled to mean 1 (the sum taken exactly, then rounded to 4 bytes). */
 int mmh_coarsen(const float* den, int ng, int ncoarse, float* out);
 
+/* ---- after the path (mmh/column_density.f90, gridfigure.f90) ----------- */
+/* Column density of mmh/column_density.f90: den and def (ng^3, Fortran order,
+ * 4-byte reals) -> proj (ng^2): den scaled to mean 1, the z displacement
+ * dspz of def, and for each column the density between the displaced faces
+ * of cells ng/2 and ng/2+nplot-1 with fractional end cells, divided by nplot.
+ * Cells outside 1..ng wrap periodically (the reference reads past the array
+ * there).  The sum that scales den is exact, rounded once. */
+int mmh_column_density(const float* den, const float* def, int ng, int nplot, float* proj);
+/* gridfigure.f90:41-120: the displacement of a coarse def (nf^3) on the
+ * reference's (0:nf)^3 node grid with its halo, interpolated to the fine
+ * cells of an ng^3 density (ng a multiple of nf); proj2 (2, nf, nf) receives
+ * the new x, y positions of every (ng/nf)-th cell of plane ng/2, proj (ng^2)
+ * the column density of plane ng/2 (either may be NULL).  A node index nf+1
+ * (fine cells i = ng, read past the array by the reference) wraps to 1. */
+int mmh_gridfigure(const float* def, int nf, const float* den, int ng, float* proj2, float* proj);
+
 /* ---- batched realisations (no single call in the reference) ------------ */
 /* One independent reconstruction of mmh/main.f90:83-179: density rho (n^3,
  * Fortran order, host), def = 0, niter deformation iterations, then the

@@ -42,6 +42,7 @@ EXPORTS = (
     "mmh_relax_noalloc_f64", "mmh_batch_run", "mmh_calcdefp_adjoint_f64",
     "mmh_relaxing_adjoint_f64", "mmh_iterate_adjoint_f64", "mmh_state_stats",
     "mmh_power_spectrum_f64", "mmh_haloden", "mmh_coarsen",
+    "mmh_column_density", "mmh_gridfigure",
 )
 
 # kernel kinds for the timing hooks
@@ -84,6 +85,27 @@ def coarsen(den, ncoarse=1):
     out = np.zeros((nc, nc, nc), dtype=np.float32, order="F")
     _chk(lib().mmh_coarsen(_p(den), int(ng), int(ncoarse), _p(out)), "coarsen")
     return out
+
+
+def column_density(den, defpot, nplot=4):
+    """mmh/column_density.f90 on the GPU: (ng, ng) column density."""
+    den = np.asfortranarray(den, dtype=np.float32)
+    defpot = np.asfortranarray(defpot, dtype=np.float32)
+    ng = den.shape[0]
+    proj = np.zeros((ng, ng), dtype=np.float32, order="F")
+    _chk(lib().mmh_column_density(_p(den), _p(defpot), int(ng), int(nplot), _p(proj)), "column_density")
+    return proj
+
+
+def gridfigure(defpot, den):
+    """gridfigure.f90:41-120 on the GPU: (proj2 (2, nf, nf), proj (ng, ng))."""
+    defpot = np.asfortranarray(defpot, dtype=np.float32)
+    den = np.asfortranarray(den, dtype=np.float32)
+    nf, ng = defpot.shape[0], den.shape[0]
+    proj2 = np.zeros((2, nf, nf), dtype=np.float32, order="F")
+    proj = np.zeros((ng, ng), dtype=np.float32, order="F")
+    _chk(lib().mmh_gridfigure(_p(defpot), int(nf), _p(den), int(ng), _p(proj2), _p(proj)), "gridfigure")
+    return proj2, proj
 
 
 class MMHError(RuntimeError):

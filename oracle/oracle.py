@@ -302,3 +302,28 @@ def coarsen(den, ncoarse=1):
     L.orc_coarsen.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
     L.orc_coarsen(_p(den), ng, ncoarse, _p(out))
     return out
+
+
+def column_density(den, defpot, nplot=4):
+    """mmh/column_density.f90: (ng, ng) column density."""
+    den = np.asfortranarray(den, dtype=np.float32)
+    defpot = np.asfortranarray(defpot, dtype=np.float32)
+    ng = den.shape[0]
+    proj = np.zeros((ng, ng), dtype=np.float32, order="F")
+    L = lib()
+    L.orc_column_density.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    L.orc_column_density(_p(den), _p(defpot), ng, nplot, _p(proj))
+    return proj
+
+
+def gridfigure(defpot, den):
+    """gridfigure.f90:41-120: (proj2 (2, nf, nf), proj (ng, ng))."""
+    defpot = np.asfortranarray(defpot, dtype=np.float32)
+    den = np.asfortranarray(den, dtype=np.float32)
+    nf, ng = defpot.shape[0], den.shape[0]
+    proj2 = np.zeros((2, nf, nf), dtype=np.float32, order="F")
+    proj = np.zeros((ng, ng), dtype=np.float32, order="F")
+    L = lib()
+    L.orc_gridfigure.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    L.orc_gridfigure(_p(defpot), nf, _p(den), ng, _p(proj2), _p(proj))
+    return proj2, proj

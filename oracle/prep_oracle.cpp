@@ -1,6 +1,7 @@
-// CPU restatement of the reference's input preparation (test infrastructure
-// only): haloden.f90's particle density assignment and from1024to512.f90's
-// coarsening, loop for loop, in the reference's default real (FP32) and
+// CPU restatement of the reference's input preparation and post-processing
+// (test infrastructure only): haloden.f90's particle density assignment,
+// from1024to512.f90's coarsening, mmh/column_density.f90 and gridfigure.f90's
+// displacement interpolation and column density, loop for loop, in the reference's default real (FP32) and
 // real(8) where it uses them.  PARITY UNPINNED: the reference ships neither
 // particle files nor outputs of these programs.
 #include <cmath>
@@ -134,6 +135,183 @@ void orc_coarsen(const float* den, int ng, int ncoarse, float* out) {
   for (long long q = 0; q < n3; ++q) s += (double)a[q];
   const float sf = (float)s, scale = (float)n3;
   for (long long q = 0; q < n3; ++q) out[q] = a[q] / sf * scale;
+}
+
+// Exact sum of floats (128-bit fixed point, 64 fractional bits, terms
+// truncated below 2^-64), rounded to double as hi + lo * 2^-64: the sum the
+// GPU forms.  It restates the reference's real(4) sum(den), whose rounding
+// depends on the compiler's reduction order.
+static double exact_sum_f(const float* a, long long n) {
+  __int128 s = 0;
+  for (long long q = 0; q < n; ++q) s += (__int128)std::ldexp((double)a[q], 64);
+  bool neg = s < 0;
+  unsigned __int128 m = neg ? (unsigned __int128)(-s) : (unsigned __int128)s;
+  double r = (double)(unsigned long long)(m >> 64) + (double)(unsigned long long)m * 5.42101086242752217e-20;
+  return neg ? -r : r;
+}
+
+// den / sum(den) * ng**3 in real(4)
+static std::vector<float> normalised(const float* den, int ng) {
+  const long long n3 = (long long)ng * ng * ng;
+  const float sf = (float)exact_sum_f(den, n3), scale = (float)(int)n3;
+  std::vector<float> d(n3);
+  for (long long q = 0; q < n3; ++q) d[q] = den[q] / sf * scale;
+  return d;
+}
+
+// The column of (i, j) between the displaced faces kk1 and kk2 (1-based
+// cells), with fractional end cells: column_density.f90:42-53.  Cells outside
+// 1..ng wrap periodically (the reference reads out of bounds there).
+static float column(const std::vector<float>& den, int ng, int i, int j, float kk1, float kk2) {
+  auto D = [&](int k) {
+    int kw = ((k - 1) % ng + ng) % ng;
+    return den[(i - 1) + (long long)ng * ((j - 1) + (long long)ng * kw)];
+  };
+  int nk1 = (int)std::floor(kk1) + 1, nk2 = (int)std::floor(kk2) + 1;
+  float r1 = (float)nk1 - kk1;
+  float r2 = kk2 - (float)nk2 + 1.0f;
+  float s1 = 0.0f, s2 = 0.0f;
+  for (int k = nk1 + 1; k <= nk2 - 1; ++k) s1 = s1 + D(k);
+  for (int k = nk2; k <= nk1; ++k) s2 = s2 + D(k);
+  float t = r1 * D(nk1) + s1;
+  t = t + r2 * D(nk2);
+  return t - s2;
+}
+
+// mmh/column_density.f90:17-57: proj (ng^2) from den and def (ng^3).
+void orc_column_density(const float* den_in, const float* def, int ng, int nplot, float* proj) {
+  const std::vector<float> den = normalised(den_in, ng);
+  const long long n3 = (long long)ng * ng * ng;
+  std::vector<float> dz(n3);
+  auto F = [&](int i, int j, int k) { return def[(i - 1) + (long long)ng * ((j - 1) + (long long)ng * (k - 1))]; };
+  for (int k = 1; k <= ng; ++k)
+    for (int j = 1; j <= ng; ++j)
+      for (int i = 1; i <= ng; ++i) {
+        int kp = k % ng + 1, jp = j % ng + 1, ip = i % ng + 1;
+        float v = F(i, j, kp) + F(ip, j, kp);
+        v = v + F(i, jp, kp);
+        v = v + F(ip, jp, kp);
+        v = v - F(i, j, k);
+        v = v - F(ip, j, k);
+        v = v - F(i, jp, k);
+        v = v - F(ip, jp, k);
+        dz[(i - 1) + (long long)ng * ((j - 1) + (long long)ng * (k - 1))] = v / 4.0f;
+      }
+  auto Z = [&](int i, int j, int k) { return dz[(i - 1) + (long long)ng * ((j - 1) + (long long)ng * (k - 1))]; };
+  const int k1 = ng / 2, k2 = k1 + nplot - 1;
+  for (int j = 1; j <= ng; ++j)
+    for (int i = 1; i <= ng; ++i) {
+      int jm = imodulo(j - 2, ng) + 1, im = imodulo(i - 2, ng) + 1, k1m = imodulo(k1 - 2, ng) + 1;
+      float a = Z(im, jm, k1m) + Z(i, jm, k1m);
+      a = a + Z(im, j, k1m);
+      a = a + Z(i, j, k1m);
+      float kk1 = (float)(k1 - 1) + a / 4.0f;
+      float b = Z(im, jm, k2) + Z(i, jm, k2);
+      b = b + Z(im, j, k2);
+      b = b + Z(i, j, k2);
+      float kk2 = (float)k2 + b / 4.0f;
+      proj[(i - 1) + (long long)ng * (j - 1)] = column(den, ng, i, j, kk1, kk2) / (float)nplot;
+    }
+}
+
+// gridfigure.f90:41-120: the displacement of the coarse def (nf^3) on the
+// (0:nf)^3 node grid with the reference's halo assignment, trilinear
+// interpolation to the fine cells (ratio = ng / nf), new positions, and the
+// column density (nplot = 1) of den (ng^3).  proj2 (2, nf, nf) receives the
+// new x, y positions of every ratio-th cell of plane ng/2, proj (ng^2) the
+// column density.  A node index nf+1 (cells i = ng, read out of bounds by the
+// reference) wraps to 1.
+void orc_gridfigure(const float* def, int nf, const float* den_in, int ng, float* proj2, float* proj) {
+  const int ratio = ng / nf, m = nf + 1;
+  const std::vector<float> den = normalised(den_in, ng);
+  std::vector<float> T0(3 * (long long)m * m * m, 0.0f), TD;
+  auto at = [&](int c, int i, int j, int k) { return (long long)c + 3 * (i + (long long)m * (j + (long long)m * k)); };
+  auto F = [&](int i, int j, int k) { return def[(i - 1) + (long long)nf * ((j - 1) + (long long)nf * (k - 1))]; };
+  const float cf = (float)ratio * 1.0f / 4.0f;
+  for (int k = 1; k <= nf; ++k)
+    for (int j = 1; j <= nf; ++j)
+      for (int i = 1; i <= nf; ++i) {
+        int ip = i % nf + 1, jp = j % nf + 1, kp = k % nf + 1;
+        float x = F(ip, j, k) - F(i, j, k);
+        x = x + F(ip, jp, k);
+        x = x - F(i, jp, k);
+        x = x + F(ip, j, kp);
+        x = x - F(i, j, kp);
+        x = x + F(ip, jp, kp);
+        x = x - F(i, jp, kp);
+        float y = F(i, jp, k) - F(i, j, k);
+        y = y + F(ip, jp, k);
+        y = y - F(ip, j, k);
+        y = y + F(i, jp, kp);
+        y = y - F(i, j, kp);
+        y = y + F(ip, jp, kp);
+        y = y - F(ip, j, kp);
+        float z = F(i, j, kp) - F(i, j, k);
+        z = z + F(ip, j, kp);
+        z = z - F(ip, j, k);
+        z = z + F(i, jp, kp);
+        z = z - F(i, jp, k);
+        z = z + F(ip, jp, kp);
+        z = z - F(ip, jp, k);
+        T0[at(0, i, j, k)] = cf * x;
+        T0[at(1, i, j, k)] = cf * y;
+        T0[at(2, i, j, k)] = cf * z;
+      }
+  // tmp = cshift by -1 along the three node dimensions (length nf+1), then
+  // the three boundary assignments of gridfigure.f90:62-64
+  TD = T0;
+  auto w = [&](int v) { return v < 0 ? v + m : v; };
+  for (int c = 0; c < 3; ++c) {
+    for (int k = 1; k <= nf; ++k)
+      for (int j = 1; j <= nf; ++j) TD[at(c, 0, j, k)] = T0[at(c, w(-1), j - 1, k - 1)];
+    for (int j = 0; j <= nf; ++j)
+      for (int i = 1; i <= nf; ++i) TD[at(c, i, j, 0)] = T0[at(c, i - 1, w(j - 1), w(-1))];
+    for (int k = 1; k <= nf; ++k)
+      for (int i = 1; i <= nf; ++i) TD[at(c, i, 0, k)] = T0[at(c, i - 1, w(-1), k - 1)];
+  }
+  auto node = [&](int v) { return v == nf + 1 ? 1 : v; };
+  auto disp = [&](int c, int i, int j, int k) {
+    float ib = (float)(i % ratio) / (float)ratio, jb = (float)(j % ratio) / (float)ratio,
+          kb = (float)(k % ratio) / (float)ratio;
+    int ip = (int)std::floor((float)i / (float)ratio) + 1 - (int)std::floor(ib);
+    int jp = (int)std::floor((float)j / (float)ratio) + 1 - (int)std::floor(jb);
+    int kp = (int)std::floor((float)k / (float)ratio) + 1 - (int)std::floor(kb);
+    int i0 = ip - 1, j0 = jp - 1, k0 = kp - 1, i1 = node(ip), j1 = node(jp), k1 = node(kp);
+    float p111 = ib * jb * kb, p211 = (1.0f - ib) * jb * kb, p121 = ib * (1.0f - jb) * kb;
+    float p112 = ib * jb * (1.0f - kb), p221 = (1.0f - ib) * (1.0f - jb) * kb, p212 = (1.0f - ib) * jb * (1.0f - kb);
+    float p122 = ib * (1.0f - jb) * (1.0f - kb), p222 = (1.0f - ib) * (1.0f - jb) * (1.0f - kb);
+    float d = 0.0f;
+    d = d + TD[at(c, i0, j0, k0)] * p111;
+    d = d + TD[at(c, i1, j0, k0)] * p211;
+    d = d + TD[at(c, i0, j1, k0)] * p121;
+    d = d + TD[at(c, i0, j0, k1)] * p112;
+    d = d + TD[at(c, i1, j1, k0)] * p221;
+    d = d + TD[at(c, i1, j0, k1)] * p212;
+    d = d + TD[at(c, i0, j1, k1)] * p122;
+    d = d + TD[at(c, i1, j1, k1)] * p222;
+    return d;
+  };
+  const int k1 = ng / 2, k2 = k1;
+  for (int j = 1; j <= ng; ++j)
+    for (int i = 1; i <= ng; ++i) {
+      int jm = imodulo(j - 2, ng) + 1, im = imodulo(i - 2, ng) + 1, k1m = imodulo(k1 - 2, ng) + 1;
+      float a = disp(2, im, jm, k1m) + disp(2, i, jm, k1m);
+      a = a + disp(2, im, j, k1m);
+      a = a + disp(2, i, j, k1m);
+      float kk1 = (float)(k1 - 1) + a / 4.0f;
+      float b = disp(2, im, jm, k2) + disp(2, i, jm, k2);
+      b = b + disp(2, im, j, k2);
+      b = b + disp(2, i, j, k2);
+      float kk2 = (float)k2 + b / 4.0f;
+      proj[(i - 1) + (long long)ng * (j - 1)] = column(den, ng, i, j, kk1, kk2) / 1.0f;
+    }
+  for (int b = 1; b <= nf; ++b)
+    for (int a = 1; a <= nf; ++a)
+      for (int c = 0; c < 2; ++c) {
+        int ii = ratio * a, jj = ratio * b, kk = ng / 2;
+        int idx[3] = {ii, jj, kk};
+        proj2[c + 2 * ((a - 1) + (long long)nf * (b - 1))] = ((float)idx[c] + 0.5f) + disp(c, ii, jj, kk);
+      }
 }
 
 }  // extern "C"
