@@ -779,26 +779,49 @@ __device__ __forceinline__ double fsign1(double a) { return a >= 0.0 ? 1.0 : -1.
 // the expression as written.
 __device__ __forceinline__ double minmod(double a, double b) {
   const double wslopelim = 1.5, wbee = 1.0;
-  double x = fabs(a), y = fabs(b);
-  // Without a NaN operand (an integer test of the bits), fmin/fmax of these
-  // non-negative values equal compare-and-select; with one, the restatement's
-  // compare-and-select decides which value propagates.
   const unsigned long long inf_bits = 0x7FF0000000000000ull;
+  const unsigned long long ax = abs_bits(a), ay = abs_bits(b);
   double lo, hi, mm;
-  if (abs_bits(a) <= inf_bits && abs_bits(b) <= inf_bits) {
-    lo = fmin(x, y);
-    hi = fmax(x, y);
-    mm = bexp(lo) < 2047 ? fmin(wslopelim * lo, hi) : fmin(wslopelim * lo, wbee * hi + (1.0 - wbee) * lo);
-  } else {
-    lo = ref_min(x, y);
-    hi = ref_max(x, y);
-    mm = bexp(lo) < 2047 ? ref_min(wslopelim * lo, hi) : ref_min(wslopelim * lo, wbee * hi + (1.0 - wbee) * lo);
+  if (ax <= inf_bits && ay <= inf_bits) {
+    // Without a NaN operand (an integer test of the bits) the magnitudes
+    // |a|, |b| and 1.5*lo are non-negative, and non-negative doubles order
+    // like their bit patterns: min, max and the comparison with hi are
+    // integer compare-and-selects with the bits fmin/fmax would return, and
+    // a >= 0.0 is a test of the sign bit (-0 included).
+    const unsigned long long lob = ax <= ay ? ax : ay, hib = ax <= ay ? ay : ax;
+    lo = __longlong_as_double((long long)lob);
+    hi = __longlong_as_double((long long)hib);
+    if (lob < inf_bits) {
+      const double l15 = wslopelim * lo;  // finite or +inf
+      mm = abs_bits(l15) <= hib ? l15 : hi;
+    } else {
+      mm = fmin(wslopelim * lo, wbee * hi + (1.0 - wbee) * lo);
+    }
+    if (bexp(mm) < 2046) {
+      const bool pa = (__double_as_longlong(a) >= 0) || ax == 0, pb = (__double_as_longlong(b) >= 0) || ay == 0;
+      return pa != pb ? 0.0 : (pa ? mm : -mm);
+    }
+    return (fsign1(a) + fsign1(b)) * mm * 0.5;
   }
+  // a NaN operand: the restatement's compare-and-select decides which value
+  // propagates
+  double x = fabs(a), y = fabs(b);
+  lo = ref_min(x, y);
+  hi = ref_max(x, y);
+  mm = bexp(lo) < 2047 ? ref_min(wslopelim * lo, hi) : ref_min(wslopelim * lo, wbee * hi + (1.0 - wbee) * lo);
   if (bexp(mm) < 2046) {
     const bool pa = a >= 0.0, pb = b >= 0.0;
     return pa != pb ? 0.0 : (pa ? mm : -mm);
   }
   return (fsign1(a) + fsign1(b)) * mm * 0.5;
+}
+// x * 0.5 with the same bits: a normal x whose half is normal (biased
+// exponent 2..2046) loses one from its exponent field; zeros, subnormals,
+// the smallest normals, inf and NaN take the multiplication.
+__device__ __forceinline__ double half_of(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  return (e >= 2u && e <= 2046u) ? __longlong_as_double((long long)(b - (1ull << 52))) : x * 0.5;
 }
 // wphalf (relaxing.f90) from the half sums s = (u+w)/2 at the cells -1, 0, +1
 // and the half differences d = (u-w)/2 at the cells 0, +1, +2 of the face.
@@ -807,10 +830,10 @@ __device__ __forceinline__ double wphalf_sd(double sm, double s0, double sp, dou
   double b = dp;
   double da = sp - a;
   double dam = a - sm;
-  double ap = a + minmod(dam, da) * 0.5;
+  double ap = a + half_of(minmod(dam, da));
   double db = dpp - b;
   double dbm = b - d0;
-  double bp = b - minmod(db, dbm) * 0.5;
+  double bp = b - half_of(minmod(db, dbm));
   return ap - bp;
 }
 
@@ -834,7 +857,7 @@ __global__ void k_relax_faces(const double* __restrict__ sd, const double* __res
     const double* S = sd;
     const double* D = sd + 3 * n3;
     double fl = wphalf_sd(S[a], S[t], S[b], D[t], D[b], D[d]);
-    g[t] = (cc[b] + c0) * 0.5 * fl;
+    g[t] = half_of(cc[b] + c0) * fl;
   }
   {
     int jm = wm(j, n), jp = wp(j, n), jpp = wp(jp, n);
@@ -842,7 +865,7 @@ __global__ void k_relax_faces(const double* __restrict__ sd, const double* __res
     const double* S = sd + n3;
     const double* D = sd + 4 * n3;
     double fl = wphalf_sd(S[a], S[t], S[b], D[t], D[b], D[d]);
-    g[n3 + t] = (cc[b] + c0) * 0.5 * fl;
+    g[n3 + t] = half_of(cc[b] + c0) * fl;
   }
   {
     int km = wm(k, n), kp = wp(k, n), kpp = wp(kp, n);
@@ -850,7 +873,7 @@ __global__ void k_relax_faces(const double* __restrict__ sd, const double* __res
     const double* S = sd + 2 * n3;
     const double* D = sd + 5 * n3;
     double fl = wphalf_sd(S[a], S[t], S[b], D[t], D[b], D[d]);
-    g[2 * n3 + t] = (cc[b] + c0) * 0.5 * fl;
+    g[2 * n3 + t] = half_of(cc[b] + c0) * fl;
   }
 }
 

@@ -642,8 +642,13 @@ int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t
   launch_smooth27<double>(defp, n, c->scr, c->s);
   launch_smooth27<double>(c->scr, n, defp, c->s);
   launch_limiter_mask(c->defplim, c->def, defp, n, dtold, &c->sc->lim, mc2, c->s);
-  RET(limiter_poisson(c, defp, c->defplim));
+  // The FFT Poisson correction adds F^-1[F[defplim]/kernel], which is zero
+  // when no cell was limited: its transforms run only when one was.
   RET(pull_scal(c));
+  if (c->hsc->lim.ncompress) {
+    RET(limiter_poisson(c, defp, c->defplim));
+    RET(pull_scal(c));
+  }
   lim_to_diag(c->hsc->lim, d);
   return st;
 }
