@@ -103,6 +103,15 @@ constexpr int kDotBlocks = 152 * 8;
 void launch_dot_fast(const float* a, const float* b, i64 count, const unsigned long long* abits,
                      const unsigned long long* bbits, unsigned long long* acc, double* part, cudaStream_t s);
 
+// float-float outer loop of the mixed form (mmh_kernels_f64.cu): a double
+// buffer reinterpreted as (hi, lo) float pairs, in place
+void launch_ff_split(double* a, i64 count, cudaStream_t s);
+void launch_ff_join(double* a, i64 count, cudaStream_t s);
+void launch_ff_add_f(double* x, const float* e, i64 count, cudaStream_t s);
+void launch_ff_sub_mean(double* x, const double* mean, i64 count, cudaStream_t s);
+void launch_residual_ff(const double* phi, const double* rhs, const double* coef, int n, double dx, float* r32,
+                        unsigned long long* maxbits, cudaStream_t s);
+
 // main.f90's iteration diagnostics: exact sums (def, def^2, defp^2, rho,
 // (rho-1)^2), ord_of-encoded extrema of rho, count of rho < 0, range flag
 struct StatsDev {

@@ -506,6 +506,164 @@ void launch_power_bins(const void* A, const void* B, int n, int nb, const double
   count_launch();
 }
 
+// ---------------------------------------------------------------------------
+// Float-float residual of the mixed form's outer loop.  A value is the
+// unevaluated sum hi + lo of two floats (|lo| <= ulp(hi)/2), about 48
+// significant bits; sums and products use the error-free transformations of
+// Knuth (TwoSum) and Dekker (TwoProduct, here with one fused multiply-add),
+// as in the double-double literature (Dekker 1971; Hida, Li and Bailey 2001).
+// This translation unit is compiled without FMA contraction, which the
+// transformations rely on.  The residual is formed from neighbour
+// differences, r = rhs - sum_f b_f (phi_nb - phi_c) - cross terms, so its
+// terms are ~ n/(2 pi) |rhs| and its error ~ 1e-12 |rhs| -- far below the
+// outer loop's tolerance -- while every product and sum runs on the FP32
+// pipes (the FP64 form of this kernel is bound by the FP64 rate).
+// ---------------------------------------------------------------------------
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+  float s = a + b;
+  float bb = s - a;
+  float e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+__device__ __forceinline__ FF ff_quick(float a, float b) {  // |a| >= |b| or a == 0
+  float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  FF s = ff_two_sum(a.hi, b.hi), t = ff_two_sum(a.lo, b.lo);
+  s.lo = s.lo + t.hi;
+  s = ff_quick(s.hi, s.lo);
+  s.lo = s.lo + t.lo;
+  return ff_quick(s.hi, s.lo);
+}
+__device__ __forceinline__ FF ff_neg(FF a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ FF ff_sub(FF a, FF b) { return ff_add(a, ff_neg(b)); }
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return ff_quick(p, e);
+}
+__device__ __forceinline__ FF ff_scale(FF a, float p2) { return {a.hi * p2, a.lo * p2}; }  // p2 a power of two
+__device__ __forceinline__ FF ff_of(double x) {
+  float h = (float)x;
+  return {h, (float)(x - (double)h)};
+}
+
+// in place: doubles -> (hi, lo) pairs in the same 8 bytes, and back
+__global__ void k_ff_split(double* __restrict__ a, i64 count) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  FF v = ff_of(a[t]);
+  reinterpret_cast<float2*>(a)[t] = make_float2(v.hi, v.lo);
+}
+__global__ void k_ff_join(double* __restrict__ a, i64 count) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  float2 v = reinterpret_cast<const float2*>(a)[t];
+  a[t] = (double)v.x + (double)v.y;
+}
+// x += e (float) ; x -= mean (double)
+__global__ void k_ff_add_f(float2* __restrict__ x, const float* __restrict__ e, i64 count) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  float2 v = x[t];
+  FF r = ff_add({v.x, v.y}, {e[t], 0.0f});
+  x[t] = make_float2(r.hi, r.lo);
+}
+__global__ void k_ff_sub_mean(float2* __restrict__ x, const double* __restrict__ mean, i64 count) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  float2 v = x[t];
+  FF r = ff_sub({v.x, v.y}, ff_of(*mean));
+  x[t] = make_float2(r.hi, r.lo);
+}
+
+// r = rhs - L[phi] * di2 in float-float: phi and the six coefficient planes
+// as (hi, lo) pairs, rhs in FP64; r32 (may be null) = r rounded to float,
+// max |r| into maxbits.
+__global__ void __launch_bounds__(256) k_residual_ff(const float2* __restrict__ phi, const double* __restrict__ rhs,
+                                                     const float2* __restrict__ coef, int n, float di2,
+                                                     float* __restrict__ r32, unsigned long long* maxbits) {
+  const i64 n3 = (i64)n * n * n;
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  double m = 0.0;
+  if (t < n3) {
+    int i, j, k;
+    cell_of(t, n, i, j, k);
+    const int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
+    auto P = [&](int a, int b, int c) {
+      float2 v = __ldg(phi + IDX(a, b, c, n));
+      return FF{v.x, v.y};
+    };
+    auto C = [&](int f, int a, int b, int c) {
+      float2 v = __ldg(coef + (i64)f * n3 + IDX(a, b, c, n));
+      return FF{v.x, v.y};
+    };
+    const FF pc = P(i, j, k);
+    // face terms: b_f (phi_nb - phi_c), b_f the mean of the two cells' coefficients
+    const FF f1c = C(0, i, j, k), f4c = C(3, i, j, k), f6c = C(5, i, j, k);
+    FF L = ff_mul(ff_scale(ff_add(C(0, ip, j, k), f1c), 0.5f), ff_sub(P(ip, j, k), pc));
+    L = ff_add(L, ff_mul(ff_scale(ff_add(C(0, im, j, k), f1c), 0.5f), ff_sub(P(im, j, k), pc)));
+    L = ff_add(L, ff_mul(ff_scale(ff_add(C(3, i, jp, k), f4c), 0.5f), ff_sub(P(i, jp, k), pc)));
+    L = ff_add(L, ff_mul(ff_scale(ff_add(C(3, i, jm, k), f4c), 0.5f), ff_sub(P(i, jm, k), pc)));
+    L = ff_add(L, ff_mul(ff_scale(ff_add(C(5, i, j, kp), f6c), 0.5f), ff_sub(P(i, j, kp), pc)));
+    L = ff_add(L, ff_mul(ff_scale(ff_add(C(5, i, j, km), f6c), 0.5f), ff_sub(P(i, j, km), pc)));
+    // cross terms (relaxplane's t2)
+    const FF ppk = P(ip, jp, k), mpk = P(im, jp, k), pmk = P(ip, jm, k), mmk = P(im, jm, k);
+    const FF jpkp = P(i, jp, kp), jmkp = P(i, jm, kp), jpkm = P(i, jp, km), jmkm = P(i, jm, km);
+    const FF ipkp = P(ip, j, kp), imkp = P(im, j, kp), ipkm = P(ip, j, km), imkm = P(im, j, km);
+    FF x = ff_mul(ff_sub(ppk, mpk), C(1, i, jp, k));
+    x = ff_sub(x, ff_mul(ff_sub(pmk, mmk), C(1, i, jm, k)));
+    x = ff_add(x, ff_mul(ff_sub(ppk, pmk), C(1, ip, j, k)));
+    x = ff_sub(x, ff_mul(ff_sub(mpk, mmk), C(1, im, j, k)));
+    x = ff_add(x, ff_mul(ff_sub(jpkp, jmkp), C(4, i, j, kp)));
+    x = ff_sub(x, ff_mul(ff_sub(jpkm, jmkm), C(4, i, j, km)));
+    x = ff_add(x, ff_mul(ff_sub(jpkp, jpkm), C(4, i, jp, k)));
+    x = ff_sub(x, ff_mul(ff_sub(jmkp, jmkm), C(4, i, jm, k)));
+    x = ff_add(x, ff_mul(ff_sub(ipkp, imkp), C(2, i, j, kp)));
+    x = ff_sub(x, ff_mul(ff_sub(ipkm, imkm), C(2, i, j, km)));
+    x = ff_add(x, ff_mul(ff_sub(ipkp, ipkm), C(2, ip, j, k)));
+    x = ff_sub(x, ff_mul(ff_sub(imkp, imkm), C(2, im, j, k)));
+    L = ff_add(L, ff_scale(x, 0.25f));
+    const FF r = ff_sub(ff_of(rhs[t]), ff_scale(L, di2));
+    if (r32) r32[t] = r.hi;
+    m = fabs((double)r.hi + (double)r.lo);
+  }
+  if (maxbits) block_max_commit(m, maxbits);
+}
+
+void launch_ff_split(double* a, i64 count, cudaStream_t s) {
+  k_ff_split<<<grid_of(count, kBlock), kBlock, 0, s>>>(a, count);
+  count_launch();
+}
+void launch_ff_join(double* a, i64 count, cudaStream_t s) {
+  k_ff_join<<<grid_of(count, kBlock), kBlock, 0, s>>>(a, count);
+  count_launch();
+}
+void launch_ff_add_f(double* x, const float* e, i64 count, cudaStream_t s) {
+  k_ff_add_f<<<grid_of(count, kBlock), kBlock, 0, s>>>(reinterpret_cast<float2*>(x), e, count);
+  count_launch();
+}
+void launch_ff_sub_mean(double* x, const double* mean, i64 count, cudaStream_t s) {
+  k_ff_sub_mean<<<grid_of(count, kBlock), kBlock, 0, s>>>(reinterpret_cast<float2*>(x), mean, count);
+  count_launch();
+}
+void launch_residual_ff(const double* phi, const double* rhs, const double* coef, int n, double dx, float* r32,
+                        unsigned long long* maxbits, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  prof_begin(KK_RESIDUAL, s, n3, n);
+  k_residual_ff<<<grid_of(n3, kBlock), kBlock, 0, s>>>(reinterpret_cast<const float2*>(phi), rhs,
+                                                       reinterpret_cast<const float2*>(coef), n,
+                                                       (float)(1.0 / (dx * dx)), r32, maxbits);
+  prof_end(KK_RESIDUAL, s, n);
+  count_launch();
+}
+
 void launch_lim_reset(LimDev* st, cudaStream_t s) {
   k_lim_reset<<<1, 1, 0, s>>>(st);
   count_launch();

@@ -422,11 +422,25 @@ int true_residual(mmh_ctx* c, int l0, double dx, const double* x, const double* 
 }
 
 // Solve L x = b to tol (MMH_SCHED_TOL).  MMH_FP64: flexible PCG in FP64.
-// MMH_MIXED: FP64 defect correction -- FP64 residual, inner FP32 flexible PCG
-// (FP32 V-cycle preconditioner) on the correction to a relative 1e-3, FP64
-// update -- until the FP64 residual meets tol.
+// MMH_MIXED: defect correction -- outer residual at FP64-class accuracy
+// (float-float for tol >= kFFTolMin, FP64 below), inner FP32 flexible PCG
+// (FP32 V-cycle preconditioner) on the correction to a relative 1e-3, update
+// of the outer solution -- until the outer residual meets tol.
 const double kInnerTol = 1e-3;
+// Smallest tolerance the float-float outer residual serves: its rounding is
+// ~1e-12 of max|rhs| (terms of ~n/(2 pi) |rhs|, ~2^-45 each); tighter
+// tolerances take the FP64 residual.
+const double kFFTolMin = 1e-10;
 const int kInnerMax = 60;
+
+// the same from the float-float outer solution and coefficients (mixed form)
+int true_residual_ff(mmh_ctx* c, int l0, double dx, const double* x, const double* b, float* r32, double* rmax) {
+  CK(cudaMemsetAsync(&c->sc->resbits, 0, 8, c->s));
+  launch_residual_ff(x, b, c->h64.coef[l0], c->nl[l0], dx, r32, &c->sc->resbits, c->s);
+  RET(pull_scal(c));
+  *rmax = bits_to_double(c->hsc->resbits);
+  return MMH_OK;
+}
 
 int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_out, double* r1_out) {
   int n = c->nl[l0];
@@ -436,7 +450,7 @@ int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_
   CK(cudaMemcpyAsync(c->pb, rhs, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
   CK(cudaMemcpyAsync(c->px, u, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
   int status = MMH_OK, total = 0;
-  double rel = 0.0;
+  double rel = 0.0, rt = 0.0;
   if (c->cfg.precision == MMH_FP64) {
     int it = 0;
     double r0 = 0.0;
@@ -445,7 +459,42 @@ int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_
     if (status != MMH_OK && status != MMH_ERR_DIVERGED) return status;
     total = it;
     *r1_out = r0;
+  } else if (c->cfg.tol >= kFFTolMin) {
+    // The outer solution and the fine coefficients are carried as
+    // float-float pairs in their own buffers (the FP32 copy of the
+    // coefficients is already made): the outer residual then runs on the
+    // FP32 pipes at ~48-bit accuracy (k_residual_ff).
+    launch_ff_split(c->h64.coef[l0], 6 * n3, c->s);
+    launch_ff_split(c->px, n3, c->s);
+    double rmax = 0.0;
+    for (int outer = 0;; ++outer) {
+      RET(true_residual_ff(c, l0, dx, c->px, c->pb, c->pb32, &rmax));
+      rel = rmax / rn;
+      if (outer == 0) *r1_out = rmax;
+      if (!(rel == rel)) return MMH_ERR_NAN;
+      if (rel <= c->cfg.tol) break;
+      if (total >= c->cfg.max_cycles) {
+        status = MMH_ERR_DIVERGED;
+        break;
+      }
+      launch_fill<float>(c->pe32, n3, 0.0f, c->s);
+      int it = 0;
+      double rin = 0.0, r0 = 0.0;
+      int st = pcg_core<float>(c, l0, dx, c->pe32, c->pb32, c->pp32, c->pq32, rmax, kInnerTol, kInnerMax, &it, &rin,
+                               &r0);
+      if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
+      total += it;
+      launch_ff_add_f(c->px, c->pe32, n3, c->s);
+    }
+    // zero mean (the exact sum of all hi and lo parts), residual, back to FP64
+    CK(cudaMemsetAsync(c->sc->acc[0], 0, 16, c->s));
+    launch_fxsum<float>(reinterpret_cast<const float*>(c->px), 2 * n3, c->sc->acc[0], &c->sc->bad, c->s);
+    launch_fx_mean(c->sc->acc[0], (double)n3, &c->sc->mean, c->s);
+    launch_ff_sub_mean(c->px, &c->sc->mean, n3, c->s);
+    RET(true_residual_ff(c, l0, dx, c->px, c->pb, nullptr, &rt));
+    launch_ff_join(c->px, n3, c->s);
   } else {
+    // tolerances below the float-float residual's rounding floor: FP64 outer loop
     double rmax = 0.0;
     for (int outer = 0;; ++outer) {
       RET(true_residual(c, l0, dx, c->px, c->pb, c->pb32, &rmax));
@@ -467,10 +516,11 @@ int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_
       launch_add_f2d(c->px, c->pe32, n3, c->s);
     }
   }
-  // zero mean, true residual, results back in place
-  RET(zerosum<double>(c, c->px, n3));
-  double rt = 0.0;
-  RET(true_residual(c, l0, dx, c->px, c->pb, nullptr, &rt));
+  if (c->cfg.precision == MMH_FP64 || c->cfg.tol < kFFTolMin) {
+    // zero mean, true residual
+    RET(zerosum<double>(c, c->px, n3));
+    RET(true_residual(c, l0, dx, c->px, c->pb, nullptr, &rt));
+  }
   CK(cudaMemcpyAsync(u, c->px, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
   CK(cudaMemcpyAsync(rhs, c->pb, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
   *rel_out = rt / rn;

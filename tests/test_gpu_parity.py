@@ -158,6 +158,29 @@ def test_multigrid_mixed_converges(mmh, oracle, fields, n, sched):
     assert rel(ug, uo) <= 1e-9
 
 
+@pytest.mark.parametrize("n", [32, 64])
+def test_multigrid_mixed_float_float_outer_loop(mmh, oracle, fields, n):
+    """Mixed form at a tolerance the float-float outer residual serves
+    (>= 1e-10): the solve reaches it, the residual it reports agrees with an
+    FP64 recomputation of rhs - L[u] from the oracle, and the potential
+    agrees with the converged FP64 oracle to the accuracy the tolerance
+    allows."""
+    defpot, u = case(fields, n, 43, sigma=1.5)
+    rho = np.asfortranarray(u[0])
+    rng = np.random.default_rng(n + 5)
+    rhs0 = np.asfortranarray(rng.standard_normal((n, n, n)) * 0.01)
+    uo = np.zeros((n, n, n), order="F"); ro = rhs0.copy(order="F")
+    oracle.multigrid(uo, ro, defpot, rho, 1.0, sched=1, tol=1e-12, maxcyc=300, colour8=True)
+    ug = np.zeros((n, n, n), order="F"); rg = rhs0.copy(order="F")
+    with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=1, tol=1e-10, max_cycles=300) as ctx:
+        dg = ctx.multigrid(ug, rg, defpot, u, 1.0, n, n, n, 5)
+    assert dg["resid_rel"] <= 1e-10
+    r64 = oracle.residual(ug, rg, oracle.metric(defpot, rho))
+    rel64 = np.abs(r64).max() / np.abs(rg).max()
+    assert abs(rel64 - dg["resid_rel"]) <= 1e-12
+    assert rel(ug, uo) <= 1e-7
+
+
 @pytest.mark.parametrize("precision", ["MMH_MIXED", "MMH_FP64"])
 def test_graph_replay_matches_direct_launches(mmh, fields, precision):
     """The preconditioner cycle replayed from a CUDA graph gives the same bits
