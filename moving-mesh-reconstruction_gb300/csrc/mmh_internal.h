@@ -26,7 +26,10 @@ template <class T> inline int kk(int base) { return base | (sizeof(T) == 4 ? KK_
 
 // Launchers, instantiated for double (mmh_kernels_f64.cu, no FMA contraction)
 // and float (mmh_kernels_f32.cu).
-template <class T> void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_t s);
+// fast_div: one division per cell (the mixed form); false: the reference's
+// operations, bit for bit
+template <class T>
+void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_t s, bool fast_div = false);
 void launch_residual_fma(const double* phi, const double* rhs, const double* coef, int n, double dx, float* r32,
                          unsigned long long* maxbits, cudaStream_t s);
 template <class T> void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, T* scratch, cudaStream_t s);
@@ -71,9 +74,9 @@ void launch_spec_tables(double* tab, int n, cudaStream_t s);
 void launch_spec_pack(const void* Xc, int n, int mode, void* Z, const LimDev* st, const double* tab, cudaStream_t s);
 void launch_spec_unpack(const void* z, int n, double* out, int stride_out, int add, const LimDev* st, cudaStream_t s);
 void launch_relax_stage1(const double* rho, const double* def, const double* defp, int n, double* baj, double* cc,
-                         double* sd, cudaStream_t s);
+                         double* sd, cudaStream_t s, bool fast_div = false);
 void launch_relax_flux(const double* u1, const double* defp, const double* baj, const double* cc, int n, double* sd,
-                       cudaStream_t s);
+                       cudaStream_t s, bool fast_div = false);
 void launch_relax_dpv(const double* sd, const double* cc, int n, const double* ubase, double dt, double* out,
                       double* gface, cudaStream_t s);
 // u(nf,n^3) (float or double) <-> density; flag |= 1 when a component 2..nf is not zero

@@ -172,7 +172,9 @@ __device__ __forceinline__ double from_bits(unsigned long long b) { return __lon
 // ---------------------------------------------------------------------------
 // Curvilinear metric (cbajraw, mmh/gauss1.f90:1107-1210, non-lsquare branch)
 // ---------------------------------------------------------------------------
-template <class T>
+// FastDiv (the mixed form, which is not bit-matched): urg/det once, then six
+// multiplications instead of six divisions.
+template <class T, bool FastDiv = false>
 __global__ void k_metric(const T* __restrict__ def, const T* __restrict__ rho, int n, T di2, T* __restrict__ coef) {
   i64 n3 = (i64)n * n * n;
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
@@ -210,6 +212,16 @@ __global__ void k_metric(const T* __restrict__ def, const T* __restrict__ rho, i
         urg = urg + rho[IDX(is[a], js[b], ks[d], n)];
       }
   urg = urg / T(27);
+  if (FastDiv) {
+    const T w = urg / det;
+    coef[0 * n3 + t] = w * b11;
+    coef[1 * n3 + t] = w * b12;
+    coef[2 * n3 + t] = w * b13;
+    coef[3 * n3 + t] = w * b22;
+    coef[4 * n3 + t] = w * b23;
+    coef[5 * n3 + t] = w * b33;
+    return;
+  }
   coef[0 * n3 + t] = urg * b11 / det;
   coef[1 * n3 + t] = urg * b12 / det;
   coef[2 * n3 + t] = urg * b13 / det;

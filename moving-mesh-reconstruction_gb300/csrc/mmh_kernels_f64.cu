@@ -819,6 +819,9 @@ __device__ __forceinline__ void store_sd(double* __restrict__ sd, i64 n3, i64 t,
 // stage 1: calcbaj + cflkeuler + flux of u at every cell.
 // baj: 7 planes (b11,b12,b13,b22,b23,b33,det); cc: freezing speed; sd: the
 // half sums and differences of store_sd.
+// FastDiv (the mixed form, which is not bit-matched): each cell's divisions
+// by det, by det again and by c become one reciprocal each and products.
+template <bool FastDiv>
 __global__ void k_relax_stage1(const double* __restrict__ rho, const double* __restrict__ def,
                                const double* __restrict__ defp, int n, double* __restrict__ baj,
                                double* __restrict__ cc, double* __restrict__ sd) {
@@ -828,7 +831,7 @@ __global__ void k_relax_stage1(const double* __restrict__ rho, const double* __r
   int i, j, k;
   cell_of(t, n, i, j, k);
   const double gamma = 5. / 3.;
-  LimM m = lim_metric(def, n, i, j, k);
+  LimM m = lim_metric<FastDiv>(def, n, i, j, k);
   baj[0 * n3 + t] = m.b11;
   baj[1 * n3 + t] = m.b12;
   baj[2 * n3 + t] = m.b13;
@@ -876,27 +879,45 @@ __global__ void k_relax_stage1(const double* __restrict__ rho, const double* __r
   {
     double rg = m.det;
     double mx = zdiv(rg), my = mx, mz = mx;
-    double pdxg = (dxp - dxm) * 0.5 / rg;
-    double pdyg = (dyp - dym) * 0.5 / rg;
-    double pdzg = (dzp - dzm) * 0.5 / rg;
+    double pdxg, pdyg, pdzg;
+    if (FastDiv) {
+      const double rr = 1.0 / rg;
+      pdxg = (dxp - dxm) * 0.5 * rr;
+      pdyg = (dyp - dym) * 0.5 * rr;
+      pdzg = (dzp - dzm) * 0.5 * rr;
+    } else {
+      pdxg = (dxp - dxm) * 0.5 / rg;
+      pdyg = (dyp - dym) * 0.5 / rg;
+      pdzg = (dzp - dzm) * 0.5 / rg;
+    }
     double b11 = m.b11 * rg, b12 = m.b12 * rg, b13 = m.b13 * rg, b22 = m.b22 * rg, b23 = m.b23 * rg, b33 = m.b33 * rg;
     double vtt1 = mx - u0 * pdxg;
     double vtt2 = my - u0 * pdyg;
     double vtt3 = mz - u0 * pdzg;
-    store_sd(sd, n3, t, u0, (b11 * vtt1 + b12 * vtt2 + b13 * vtt3) / c, (b12 * vtt1 + b22 * vtt2 + b23 * vtt3) / c,
-             (b13 * vtt1 + b23 * vtt2 + b33 * vtt3) / c);
+    if (FastDiv) {
+      const double rc = 1.0 / c;
+      store_sd(sd, n3, t, u0, (b11 * vtt1 + b12 * vtt2 + b13 * vtt3) * rc, (b12 * vtt1 + b22 * vtt2 + b23 * vtt3) * rc,
+               (b13 * vtt1 + b23 * vtt2 + b33 * vtt3) * rc);
+    } else {
+      store_sd(sd, n3, t, u0, (b11 * vtt1 + b12 * vtt2 + b13 * vtt3) / c, (b12 * vtt1 + b22 * vtt2 + b23 * vtt3) / c,
+               (b13 * vtt1 + b23 * vtt2 + b33 * vtt3) / c);
+    }
   }
 }
 
 void launch_relax_stage1(const double* rho, const double* def, const double* defp, int n, double* baj, double* cc,
-                         double* sd, cudaStream_t s) {
+                         double* sd, cudaStream_t s, bool fast_div) {
   i64 n3 = (i64)n * n * n;
-  k_relax_stage1<<<grid_of(n3, kBlock), kBlock, 0, s>>>(rho, def, defp, n, baj, cc, sd);
+  if (fast_div)
+    k_relax_stage1<true><<<grid_of(n3, kBlock), kBlock, 0, s>>>(rho, def, defp, n, baj, cc, sd);
+  else
+    k_relax_stage1<false><<<grid_of(n3, kBlock), kBlock, 0, s>>>(rho, def, defp, n, baj, cc, sd);
   count_launch();
 }
 
 // flux of the half-step state u1 with the metric of stage 1 (relaxing.f90:
 // 970-988), as the half sums and differences of store_sd.
+template <bool FastDiv>
 __global__ void k_relax_flux(const double* __restrict__ u1, const double* __restrict__ defp,
                              const double* __restrict__ baj, const double* __restrict__ cc, int n,
                              double* __restrict__ sd) {
@@ -910,22 +931,39 @@ __global__ void k_relax_flux(const double* __restrict__ u1, const double* __rest
   double u0 = u1[t];
   double c = cc[t];
   double mx = zdiv(rg), my = mx, mz = mx;
-  double pdxg = (defp[IDX(ip, j, k, n)] - defp[IDX(im, j, k, n)]) * 0.5 / rg;
-  double pdyg = (defp[IDX(i, jp, k, n)] - defp[IDX(i, jm, k, n)]) * 0.5 / rg;
-  double pdzg = (defp[IDX(i, j, kp, n)] - defp[IDX(i, j, km, n)]) * 0.5 / rg;
+  double pdxg, pdyg, pdzg;
+  if (FastDiv) {
+    const double rr = 1.0 / rg;
+    pdxg = (defp[IDX(ip, j, k, n)] - defp[IDX(im, j, k, n)]) * 0.5 * rr;
+    pdyg = (defp[IDX(i, jp, k, n)] - defp[IDX(i, jm, k, n)]) * 0.5 * rr;
+    pdzg = (defp[IDX(i, j, kp, n)] - defp[IDX(i, j, km, n)]) * 0.5 * rr;
+  } else {
+    pdxg = (defp[IDX(ip, j, k, n)] - defp[IDX(im, j, k, n)]) * 0.5 / rg;
+    pdyg = (defp[IDX(i, jp, k, n)] - defp[IDX(i, jm, k, n)]) * 0.5 / rg;
+    pdzg = (defp[IDX(i, j, kp, n)] - defp[IDX(i, j, km, n)]) * 0.5 / rg;
+  }
   double b11 = baj[0 * n3 + t] * rg, b12 = baj[1 * n3 + t] * rg, b13 = baj[2 * n3 + t] * rg;
   double b22 = baj[3 * n3 + t] * rg, b23 = baj[4 * n3 + t] * rg, b33 = baj[5 * n3 + t] * rg;
   double vtt1 = mx - u0 * pdxg;
   double vtt2 = my - u0 * pdyg;
   double vtt3 = mz - u0 * pdzg;
-  store_sd(sd, n3, t, u0, (b11 * vtt1 + b12 * vtt2 + b13 * vtt3) / c, (b12 * vtt1 + b22 * vtt2 + b23 * vtt3) / c,
-           (b13 * vtt1 + b23 * vtt2 + b33 * vtt3) / c);
+  if (FastDiv) {
+    const double rc = 1.0 / c;
+    store_sd(sd, n3, t, u0, (b11 * vtt1 + b12 * vtt2 + b13 * vtt3) * rc, (b12 * vtt1 + b22 * vtt2 + b23 * vtt3) * rc,
+             (b13 * vtt1 + b23 * vtt2 + b33 * vtt3) * rc);
+  } else {
+    store_sd(sd, n3, t, u0, (b11 * vtt1 + b12 * vtt2 + b13 * vtt3) / c, (b12 * vtt1 + b22 * vtt2 + b23 * vtt3) / c,
+             (b13 * vtt1 + b23 * vtt2 + b33 * vtt3) / c);
+  }
 }
 
 void launch_relax_flux(const double* u1, const double* defp, const double* baj, const double* cc, int n, double* sd,
-                       cudaStream_t s) {
+                       cudaStream_t s, bool fast_div) {
   i64 n3 = (i64)n * n * n;
-  k_relax_flux<<<grid_of(n3, kBlock), kBlock, 0, s>>>(u1, defp, baj, cc, n, sd);
+  if (fast_div)
+    k_relax_flux<true><<<grid_of(n3, kBlock), kBlock, 0, s>>>(u1, defp, baj, cc, n, sd);
+  else
+    k_relax_flux<false><<<grid_of(n3, kBlock), kBlock, 0, s>>>(u1, defp, baj, cc, n, sd);
   count_launch();
 }
 

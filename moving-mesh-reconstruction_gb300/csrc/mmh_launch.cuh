@@ -9,11 +9,14 @@ static inline unsigned grid_of(i64 count, int block) { return (unsigned)((count 
 static const int kBlock = 256;
 
 template <class T>
-void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_t s) {
+void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_t s, bool fast_div) {
   i64 n3 = (i64)n * n * n;
   T di2 = T(1) / (dx * dx);
   prof_begin(kk<T>(KK_METRIC), s, n3, n);
-  k_metric<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(def, rho, n, di2, coef);
+  if (fast_div)
+    k_metric<T, true><<<grid_of(n3, kBlock), kBlock, 0, s>>>(def, rho, n, di2, coef);
+  else
+    k_metric<T, false><<<grid_of(n3, kBlock), kBlock, 0, s>>>(def, rho, n, di2, coef);
   prof_end(kk<T>(KK_METRIC), s, n);
   count_launch();
 }
@@ -214,7 +217,7 @@ void launch_usum_flag(const unsigned long long* acc, int* flag, cudaStream_t s) 
 }
 
 #define MMH_INSTANTIATE(T)                                                                                          \
-  template void launch_metric<T>(const T*, const T*, int, T, T*, cudaStream_t);                                   \
+  template void launch_metric<T>(const T*, const T*, int, T, T*, cudaStream_t, bool);                             \
   template void launch_gs_sweeps<T>(T*, const T*, const T*, int, T, int, T*, cudaStream_t);                         \
   template void launch_residual<T>(const T*, const T*, const T*, int, T, T*, float*, unsigned long long*,          \
                                    cudaStream_t);                                                                   \

@@ -16,6 +16,9 @@ struct LimM {
   double phixx, phiyy, phizz, phixy, phiyz, phixz;
 };
 
+// FastDiv (the mixed form, which is not bit-matched): the six divisions by
+// det become one reciprocal and six multiplications.
+template <bool FastDiv = false>
 __device__ __forceinline__ LimM lim_metric(const double* __restrict__ def, int n, int i, int j, int k) {
   int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
   LimM m;
@@ -29,12 +32,22 @@ __device__ __forceinline__ LimM lim_metric(const double* __restrict__ def, int n
   double a11 = 1.0 + m.phixx, a12 = m.phixy, a13 = m.phixz, a22 = 1.0 + m.phiyy, a23 = m.phiyz, a33 = 1.0 + m.phizz;
   double det = a11 * a22 * a33 + 2.0 * a12 * a13 * a23 - a13 * a13 * a22 - a11 * (a23 * a23) - a12 * a12 * a33;
   m.det = det;
-  m.b11 = (a22 * a33 - a23 * a23) / det;
-  m.b12 = (a13 * a23 - a12 * a33) / det;
-  m.b13 = (a12 * a23 - a13 * a22) / det;
-  m.b22 = (a11 * a33 - a13 * a13) / det;
-  m.b23 = (a12 * a13 - a11 * a23) / det;
-  m.b33 = (a11 * a22 - a12 * a12) / det;
+  if (FastDiv) {
+    const double r = 1.0 / det;
+    m.b11 = (a22 * a33 - a23 * a23) * r;
+    m.b12 = (a13 * a23 - a12 * a33) * r;
+    m.b13 = (a12 * a23 - a13 * a22) * r;
+    m.b22 = (a11 * a33 - a13 * a13) * r;
+    m.b23 = (a12 * a13 - a11 * a23) * r;
+    m.b33 = (a11 * a22 - a12 * a12) * r;
+  } else {
+    m.b11 = (a22 * a33 - a23 * a23) / det;
+    m.b12 = (a13 * a23 - a12 * a33) / det;
+    m.b13 = (a12 * a23 - a13 * a22) / det;
+    m.b22 = (a11 * a33 - a13 * a13) / det;
+    m.b23 = (a12 * a13 - a11 * a23) / det;
+    m.b33 = (a11 * a22 - a12 * a12) / det;
+  }
   return m;
 }
 

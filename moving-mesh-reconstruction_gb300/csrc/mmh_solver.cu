@@ -275,7 +275,8 @@ int build_levels(mmh_ctx* c, int l0) {
   }
   for (int l = l0; l < c->nlev; ++l) {
     int n = c->nl[l];
-    launch_metric<double>(c->defl[l], c->rhol[l], n, double(1 << l), c->h64.coef[l], c->s);
+    launch_metric<double>(c->defl[l], c->rhol[l], n, double(1 << l), c->h64.coef[l], c->s,
+                          c->cfg.precision == MMH_MIXED);
     if (c->cfg.precision == MMH_MIXED) launch_d2f(c->h64.coef[l], c->h32.coef[l], 6 * (i64)n * n * n, c->s);
   }
   return MMH_OK;
@@ -706,9 +707,10 @@ int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t
 // relaxing(u, def, defp, cmax, dt, 5) on the resident density.
 int relaxing_dev(mmh_ctx* c, double dt) {
   int n = c->n;
-  launch_relax_stage1(c->rho, c->def, c->defp(), n, c->baj, c->cc, c->vt, c->s);
+  const bool fast = c->cfg.precision == MMH_MIXED;  // one reciprocal per division site
+  launch_relax_stage1(c->rho, c->def, c->defp(), n, c->baj, c->cc, c->vt, c->s, fast);
   launch_relax_dpv(c->vt, c->cc, n, c->rho, dt / 2.0, c->u1, c->gface, c->s);
-  launch_relax_flux(c->u1, c->defp(), c->baj, c->cc, n, c->vt, c->s);
+  launch_relax_flux(c->u1, c->defp(), c->baj, c->cc, n, c->vt, c->s, fast);
   launch_relax_dpv(c->vt, c->cc, n, c->rho, dt, c->rho, c->gface, c->s);
   return MMH_OK;
 }
@@ -886,10 +888,11 @@ int relaxing_adjoint_dev(mmh_ctx* c, double dt, const double* ubar, double* gu, 
   double* xbar = u1bar + n3;
   double* defp = c->defp();
   // forward pass (relaxing_dev) with both stages' half sums kept
-  launch_relax_stage1(c->rho, c->def, defp, n, c->baj, c->cc, sd0, c->s);
+  const bool fast = c->cfg.precision == MMH_MIXED;  // as relaxing_dev
+  launch_relax_stage1(c->rho, c->def, defp, n, c->baj, c->cc, sd0, c->s, fast);
   launch_adj_alpha(c->baj, defp, c->cc, n, alpha, c->s);
   launch_relax_dpv(sd0, c->cc, n, c->rho, dt / 2.0, c->u1, c->gface, c->s);
-  launch_relax_flux(c->u1, defp, c->baj, c->cc, n, sd1, c->s);
+  launch_relax_flux(c->u1, defp, c->baj, c->cc, n, sd1, c->s, fast);
   // stage 2 (u' = u - dt R(u1)), then stage 1 (u1 = u - dt/2 R(u))
   CK(cudaMemsetAsync(alphabar, 0, sizeof(double) * 4 * n3, c->s));
   launch_adj_dpv(sd1, c->cc, alpha, c->u1, ubar, -dt, n, u1bar, alphabar, cbar, c->s);
