@@ -106,6 +106,9 @@ constexpr int kDotBlocks = 152 * 8;
 void launch_dot_fast(const float* a, const float* b, i64 count, const unsigned long long* abits,
                      const unsigned long long* bbits, unsigned long long* acc, double* part, cudaStream_t s);
 
+// the mixed form's nsmooth: three axis passes, `in` overwritten
+void launch_smooth_sep(double* in, int n, double* out, cudaStream_t s);
+
 // float-float outer loop of the mixed form (mmh_kernels_f64.cu): a double
 // buffer reinterpreted as (hi, lo) float pairs, in place
 void launch_ff_split(double* a, i64 count, cudaStream_t s);

@@ -664,6 +664,31 @@ void launch_residual_ff(const double* phi, const double* rhs, const double* coef
   count_launch();
 }
 
+// One axis of the smoother [1/4, 1/2, 1/4] (the 27-point nsmooth of
+// limiter.f90:677-781 is its product over the three axes), periodic:
+// out = (in(-1) + in(+1)) / 4 + in / 2.
+__global__ void k_smooth_axis(const double* __restrict__ in, int n, int axis, double* __restrict__ out) {
+  const i64 n3 = (i64)n * n * n;
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  int c[3];
+  cell_of(t, n, c[0], c[1], c[2]);
+  const i64 stride = axis == 0 ? 1 : (axis == 1 ? (i64)n : (i64)n * n);
+  const i64 lo = c[axis] == 0 ? t + (i64)(n - 1) * stride : t - stride;
+  const i64 hi = c[axis] == n - 1 ? t - (i64)(n - 1) * stride : t + stride;
+  out[t] = (in[lo] + in[hi]) * 0.25 + in[t] * 0.5;
+}
+// The 27-point smoother as three axis passes (the mixed form's nsmooth:
+// the same operator, other rounding): in -> out -> in -> out; in is
+// overwritten.
+void launch_smooth_sep(double* in, int n, double* out, cudaStream_t s) {
+  const i64 n3 = (i64)n * n * n;
+  k_smooth_axis<<<grid_of(n3, kBlock), kBlock, 0, s>>>(in, n, 0, out);
+  k_smooth_axis<<<grid_of(n3, kBlock), kBlock, 0, s>>>(out, n, 1, in);
+  k_smooth_axis<<<grid_of(n3, kBlock), kBlock, 0, s>>>(in, n, 2, out);
+  count_launch(3);
+}
+
 void launch_lim_reset(LimDev* st, cudaStream_t s) {
   k_lim_reset<<<1, 1, 0, s>>>(st);
   count_launch();

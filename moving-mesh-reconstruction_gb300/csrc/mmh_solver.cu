@@ -673,6 +673,16 @@ int limiter_poisson(mmh_ctx* c, double* defp, const double* defplim) {
   return MMH_OK;
 }
 
+// nsmooth of calcdefp: the reference's 27-point sum in the FP64 form; three
+// axis passes in the mixed form (same operator, other rounding), which
+// overwrite `in` (every source calcdefp smooths is dead afterwards).
+void smooth_step(mmh_ctx* c, double* in, double* out) {
+  if (c->cfg.precision == MMH_MIXED)
+    launch_smooth_sep(in, c->n, out, c->s);
+  else
+    launch_smooth27<double>(in, c->n, out, c->s);
+}
+
 // calcdefp on the resident state: defp (= h64.u[0]) from def and rho.
 int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t* mc1, uint8_t* mc2, mmh_diag* d) {
   int n = c->n;
@@ -681,17 +691,17 @@ int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t
   double* tmp = c->tmp();
   double* defp = c->defp();
   launch_calcdefp_rhs(tmp, c->rho, n, dtold, c->s);
-  launch_smooth27<double>(tmp, n, c->scr, c->s);
-  launch_smooth27<double>(c->scr, n, tmp, c->s);
-  launch_smooth27<double>(tmp, n, c->scr, c->s);
+  smooth_step(c, tmp, c->scr);
+  smooth_step(c, c->scr, tmp);
+  smooth_step(c, tmp, c->scr);
   launch_lim_reset(&c->sc->lim, c->s);
   launch_limiter_pass1(c->scr, c->def, c->rho, n, dtold, dtaumesh, &c->sc->lim, mx, mc1, c->s);
-  launch_smooth27<double>(c->scr, n, tmp, c->s);
+  smooth_step(c, c->scr, tmp);
   launch_fill<double>(defp, n3, 0.0, c->s);
   int st = multigrid_level(c, 0, 1.0, d);
   if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
-  launch_smooth27<double>(defp, n, c->scr, c->s);
-  launch_smooth27<double>(c->scr, n, defp, c->s);
+  smooth_step(c, defp, c->scr);
+  smooth_step(c, c->scr, defp);
   launch_limiter_mask(c->defplim, c->def, defp, n, dtold, &c->sc->lim, mc2, c->s);
   // The FFT Poisson correction adds F^-1[F[defplim]/kernel], which is zero
   // when no cell was limited: its transforms run only when one was.
@@ -761,20 +771,20 @@ int calcdefp_fwd_keep(mmh_ctx* c, double dtold, double dtaumesh, const CalcKeep&
   double* tmp = c->tmp();
   double* defp = c->defp();
   launch_calcdefp_rhs(tmp, c->rho, n, dtold, c->s);
-  launch_smooth27<double>(tmp, n, c->scr, c->s);
-  launch_smooth27<double>(c->scr, n, tmp, c->s);
-  launch_smooth27<double>(tmp, n, c->scr, c->s);
+  smooth_step(c, tmp, c->scr);
+  smooth_step(c, c->scr, tmp);
+  smooth_step(c, tmp, c->scr);
   CK(cudaMemcpyAsync(kp.pre, c->scr, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
   launch_lim_reset(&c->sc->lim, c->s);
   launch_limiter_pass1(c->scr, c->def, c->rho, n, dtold, dtaumesh, &c->sc->lim, kp.mk, kp.mk + n3, c->s);
-  launch_smooth27<double>(c->scr, n, tmp, c->s);
+  smooth_step(c, c->scr, tmp);
   launch_fill<double>(defp, n3, 0.0, c->s);
   int st = multigrid_level(c, 0, 1.0, d);
   if (st != MMH_OK) return st;
   CK(cudaMemcpyAsync(kp.ratio, &c->sc->ratio, sizeof(double), cudaMemcpyDeviceToDevice, c->s));
   CK(cudaMemcpyAsync(kp.uf, defp, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
-  launch_smooth27<double>(defp, n, c->scr, c->s);
-  launch_smooth27<double>(c->scr, n, defp, c->s);
+  smooth_step(c, defp, c->scr);
+  smooth_step(c, c->scr, defp);
   launch_limiter_mask(c->defplim, c->def, defp, n, dtold, &c->sc->lim, nullptr, c->s);
   RET(pull_scal(c));
   lim_to_diag(c->hsc->lim, d);
