@@ -200,7 +200,9 @@ int mmh_power_spectrum_f64(mmh_ctx* ctx, const double* a, const double* b, int n
  * mass shared equally by its cells, normalised to mean 1.  raw (ng^3, may be
  * NULL) receives the density before normalisation, wp (np, may be NULL) the
  * cells of each particle.  ng <= 1024, np < 2^31.  MMH_ERR_RANGE when a
- * position falls outside the grid after the wrap.  No context: the call
+ * position falls outside the grid after the wrap, or when an empty cell has
+ * no particle within 64 cells (the search's cost grows as the cube of that
+ * distance; the reference would keep searching).  No context: the call
  * allocates and frees its own device memory on the current device. */
 int mmh_haloden(const float* x, long long np, int nf, int ng, float* den, float* raw, int* wp);
 /* from1024to512.f90: ncoarse halvings of an ng^3 density by 2x2x2 block sums,
@@ -213,7 +215,8 @@ int mmh_coarsen(const float* den, int ng, int ncoarse, float* out);
  * dspz of def, and for each column the density between the displaced faces
  * of cells ng/2 and ng/2+nplot-1 with fractional end cells, divided by nplot.
  * Cells outside 1..ng wrap periodically (the reference reads past the array
- * there).  The sum that scales den is exact, rounded once. */
+ * there); faces more than 4 ng cells apart give MMH_ERR_RANGE.  The sum that
+ * scales den is exact, rounded once. */
 int mmh_column_density(const float* den, const float* def, int ng, int nplot, float* proj);
 /* gridfigure.f90:41-120: the displacement of a coarse def (nf^3) on the
  * reference's (0:nf)^3 node grid with its halo, interpolated to the fine

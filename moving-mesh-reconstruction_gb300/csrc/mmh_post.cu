@@ -50,7 +50,13 @@ struct Norm {
 // column_density.f90:42-53: the column of (i, j) between the displaced faces
 // kk1 and kk2 with fractional end cells (cells outside 1..ng wrap; the
 // reference reads out of bounds there)
-__device__ float column(const Norm& D, int i, int j, float kk1, float kk2) {
+__device__ float column(const Norm& D, int i, int j, float kk1, float kk2, int* flag) {
+  // faces more than 4 ng cells apart (displacements of several boxes) or not
+  // finite: flagged, not summed
+  if (!(fabsf(kk2 - kk1) <= 4.0f * (float)D.ng) || !(fabsf(kk1) < 1.0e9f)) {
+    atomicOr(flag, 2);
+    return 0.0f;
+  }
   int nk1 = (int)floorf(kk1) + 1, nk2 = (int)floorf(kk2) + 1;
   float r1 = (float)nk1 - kk1;
   float r2 = kk2 - (float)nk2 + 1.0f;
@@ -77,7 +83,7 @@ __device__ __forceinline__ float dspz(const float* __restrict__ def, int ng, int
 }
 
 __global__ void k_column_density(const float* __restrict__ den, const float* __restrict__ def, int ng, int nplot,
-                                 const unsigned long long* acc, float* __restrict__ proj) {
+                                 const unsigned long long* acc, float* __restrict__ proj, int* flag) {
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (i64)ng * ng) return;
   int i = (int)(t % ng) + 1, j = (int)(t / ng) + 1;
@@ -92,7 +98,7 @@ __global__ void k_column_density(const float* __restrict__ den, const float* __r
   b = b + dspz(def, ng, im, j, k2);
   b = b + dspz(def, ng, i, j, k2);
   float kk2 = (float)k2 + b / 4.0f;
-  proj[t] = column(D, i, j, kk1, kk2) / (float)nplot;
+  proj[t] = column(D, i, j, kk1, kk2, flag) / (float)nplot;
 }
 
 // gridfigure.f90:46-56: the displacement of the coarse def at the nodes
@@ -182,7 +188,7 @@ __device__ float grid_disp(const float* __restrict__ TD, int nf, int ratio, int 
 }
 
 __global__ void k_grid_column(const float* __restrict__ den, const float* __restrict__ TD, int nf, int ng,
-                              const unsigned long long* acc, float* __restrict__ proj) {
+                              const unsigned long long* acc, float* __restrict__ proj, int* flag) {
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (i64)ng * ng) return;
   const int ratio = ng / nf;
@@ -198,7 +204,7 @@ __global__ void k_grid_column(const float* __restrict__ den, const float* __rest
   b = b + grid_disp(TD, nf, ratio, 2, im, j, k2);
   b = b + grid_disp(TD, nf, ratio, 2, i, j, k2);
   float kk2 = (float)k2 + b / 4.0f;
-  proj[t] = column(D, i, j, kk1, kk2) / 1.0f;
+  proj[t] = column(D, i, j, kk1, kk2, flag) / 1.0f;
 }
 
 // proj2(1:2, a, b) = newposition(1:2, ratio*a, ratio*b, ng/2)
@@ -249,7 +255,7 @@ int mmh_column_density(const float* den, const float* def, int ng, int nplot, fl
   QK(cudaMemcpy(ddef, def, sizeof(float) * n3, cudaMemcpyHostToDevice));
   QK(cudaMemset(acc, 0, 24));
   k_post_fsum<<<(unsigned)std::min<i64>(nblk(n3), 152 * 8), kB>>>(dden, n3, acc, flag);
-  k_column_density<<<nblk((i64)ng * ng), kB>>>(dden, ddef, ng, nplot, acc, dproj);
+  k_column_density<<<nblk((i64)ng * ng), kB>>>(dden, ddef, ng, nplot, acc, dproj, flag);
   count_launch(2);
   QK(cudaGetLastError());
   int hflag = 0;
@@ -280,7 +286,7 @@ int mmh_gridfigure(const float* def, int nf, const float* den, int ng, float* pr
   k_grid_nodes<<<nblk(m3), kB>>>(ddef, nf, T0);
   k_grid_halo<<<nblk(m3), kB>>>(T0, nf, cf, TD);
   k_post_fsum<<<(unsigned)std::min<i64>(nblk(n3), 152 * 8), kB>>>(dden, n3, acc, flag);
-  k_grid_column<<<nblk((i64)ng * ng), kB>>>(dden, TD, nf, ng, acc, dproj);
+  k_grid_column<<<nblk((i64)ng * ng), kB>>>(dden, TD, nf, ng, acc, dproj, flag);
   k_grid_positions<<<nblk((i64)nf * nf), kB>>>(TD, nf, ng, dproj2);
   count_launch(5);
   QK(cudaGetLastError());

@@ -28,6 +28,8 @@ namespace mmh {
 namespace {
 
 constexpr int kB = 256;
+// largest search radius (cells) of an empty cell's nearest-particle search
+constexpr int kHaloMaxRadius = 64;
 unsigned blocks_of(i64 count) { return (unsigned)((count + kB - 1) / kB); }
 
 // Fortran MODULO for reals: the exact remainder, moved into [0, p).
@@ -73,19 +75,21 @@ __global__ void k_halo_bounds(const unsigned* __restrict__ key, i64 np, int* __r
 // (haloden.f90:127-170).  Cells are scanned in the reference's order (k_s, j_s,
 // i_s), each cell's particles in its linked-list order (descending index), and
 // only a strictly smaller distance replaces the choice, so ties go as there.
+// The shells grow to at most rmax cells; a cell with no particle within that
+// radius sets flag bit 4 (the reference's search would go on, and so would
+// its cost: (2r+1)^3 cells per empty cell).  Launched on cells [g0, g1).
 __global__ void k_halo_search(const float* __restrict__ xp, const unsigned* __restrict__ order,
-                              const int* __restrict__ first, const int* __restrict__ last, int ng,
-                              int* __restrict__ choice, int* __restrict__ wp) {
-  i64 ng3 = (i64)ng * ng * ng;
-  i64 g = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= ng3) return;
+                              const int* __restrict__ first, const int* __restrict__ last, int ng, int rmax,
+                              i64 g0, i64 g1, int* __restrict__ choice, int* __restrict__ wp, int* flag) {
+  i64 g = g0 + (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= g1) return;
   if (first[g] >= 0) return;
   int i = (int)(g % ng), j = (int)((g / ng) % ng), k = (int)(g / ((i64)ng * ng));
   const float gx = (float)(i + 1) - 0.5f, gy = (float)(j + 1) - 0.5f, gz = (float)(k + 1) - 0.5f;
   const float h = (float)(ng / 2), fng = (float)ng;
   float r2min = (float)(1000 * ng * ng);
   int best = -1;
-  for (int r = 1; r <= ng && best < 0; ++r) {
+  for (int r = 1; r <= rmax && best < 0; ++r) {
     for (int dk = -r; dk <= r; ++dk)
       for (int dj = -r; dj <= r; ++dj)
         for (int di = -r; di <= r; ++di) {
@@ -111,6 +115,7 @@ __global__ void k_halo_search(const float* __restrict__ xp, const unsigned* __re
   }
   choice[g] = best;
   if (best >= 0) atomicAdd(&wp[best], 1);
+  else atomicOr(flag, 4);
 }
 
 // the unnormalised density (haloden.f90:173-182): a cell's particles add
@@ -256,12 +261,23 @@ int mmh_haloden(const float* x, long long np, int nf, int ng, float* den, float*
   PK(cub::DeviceRadixSort::SortPairs(sort_tmp, sort_bytes, key, skey, ips, order, (int)np, 0, bits));
   k_halo_bounds<<<blocks_of(np), kB>>>(skey, np, first, last);
   k_fill_int<<<blocks_of(np), kB>>>(dwp, np, 1);
-  k_halo_search<<<blocks_of(ng3), kB>>>(xp, order, first, last, ng, choice, dwp);
+  // empty-cell searches in chunks, the flag read between them, so an input
+  // whose voids exceed the radius cap ends after one chunk
+  const int rmax = std::min(ng / 2 + 1, kHaloMaxRadius);
+  const i64 chunk = (i64)1 << 20;
+  for (i64 g0 = 0; g0 < ng3; g0 += chunk) {
+    const i64 g1 = std::min(ng3, g0 + chunk);
+    k_halo_search<<<blocks_of(g1 - g0), kB>>>(xp, order, first, last, ng, rmax, g0, g1, choice, dwp, flag);
+    count_launch();
+    int hf = 0;
+    PK(cudaMemcpy(&hf, flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (hf & 4) return MMH_ERR_RANGE;
+  }
   k_halo_density<<<blocks_of(ng3), kB>>>(order, first, last, choice, dwp, ng3, draw);
   k_fsum<<<sum_blocks(ng3), kB>>>(draw, ng3, acc, flag);
   const double scale = (double)((float)ng * (float)ng * (float)ng);
   k_halo_norm<<<blocks_of(ng3), kB>>>(draw, ng3, acc, scale, dden);
-  count_launch(6);
+  count_launch(5);
   PK(cudaGetLastError());
   int hflag = 0;
   PK(cudaMemcpy(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost));
