@@ -137,13 +137,14 @@ def test_gpu_haloden_matches_oracle(mmh, oracle, kind, np_, nf, ng):
 
 @pytest.mark.gpu
 def test_gpu_haloden_search_radius_cap(mmh):
-    """A void whose centre is more than 64 cells from every particle: the
-    search stops at its radius cap and the call reports MMH_ERR_RANGE."""
+    """A void whose centre is more than 64 shells (cube shells, the search's
+    own radius) from every particle: the search stops at its radius cap and
+    the call reports MMH_ERR_RANGE."""
     ng = 144
     c = np.arange(ng, dtype=np.float32) + 0.5
     X, Y, Z = np.meshgrid(c, c, c, indexing="ij")
-    r2 = (X - ng / 2) ** 2 + (Y - ng / 2) ** 2 + (Z - ng / 2) ** 2
-    keep = r2 > 66.5 ** 2
+    cheb = np.maximum(np.maximum(np.abs(X - ng / 2), np.abs(Y - ng / 2)), np.abs(Z - ng / 2))
+    keep = cheb > 66.5
     x = np.stack([X[keep], Y[keep], Z[keep]]).astype(np.float32)
     with pytest.raises(mmh.MMHError) as e:
         mmh.haloden(x, ng, ng)
