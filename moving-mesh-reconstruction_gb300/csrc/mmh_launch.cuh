@@ -61,7 +61,10 @@ void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nswe
   if (n <= 8) {
     if (nsweeps > 0) {
       prof_begin(kk<T>(KK_GS), s, h3 * 8 * nsweeps, n);
-      k_gs_small_sm<T><<<1, 512, sizeof(T) * 8 * n * n * n, s>>>(phi, rhs, coef, n, dx2, nsweeps);
+      // one thread per cell of a colour (8 at 4^3, 64 at 8^3), whole warps: the
+      // colour phases' barriers then span one or two warps instead of 16
+      const int nt = (int)std::max<i64>(32, (h3 + 31) / 32 * 32);
+      k_gs_small_sm<T><<<1, nt, sizeof(T) * 8 * n * n * n, s>>>(phi, rhs, coef, n, dx2, nsweeps);
       prof_end(kk<T>(KK_GS), s, n);
       count_launch();
     }
