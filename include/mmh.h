@@ -294,7 +294,8 @@ int mmh_relaxing_adjoint_f64(mmh_ctx* ctx, const double* u, const double* def, c
  * (wdef, wdelta: n^3 host arrays, NULL: zero), the limiter and slope-limiter
  * branches frozen as above.  The forward states are kept every
  * checkpoint_every iterations and the others recomputed as the adjoint walks
- * back.  Needs a solving schedule; the state ends as after mmh_iterate(niter). */
+ * back.  Needs a solving schedule; the state ends as after mmh_iterate(niter)
+ * (after an error it is the failing step's: reload before reuse). */
 int mmh_iterate_adjoint_f64(mmh_ctx* ctx, int niter, int checkpoint_every, const double* wdef, const double* wdelta,
                             double* grho, double* gdef, mmh_diag* diag);
 
