@@ -2,6 +2,7 @@
 // tolerance schedules, FP64 and mixed precision), calcdefp, relaxing, spectral
 // outputs, and the C ABI declared in include/mmh.h.
 #include <cufft.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -62,6 +63,13 @@ struct Err {
   } while (0)
 
 bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+// NVTX range over one stage of the path (calcdefp, multigrid, relaxing,
+// spectral outputs, adjoint) for profilers; free when none is attached.
+struct Stage {
+  explicit Stage(const char* name) { nvtxRangePushA(name); }
+  ~Stage() { nvtxRangePop(); }
+};
 int ilog2(int n) {
   int l = 0;
   while ((1 << l) < n) ++l;
@@ -534,6 +542,7 @@ int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_
 // multigrid(u, rhs, defpot, ubig, dx, ...) at level l0: u = h64.u[l0],
 // rhs = h64.rhs[l0], defpot = defl[l0], density = rhol[l0] already in place.
 int multigrid_level(mmh_ctx* c, int l0, double dx, mmh_diag* d) {
+  Stage stage_("mmh multigrid");
   int n = c->nl[l0];
   i64 n3 = (i64)n * n * n;
   CK(cudaMemsetAsync(c->sc, 0, offsetof(Scal, lim), c->s));
@@ -685,6 +694,7 @@ void smooth_step(mmh_ctx* c, double* in, double* out) {
 
 // calcdefp on the resident state: defp (= h64.u[0]) from def and rho.
 int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t* mc1, uint8_t* mc2, mmh_diag* d) {
+  Stage stage_("mmh calcdefp");
   int n = c->n;
   i64 n3 = c->n3;
   if (dtold < 1.e-8) dtold = 1.0;
@@ -716,6 +726,7 @@ int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t
 
 // relaxing(u, def, defp, cmax, dt, 5) on the resident density.
 int relaxing_dev(mmh_ctx* c, double dt) {
+  Stage stage_("mmh relaxing");
   int n = c->n;
   const bool fast = c->cfg.precision == MMH_MIXED;  // one reciprocal per division site
   launch_relax_stage1(c->rho, c->def, c->defp(), n, c->baj, c->cc, c->vt, c->s, fast);
@@ -727,6 +738,7 @@ int relaxing_dev(mmh_ctx* c, double dt) {
 
 // spectral outputs of src into host/device buffers (grad: 3 planes of n^3)
 int spectral_outputs(mmh_ctx* c, const double* src, double* d_grad, double* d_delta) {
+  Stage stage_("mmh spectral outputs");
   RET(make_plans(c));
   CKF(cufftExecD2Z(c->pd2z, (cufftDoubleReal*)src, (cufftDoubleComplex*)c->Xc));
   for (int ax = 0; ax < 3 && d_grad; ++ax) {
@@ -929,6 +941,7 @@ int relaxing_adjoint_dev(mmh_ctx* c, double dt, const double* ubar, double* gu, 
 // resident state ends as (def_N, rho_N); the defp buffer is scratch.
 int iterate_adjoint_dev(mmh_ctx* c, int niter, int every, const double* wdef, const double* wdelta, double* grho,
                         double* gdef, mmh_diag* d) {
+  Stage stage_("mmh adjoint");
   if (c->cfg.schedule == MMH_SCHED_REF) return MMH_ERR_UNSUPPORTED;
   if (niter < 0 || every < 1) return MMH_ERR_ARG;
   const i64 n3 = c->n3;

@@ -27,8 +27,10 @@ MMH_SCHED_TOL = 1      # flexible CG, one V-cycle per iteration as preconditione
 MMH_SCHED_VCYCLE = 2   # plain repeated V-cycles
 
 MMH_OK = 0
+MMH_ERR_NAN = -5
 MMH_ERR_DIVERGED = -6
 MMH_ERR_UNSUPPORTED = -7
+MMH_ERR_RANGE = -8
 
 # every entry point of include/mmh.h
 EXPORTS = (

@@ -351,3 +351,31 @@ def test_errors(mmh, fields):
     with pytest.raises(mmh.MMHError) as e:
         mmh.Context(16, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_REF)
     assert e.value.code == -1
+
+
+def test_injected_failures(mmh, fields):
+    """Failures made on the host, never on the GPU: a NaN seeded into the
+    density, a deformation potential whose determinants leave the exact-sum
+    range, a solve allowed too few cycles.  Each call returns its status and
+    the context stays usable."""
+    n = 16
+    rho = fields.lognormal_density(n, sigma=0.5, seed=5)
+    z = np.zeros((n, n, n), order="F")
+    defp = np.zeros((n, n, n), order="F")
+    failed = (mmh.MMH_ERR_NAN, mmh.MMH_ERR_RANGE)
+    with mmh.Context(n, precision=mmh.MMH_FP64, schedule=mmh.MMH_SCHED_TOL, tol=1e-10, max_cycles=200) as ctx:
+        bad = rho.copy(order="F")
+        bad[3, 4, 5] = np.nan
+        with pytest.raises(mmh.MMHError) as e:
+            ctx.calcdefp(defp, None, None, z, bad, 1.0, 1.0, nfluid=1)
+        assert e.value.code in failed
+        spike = np.zeros((n, n, n), order="F")
+        spike[7, 7, 7] = 1e12
+        with pytest.raises(mmh.MMHError) as e:
+            ctx.calcdefp(defp, None, None, spike, rho, 1.0, 1.0, nfluid=1)
+        assert e.value.code in failed
+        d = ctx.calcdefp(defp, None, None, z, rho, 1.0, 1.0, nfluid=1)
+        assert d["status"] == 0 and np.isfinite(defp).all()
+    with mmh.Context(n, precision=mmh.MMH_FP64, schedule=mmh.MMH_SCHED_TOL, tol=1e-14, max_cycles=2) as ctx:
+        d = ctx.calcdefp(defp, None, None, z, rho, 1.0, 1.0, nfluid=1)
+        assert d["status"] == mmh.MMH_ERR_DIVERGED
