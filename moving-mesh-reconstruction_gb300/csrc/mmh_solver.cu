@@ -468,45 +468,23 @@ int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_
     if (status != MMH_OK && status != MMH_ERR_DIVERGED) return status;
     total = it;
     *r1_out = r0;
-  } else if (c->cfg.tol >= kFFTolMin) {
-    // The outer solution and the fine coefficients are carried as
-    // float-float pairs in their own buffers (the FP32 copy of the
-    // coefficients is already made): the outer residual then runs on the
-    // FP32 pipes at ~48-bit accuracy (k_residual_ff).
-    launch_ff_split(c->h64.coef[l0], 6 * n3, c->s);
-    launch_ff_split(c->px, n3, c->s);
-    double rmax = 0.0;
-    for (int outer = 0;; ++outer) {
-      RET(true_residual_ff(c, l0, dx, c->px, c->pb, c->pb32, &rmax));
-      rel = rmax / rn;
-      if (outer == 0) *r1_out = rmax;
-      if (!(rel == rel)) return MMH_ERR_NAN;
-      if (rel <= c->cfg.tol) break;
-      if (total >= c->cfg.max_cycles) {
-        status = MMH_ERR_DIVERGED;
-        break;
-      }
-      launch_fill<float>(c->pe32, n3, 0.0f, c->s);
-      int it = 0;
-      double rin = 0.0, r0 = 0.0;
-      int st = pcg_core<float>(c, l0, dx, c->pe32, c->pb32, c->pp32, c->pq32, rmax, kInnerTol, kInnerMax, &it, &rin,
-                               &r0);
-      if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
-      total += it;
-      launch_ff_add_f(c->px, c->pe32, n3, c->s);
-    }
-    // zero mean (the exact sum of all hi and lo parts), residual, back to FP64
-    CK(cudaMemsetAsync(c->sc->acc[0], 0, 16, c->s));
-    launch_fxsum<float>(reinterpret_cast<const float*>(c->px), 2 * n3, c->sc->acc[0], &c->sc->bad, c->s);
-    launch_fx_mean(c->sc->acc[0], (double)n3, &c->sc->mean, c->s);
-    launch_ff_sub_mean(c->px, &c->sc->mean, n3, c->s);
-    RET(true_residual_ff(c, l0, dx, c->px, c->pb, nullptr, &rt));
-    launch_ff_join(c->px, n3, c->s);
   } else {
-    // tolerances below the float-float residual's rounding floor: FP64 outer loop
+    // For tol >= kFFTolMin the outer solution and the fine coefficients are
+    // carried as float-float pairs in their own buffers (the FP32 copy of the
+    // coefficients is already made): the outer residual then runs on the FP32
+    // pipes at ~48-bit accuracy (k_residual_ff).  Tighter tolerances keep the
+    // FP64 residual of an FP64 solution.
+    const bool ff = c->cfg.tol >= kFFTolMin;
+    if (ff) {
+      launch_ff_split(c->h64.coef[l0], 6 * n3, c->s);
+      launch_ff_split(c->px, n3, c->s);
+    }
+    auto outer_residual = [&](float* r32, double* r) {
+      return ff ? true_residual_ff(c, l0, dx, c->px, c->pb, r32, r) : true_residual(c, l0, dx, c->px, c->pb, r32, r);
+    };
     double rmax = 0.0;
     for (int outer = 0;; ++outer) {
-      RET(true_residual(c, l0, dx, c->px, c->pb, c->pb32, &rmax));
+      RET(outer_residual(c->pb32, &rmax));
       rel = rmax / rn;
       if (outer == 0) *r1_out = rmax;
       if (!(rel == rel)) return MMH_ERR_NAN;
@@ -522,7 +500,19 @@ int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_
                                &r0);
       if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
       total += it;
-      launch_add_f2d(c->px, c->pe32, n3, c->s);
+      if (ff)
+        launch_ff_add_f(c->px, c->pe32, n3, c->s);
+      else
+        launch_add_f2d(c->px, c->pe32, n3, c->s);
+    }
+    if (ff) {
+      // zero mean (the exact sum of all hi and lo parts), residual, back to FP64
+      CK(cudaMemsetAsync(c->sc->acc[0], 0, 16, c->s));
+      launch_fxsum<float>(reinterpret_cast<const float*>(c->px), 2 * n3, c->sc->acc[0], &c->sc->bad, c->s);
+      launch_fx_mean(c->sc->acc[0], (double)n3, &c->sc->mean, c->s);
+      launch_ff_sub_mean(c->px, &c->sc->mean, n3, c->s);
+      RET(outer_residual(nullptr, &rt));
+      launch_ff_join(c->px, n3, c->s);
     }
   }
   if (c->cfg.precision == MMH_FP64 || c->cfg.tol < kFFTolMin) {
