@@ -65,3 +65,18 @@ def test_power_spectrum_matches_numpy(mmh, fields, n):
             assert np.all(p[~full] == 0)
         if n == 128:
             assert {q + 1 for q in range(48) if m[q] == 0} == SKIPPED_AT_128
+
+
+def test_spectrum_file_layout(mmh, tmp_path):
+    """write_spectrum gives what calcfisherinfo.f90:41-49 reads list-directed
+    into tmp(:, 1:2, 1:48): per bin the k then the power, whitespace-separated,
+    read back exactly."""
+    k = np.logspace(0, np.log10(64), 48)
+    p = np.random.default_rng(3).uniform(0, 1e4, 48)
+    path = str(tmp_path / "ps48bins_128_2.txt")
+    mmh.write_spectrum(path, k, p)
+    flat = np.array(open(path).read().split(), dtype=np.float64)
+    assert flat.size == 96
+    # Fortran column-major fill of a (2, 48) array: k_1, P_1, k_2, P_2, ...
+    got = flat.reshape((2, 48), order="F")
+    assert np.array_equal(got[0], k) and np.array_equal(got[1], p)
