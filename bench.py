@@ -10,16 +10,21 @@ FP64, followed by the spectral displacement and density outputs.  One "step"
 is one such reconstruction; the metric is seconds per reconstruction.
 
   value   : mixed form (FP32 V-cycles in an FP64 defect-correction loop), input
-            density resident in HBM, CUDA events on the library's stream.
+            density resident in HBM, CUDA events on the library's stream,
+            kernel timing hooks off (the production configuration).
   e2e     : the same through the C ABI with host buffers: H2D of the density
             from pinned memory, D2H of def, the displacement and the density
             outputs, all inside the timed region.
   fp64    : the plain FP64 GPU form of the same workload, for the mixed/FP64
-            ratio the metric asks for.
-  roofline: the dominant kernel timed live over the timed region with CUDA
-            events (achieved = algorithmic bytes / device time) against the
+            ratio the metric asks for; `errors` gives the mixed form's
+            per-field difference from it.
+  roofline: the dominant kernel's launches on the finest level, timed one by
+            one with CUDA events in a separate reconstruction after the timed
+            ones (achieved = algorithmic bytes / device time) against the
             measured HBM copy bandwidth.
-  cpu_baseline: the CPU oracle (FP64, all host threads) on a bounded sample.
+  cpu_baseline: the CPU oracle (FP64, all host threads) on complete work: one
+            whole deformation iteration and the outputs of a 256^3 instance,
+            scaled to the reconstruction.
 
 --batch and --adjoint print the batched-realisation line and the adjoint
 line (the density gradient of a band-power loss at 256^3) instead.
@@ -47,14 +52,16 @@ import numpy as np  # noqa: E402
 
 METRIC = "s per 512³ reconstruction to residual 1e-8: mixed vs FP64 GPU; stencil HBM GB/s"
 UNIT = "s/reconstruction"
-# Algorithmic words per processed cell.  One launch of the fused Gauss-Seidel
-# plane kernel updates every cell of the planes of one parity (n^3/2 cells):
-# it must read phi, rhs and the 6 metric coefficients of those planes (8 words
-# per updated cell), phi and coefficients 3, 5, 6 of the planes of the other
-# parity (4 words per updated cell, each plane once although two planes use
-# it) and write phi (1 word): 13 words.  The residual reads phi, rhs and the 6
-# coefficients and writes r: 9 words per cell.
-ALG_WORDS = {"gs": 13, "residual": 9}
+# Algorithmic words per processed cell (the minimum one pass must move).  A
+# Gauss-Seidel sweep must read phi, rhs and the 6 metric coefficients of every
+# cell and write phi: 9 words per updated cell.  The residual reads phi, rhs
+# and the 6 coefficients and writes r: 9 words per cell.
+ALG_WORDS = {"gs": 9, "residual": 9}
+# Words per updated cell the current kernel itself moves: one launch of the
+# fused plane kernel updates the planes of one parity and also reads phi and
+# coefficients 3, 5, 6 of the other parity's planes (4 more words per updated
+# cell).
+KERNEL_WORDS = {"gs": 13, "residual": 9}
 KERNEL_NAME = {"gs32": "k_gs_plane<float,32,16>", "gs64": "k_gs_plane<double,32,8>",
                "res64": "k_residual<double>", "res32": "k_residual<float>"}
 
@@ -74,8 +81,11 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=1, help="timed FP64 reconstructions (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-sample", default="auto", choices=["auto", "none"])
-    ap.add_argument("--cpu-n", type=int, default=0, help="grid of the CPU sample (default: --n)")
+    ap.add_argument("--cpu-n", type=int, default=256, help="grid of the CPU sample's complete iteration")
     ap.add_argument("--profile", default="gs32", choices=["gs32", "gs64", "res64", "res32", "none"])
+    ap.add_argument("--roofline-steps", type=int, default=1,
+                    help="reconstructions run after the timed ones with the profiled kernel's launches timed")
+    ap.add_argument("--errors", type=int, default=1, help="report the mixed form's per-field error vs the FP64 form")
     ap.add_argument("--batch", action="store_true",
                     help="batched-realisations workload (mmh_batch_run) instead of the headline reconstruction")
     ap.add_argument("--adjoint", action="store_true",
@@ -143,67 +153,84 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU oracle sample (test infrastructure timed as the baseline)
 # ---------------------------------------------------------------------------
-def cpu_sample(n, niter, sigma, seed, tol, cycles_hint=None):
-    """Time the oracle (FP64, tolerance schedule, 8-colour order, all host
-    threads) on a bounded sample of the workload and scale it to seconds per
-    reconstruction: one deformation iteration with the solve capped at one
-    V-cycle (t1) and at two V-cycles (t2); t_v = t2 - t1 is one V-cycle.
-    The V-cycles per solve C are measured by the oracle itself on a 64^3
-    instance solved to tol.  s/reconstruction = niter * (t1 + (C - 1) * t_v)."""
+def _oracle_outputs_seconds(oracle, d):
+    t = time.perf_counter()
+    oracle.gradient(d)
+    oracle.delta(d)
+    return time.perf_counter() - t
+
+
+def cpu_sample(n_full, niter, sigma, seed, tol, n_sample=256):
+    """Time the oracle (FP64, tolerance schedule as the GPU runs it, 8-colour
+    order, all host threads) on complete work: one whole deformation
+    iteration (calcdefp with its solve run to tol, def += defp, relaxing) of
+    an n_sample^3 instance of the workload (same recipe, sigma and seed), and
+    the spectral outputs of its def.  Nothing is modelled inside the sample:
+    it is the path's full work for one iteration.  It is scaled to one
+    n_full^3 reconstruction by the cell count (n_full/n_sample)^3 and by the
+    niter iterations; the solves' iteration counts at n_full are within a few
+    of n_sample's (13 and 14 PCG iterations at 256^3 and 512^3)."""
     import oracle
     import fields
     threads = oracle.threads(0)
-    rho = fields.lognormal_density(n, sigma=sigma, seed=seed)
-    u = np.asfortranarray(rho.reshape((1,) + rho.shape))
-    d0 = np.zeros_like(rho, order="F")
-    times = []
-    for cyc in (1, 2):
-        t = time.perf_counter()
-        oracle.calcdefp(d0, u, sched=oracle.SCHED_TOL, tol=tol, maxcyc=cyc, colour8=True)
-        times.append(time.perf_counter() - t)
-    t1, t2 = times
-    tv = max(t2 - t1, 0.0)
-    if cycles_hint is None:
-        m = 64
-        r64 = fields.lognormal_density(m, sigma=sigma, seed=seed)
-        _, _, dg, _ = oracle.calcdefp(np.zeros_like(r64, order="F"), np.asfortranarray(r64.reshape((1,) + r64.shape)),
-                                      sched=oracle.SCHED_TOL, tol=tol, maxcyc=500, colour8=True)
-        cycles = float(dg["vcycles"])
-        src = f"oracle 64^3 solve to {tol:g}"
-    else:
-        cycles = float(cycles_hint)
-        src = "GPU FP64 run of the same workload"
-    value = niter * (t1 + (cycles - 1.0) * tv)
+    defpot, u = fields.initial_state(n_sample, sigma=sigma, seed=seed)
+    kw = dict(sched=oracle.SCHED_TOL, tol=tol, maxcyc=500, colour8=True)
+    t = time.perf_counter()
+    d, _, _, _, diag = oracle.iteration(defpot, u, **kw)
+    t_it = time.perf_counter() - t
+    t_out = _oracle_outputs_seconds(oracle, d)
+    scale = (n_full / n_sample) ** 3
+    value = scale * (niter * t_it + t_out)
     return {
         "value": value, "unit": UNIT, "cores": threads, "kind": "port",
-        "sample": (f"oracle FP64 on {n}^3: one deformation iteration with the solve capped at 1 V-cycle "
-                   f"({t1:.2f} s) and at 2 ({t2:.2f} s); scaled to {niter} iterations x {cycles:.1f} V-cycles "
-                   f"per solve ({src}); {threads} threads"),
-        "sample_seconds": t1 + t2,
+        "sample": (f"oracle FP64 (tolerance schedule to {tol:g}, {threads} threads): one complete deformation "
+                   f"iteration of the {n_sample}^3 instance ({t_it:.2f} s, {diag['vcycles']} PCG iterations) and its "
+                   f"spectral outputs ({t_out:.2f} s), scaled by {niter} iterations and by the cell count "
+                   f"({n_full}/{n_sample})^3 = {scale:g}"),
+        "sample_seconds": t_it + t_out,
     }
 
 
 def reference_arm(args):
-    """--impl reference: the CPU restatement on the host cores (rank 0 only)."""
+    """--impl reference: the CPU restatement of the reference path on all the
+    host cores (rank 0 only; the Fortran reference has no compiler here).
+    Each step is one complete deformation iteration (calcdefp with its solve
+    run to tol, def += defp, relaxing) of a cpu_n^3 instance of the workload,
+    each step continuing the previous one's state; the warm-up steps are the
+    first iterations.  The spectral outputs of the final def are timed once.
+    value = (niter * median step + outputs) * (n / cpu_n)^3 seconds per n^3
+    reconstruction."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    n = args.cpu_n or args.n
-    for _ in range(args.warmup):  # warm-up on a small grid (first touch, thread pool)
-        cpu_sample(64, 1, args.sigma, args.seed, args.tol, cycles_hint=1)
-    vals, last = [], None
+    import oracle
+    import fields
+    threads = oracle.threads(0)
+    m = args.cpu_n or 256
+    defpot, u = fields.initial_state(m, sigma=args.sigma, seed=args.seed)
+    kw = dict(sched=oracle.SCHED_TOL, tol=args.tol, maxcyc=500, colour8=True)
+    for _ in range(args.warmup):
+        defpot, u, _, _, _ = oracle.iteration(defpot, u, **kw)
+    times = []
     t0 = time.perf_counter()
     for _ in range(max(args.steps, 1)):
-        last = cpu_sample(n, args.niter, args.sigma, args.seed, args.tol)
-        vals.append(last["value"])
+        t = time.perf_counter()
+        defpot, u, _, _, diag = oracle.iteration(defpot, u, **kw)
+        times.append(time.perf_counter() - t)
+    t_out = _oracle_outputs_seconds(oracle, defpot)
     wall = time.perf_counter() - t0
-    v = statistics.median(vals)
+    scale = (args.n / m) ** 3
+    v = scale * (args.niter * statistics.median(times) + t_out)
+    sample = (f"oracle FP64 (tolerance schedule to {args.tol:g}, {threads} threads): complete deformation "
+              f"iterations of the {m}^3 instance, one per step (median {statistics.median(times):.2f} s, last solve "
+              f"{diag['vcycles']} PCG iterations), spectral outputs {t_out:.2f} s; scaled by {args.niter} iterations "
+              f"and by the cell count ({args.n}/{m})^3 = {scale:g}")
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * wall / max(args.steps, 1), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args),
-        "cpu_baseline": {k: last[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the Fortran reference cannot be compiled here (no Fortran compiler); the CPU restatement "
                 "in oracle/ stands in for it",
@@ -442,20 +469,35 @@ def main():
         ms = max_over_ranks(e0.elapsed_time(e1) / steps, dev)
         return ms, diags, mmh.launch_count() - launches0, prof
 
-    # ---- mixed (headline value) ----
+    # ---- mixed (headline value): timing hooks off, graph replay on ----
     ctx = make_ctx(mmh.MMH_MIXED)
     for _ in range(args.warmup):
         recon(ctx)
         ctx.sync()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_mixed, diags, launches, _ = timed(ctx, args.steps)
+    clk = clocks.stop()
+
+    # ---- roofline pass: one more reconstruction with the dominant kernel's
+    # launches on the finest level timed one by one (hooks armed: the
+    # preconditioner then runs launch by launch, not from its graph) ----
     kinds = {"gs32": mmh.K_GS | mmh.K_F32, "gs64": mmh.K_GS, "res64": mmh.K_RESIDUAL,
              "res32": mmh.K_RESIDUAL | mmh.K_F32, "none": None}
     pk = kinds[args.profile]
-    if pk is not None:
+    prof = None
+    if pk is not None and args.roofline_steps > 0:
         pk |= mmh.K_AT(n)  # the finest grid level only: the launches that dominate the step
-    clocks = ClockSampler(local)
-    clocks.start()
-    ms_mixed, diags, launches, prof = timed(ctx, args.steps, pk)
-    clk = clocks.stop()
+        ms_prof, _, _, prof = timed(ctx, args.roofline_steps, pk)
+
+    # mixed results kept for the error against the FP64 form
+    keep = {}
+    if args.fp64_steps > 0 and args.errors:
+        keep["grad"] = grad_dev.clone()
+        keep["delta"] = delta_dev.clone()
+        keep["def"] = np.zeros((n, n, n), order="F")
+        keep["rho"] = np.zeros((1, n, n, n), order="F")
+        ctx.store(keep["def"], keep["rho"])
 
     # ---- e2e through the C ABI with host buffers ----
     rho_host = torch.from_numpy(rho_np.ravel(order="F").copy()).pin_memory()
@@ -494,14 +536,30 @@ def main():
 
     # ---- FP64 form ----
     fp64 = None
+    errors = None
     if args.fp64_steps > 0:
         c64 = make_ctx(mmh.MMH_FP64)
         recon(c64)
         c64.sync()
         ms64, d64, _, _ = timed(c64, args.fp64_steps)
-        c64.close()
         fp64 = {"value": ms64 / 1000.0, "unit": UNIT, "vcycles_last_solve": d64[-1]["vcycles"],
                 "resid_rel_last_solve": d64[-1]["resid_rel"], "steps": args.fp64_steps, "warmup": 1}
+        if keep:
+            # the mixed form's fields against the FP64 form's, both solved to
+            # tol: max |mixed - FP64| / max |FP64| per field
+            f_def = np.zeros((n, n, n), order="F")
+            f_rho = np.zeros((1, n, n, n), order="F")
+            c64.store(f_def, f_rho)
+
+            def rel_dev(a, b):
+                return float((a - b).abs().max() / b.abs().max())
+
+            errors = {"vs": f"FP64 GPU form of the same workload (solves to {args.tol:g})",
+                      "def": float(np.abs(keep["def"] - f_def).max() / np.abs(f_def).max()),
+                      "rho": float(np.abs(keep["rho"] - f_rho).max() / np.abs(f_rho).max()),
+                      "displacement": rel_dev(keep["grad"], grad_dev),
+                      "delta": rel_dev(keep["delta"], delta_dev)}
+        c64.close()
 
     if rank != 0:
         if dist:
@@ -515,21 +573,26 @@ def main():
         nl, pms, cells = prof
         word = 4 if args.profile.endswith("32") else 8
         kname = args.profile
-        words = ALG_WORDS["gs" if kname.startswith("gs") else "residual"]
-        alg_bytes = cells * words * word
+        unit = "gs" if kname.startswith("gs") else "residual"
+        alg_bytes = cells * ALG_WORDS[unit] * word
         achieved = alg_bytes / (pms / 1000.0) / 1e9
+        kern_bytes = cells * KERNEL_WORDS[unit] * word
         tr = traffic_from_profiles(KERNEL_NAME[kname])
         roofline = {"kernel": f"{KERNEL_NAME[kname]} on the {n}^3 level",
                     "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else peak_src,
+                    "alg_words_per_cell": ALG_WORDS[unit],
                     "traffic": (tr * cells / nl) if tr else None,
                     "alg_bytes_per_launch": alg_bytes / nl, "launches": nl,
-                    "avg_launch_ms": pms / nl, "share_of_step": (pms / args.steps) / ms_mixed}
+                    "avg_launch_ms": pms / nl, "share_of_step": (pms / args.roofline_steps) / ms_prof,
+                    "kernel_words_per_cell": KERNEL_WORDS[unit],
+                    "frac_kernel_words": kern_bytes / (pms / 1000.0) / 1e9 / hbm,
+                    "pass": f"{args.roofline_steps} reconstruction(s) after the timed ones, every launch of the "
+                            f"kernel on the {n}^3 level timed with CUDA events on its stream"}
 
     cpu = None
     if args.cpu_sample != "none" and not dist:
-        hint = fp64["vcycles_last_solve"] if fp64 else None
-        cpu = cpu_sample(args.cpu_n or n, args.niter, args.sigma, args.seed, args.tol, cycles_hint=hint)
+        cpu = cpu_sample(n, args.niter, args.sigma, args.seed, args.tol, n_sample=args.cpu_n)
         cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
     value = ms_mixed / 1000.0 / world  # whole-job seconds per reconstruction (replicas)
@@ -541,6 +604,7 @@ def main():
                 "h2d_bytes_per_step": 8 * n3, "d2h_bytes_per_step": 8 * 5 * n3, "clocks": e2e_clk},
         "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
         "fp64": fp64, "mixed_vs_fp64_speedup": (fp64["value"] / (ms_mixed / 1000.0)) if fp64 else None,
+        "errors": errors,
         "solve": {"vcycles_last": diags[-1]["vcycles"], "resid_rel_last": diags[-1]["resid_rel"],
                   "ncompress_last": diags[-1]["ncompress"], "guards_last": diags[-1]["guards"]},
         "cells_per_s": n3 * args.niter * world / (ms_mixed / 1000.0),

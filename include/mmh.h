@@ -127,6 +127,10 @@ int mmh_defp2delta(mmh_ctx* ctx, const float* indata, float* outdata, const int*
 int mmh_defp2delta_f64(mmh_ctx* ctx, const double* indata, double* outdata, const int* nn);
 
 /* ---- reference subroutines on the path (FP64 host arrays) ------------- */
+/* Each computes in the context's precision form: in an MMH_MIXED context
+ * mmh_metric_f64 takes one division per cell, mmh_nsmooth_f64 runs three axis
+ * passes and mmh_relaxing_f64 one reciprocal per division site (the kernels
+ * mmh_iterate runs in that form; not bit-matched to the reference). */
 /* relax(arr,resid,rhs,deformpot,u,rinf,dx,n,n,n,1,nrelax,iopt)  gauss1.f90:64
  * iopt = 8*isolver + iresidopt with isolver = 2; resid((n/2)^3) is written
  * when iresidopt is 1 or 3. */
@@ -178,6 +182,18 @@ typedef struct mmh_stats {
   long long rho_negative;
 } mmh_stats;
 int mmh_state_stats(mmh_ctx* ctx, mmh_stats* stats);
+
+/* The limiter's trigger masks of the last calcdefp run on the context
+ * (mmh_calcdefp*, mmh_iterate), for checking them against the reference's:
+ * expand and compress1 are pass 1's expansion and compression triggers
+ * (limiter.f90:335-370, the flux cell km of the tested plane), compress2 the
+ * final compression test's (limiter.f90:523-529); n^3 bytes each in the
+ * Fortran layout, 1 where the limiter acted; any pointer may be NULL.  The
+ * reference keeps no masks (it counts them, limiter.f90:657-667).  Keeping
+ * them is armed by mmh_keep_masks(ctx, 1), which costs 3 n^3 bytes of device
+ * memory; mmh_masks returns MMH_ERR_ARG while it is not armed. */
+int mmh_keep_masks(mmh_ctx* ctx, int on);
+int mmh_masks(mmh_ctx* ctx, unsigned char* expand, unsigned char* compress1, unsigned char* compress2);
 
 /* Binned power spectrum of a (n^3, host) -- or the cross spectrum with b (NULL:
  * auto) -- in the bins of the reference's Fisher inputs: nbins (<= 128) bins
@@ -257,10 +273,12 @@ int mmh_batch_run(const mmh_config* cfg, mmh_problem* probs, int count, int work
  * for n <= MMH_NOALLOC_MAX_N (7*64^3+2 doubles, about 14.7 MB, held on every
  * GPU that loads the library until the process exits).  Larger grids return
  * MMH_ERR_TOO_LARGE.  The first call on a device looks up the array's device
- * address; make that first call before any stream capture.  All calls share
- * the array, so calls that overlap on the GPU (concurrent streams, devices
- * sharing nothing else) race and must be serialised by the caller.  The call
- * synchronises `stream` (a cudaStream_t, NULL for the default stream). */
+ * address; make that first call before any stream capture.  All calls on one
+ * device share that device's array, so calls that overlap on the same GPU
+ * (concurrent streams or host threads) race and must be serialised by the
+ * caller; each device has its own copy.  iopt is bounded as in mmh_relax_f64.
+ * The call synchronises `stream` (a cudaStream_t, NULL for the default
+ * stream). */
 #define MMH_NOALLOC_MAX_N 64
 int mmh_relax_noalloc_f64(const double* d_deformpot, const double* d_rho, double* d_arr, const double* d_rhs,
                           double dx, int n, int nrelax, int iopt, double* rinf, void* stream);
@@ -303,7 +321,11 @@ int mmh_iterate_adjoint_f64(mmh_ctx* ctx, int niter, int checkpoint_every, const
 /* Arm CUDA-event timing of one kernel kind (MMH_K_* | MMH_K_F32 for the FP32
  * instantiation) on the stream it is launched on; mmh_profile_stop returns the
  * number of launches timed, their summed device time in ms and the number of
- * cells they processed (cells updated, for the Gauss-Seidel colour kernel). */
+ * cells they processed (cells updated, for the Gauss-Seidel colour kernel).
+ * The event pool grows with the launches timed; mmh_profile_stop returns
+ * MMH_ERR_NOMEM (with the figures of the launches it did time) when a launch
+ * went untimed because no event could be created.  While armed, the
+ * preconditioner cycle runs launch by launch instead of from its CUDA graph. */
 #define MMH_K_GS 1
 #define MMH_K_RESIDUAL 2
 #define MMH_K_RESTRICT_RESID 3

@@ -30,12 +30,22 @@ Prof g_prof;
 
 bool prof_armed() { return g_prof.kind != 0; }
 
+// Events are created in chunks as launches are timed (the pool grows with the
+// launch count: a 512^3 reconstruction times ~2400 finest-level launches).
+static bool prof_grow() {
+  const size_t have = g_prof.ev.size();
+  g_prof.ev.resize(have + 2 * 4096);
+  for (size_t q = have; q < g_prof.ev.size(); ++q)
+    if (cudaEventCreate(&g_prof.ev[q]) != cudaSuccess) {
+      g_prof.ev.resize(q);
+      g_prof.ev.resize(q & ~(size_t)1);
+      return false;
+    }
+  return true;
+}
+
 int prof_start(int kind) {
-  if (g_prof.ev.empty()) {
-    g_prof.ev.resize(2 * 8192);
-    for (auto& e : g_prof.ev)
-      if (cudaEventCreate(&e) != cudaSuccess) return -1;
-  }
+  if (g_prof.ev.empty() && !prof_grow()) return -1;
   g_prof.kind = kind;
   g_prof.used = 0;
   g_prof.dropped = 0;
@@ -53,7 +63,7 @@ static bool prof_match(int kind, int n) {
 
 void prof_begin(int kind, cudaStream_t s, i64 cells, int n) {
   if (!prof_match(kind, n)) return;
-  if (g_prof.used >= (int)g_prof.ev.size() / 2) {
+  if (g_prof.used >= (int)g_prof.ev.size() / 2 && !prof_grow()) {
     g_prof.dropped++;
     return;
   }

@@ -1,12 +1,29 @@
 // Launcher templates for the multigrid kernels; each precision's translation
 // unit includes this file and instantiates the launchers explicitly.
 #pragma once
+#include <atomic>
+
 #include "mmh_kernels.cuh"
 
 namespace mmh {
 
 static inline unsigned grid_of(i64 count, int block) { return (unsigned)((count + block - 1) / block); }
 static const int kBlock = 256;
+
+// Dynamic shared memory above the 48 KB default is an attribute of a kernel on
+// one device: it is set on each device the library launches the kernel on,
+// once per device (bit d of `done`).  A failure leaves the bit clear, and the
+// launch that needs the attribute then fails and is reported by the entry
+// point's launch-error check.
+template <class K>
+inline void smem_attr_once(K* kernel, int bytes, std::atomic<unsigned long long>& done) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+  const unsigned long long bit = 1ull << dev;
+  if (done.load(std::memory_order_acquire) & bit) return;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess)
+    done.fetch_or(bit, std::memory_order_acq_rel);
+}
 
 template <class T>
 void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_t s, bool fast_div) {
@@ -35,11 +52,8 @@ void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nswe
   if (n >= 64) {
     constexpr int TX = GsTile<T>::TX, TY = GsTile<T>::TY;
     const size_t smem = sizeof(T) * GsGeom<T, TX, TY>::WORDS;
-    // once per process (thread-safe static initialisation)
-    static const bool attr =
-        cudaFuncSetAttribute(k_gs_plane<T, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
-        cudaSuccess;
-    (void)attr;
+    static std::atomic<unsigned long long> attr_done{0};
+    smem_attr_once(k_gs_plane<T, TX, TY>, (int)smem, attr_done);
     dim3 grid(n / TX, n / TY, n / 2);
     // double buffer: a sweep reads a and leaves the swept field in b
     T* a = phi;

@@ -55,9 +55,13 @@ extern "C" int mmh_relax_noalloc_f64(const double* d_deformpot, const double* d_
   if (n < 4) return MMH_ERR_SIZE;
   if (n > kMaxN) return MMH_ERR_TOO_LARGE;
   int ir = iopt % 8;
-  if (iopt < 0 || (iopt / 8) % 8 != 2 || (ir != 0 && ir != 2) || nrelax < 0) return MMH_ERR_ARG;
+  // the same iresidopt bounds as mmh_relax_f64 (modes 1 and 3 need a resid
+  // array this entry point does not take)
+  if (iopt < 0 || iopt > 256 || (iopt / 8) % 8 != 2 || (ir != 0 && ir != 2) || nrelax < 0) return MMH_ERR_ARG;
   if (ir == 2 && !rinf) return MMH_ERR_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // an error left pending by earlier, unrelated work is not this call's
+  cudaGetLastError();
   double* scratch = nullptr;
   int rc = scratch_address(&scratch);
   if (rc != MMH_OK) return rc;
@@ -67,20 +71,21 @@ extern "C" int mmh_relax_noalloc_f64(const double* d_deformpot, const double* d_
   unsigned long long* maxw = reinterpret_cast<unsigned long long*>(scratch + 7 * kMaxN3);
   launch_metric<double>(d_deformpot, d_rho, n, dx, coef, s);
   launch_gs_sweeps<double>(d_arr, d_rhs, coef, n, dx, nrelax, buf, s);
+  if (cudaGetLastError() != cudaSuccess) return MMH_ERR_CUDA;
+  double v = 0.0;
   if (ir == 2) {
     // the word keeps the previous call's maximum: clear it first
     if (cudaMemsetAsync(maxw, 0, sizeof(unsigned long long), s) != cudaSuccess) return MMH_ERR_CUDA;
     launch_residual<double>(d_arr, d_rhs, coef, n, dx, nullptr, nullptr, maxw, s);
+    if (cudaGetLastError() != cudaSuccess) return MMH_ERR_CUDA;
     unsigned long long bits = 0;
     if (cudaMemcpyAsync(&bits, maxw, sizeof(bits), cudaMemcpyDeviceToHost, s) != cudaSuccess) return MMH_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return MMH_ERR_CUDA;
-    double v;
     static_assert(sizeof(v) == sizeof(bits), "word size");
     memcpy(&v, &bits, sizeof(v));
-    *rinf = v;
   } else {
-    if (rinf) *rinf = 0.0;
     if (cudaStreamSynchronize(s) != cudaSuccess) return MMH_ERR_CUDA;
   }
-  return cudaGetLastError() == cudaSuccess ? MMH_OK : MMH_ERR_CUDA;
+  if (rinf) *rinf = v;
+  return MMH_OK;
 }

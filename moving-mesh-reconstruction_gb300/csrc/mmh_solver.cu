@@ -130,6 +130,11 @@ struct mmh_ctx {
   bool graphs = true;
   std::vector<void*> allocs;
   int last_status = MMH_OK;
+  // limiter masks of the last calcdefp (expansion, pass-1 compression, final
+  // compression test; n^3 bytes each), kept once mmh_keep_masks armed them
+  uint8_t* masks = nullptr;
+  bool keep_masks = false;
+  uint8_t* mask(int q) { return keep_masks ? masks + q * n3 : nullptr; }
 
   double* defp() { return h64.u[0]; }
   double* tmp() { return h64.rhs[0]; }
@@ -1115,7 +1120,7 @@ int calcdefp_host(mmh_ctx* c, H* defp, H* tmp, H* tmp2, const H* def, const H* u
   RET(upload(c, def, c->def, c->n3));
   RET(upload_density(c, u, nfluid, c->n3, c->rho));
   mmh_diag dd{};
-  int st = calcdefp_dev(c, dtold, dtaumesh, nullptr, nullptr, nullptr, &dd);
+  int st = calcdefp_dev(c, dtold, dtaumesh, c->mask(0), c->mask(1), c->mask(2), &dd);
   if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
   RET(download(c, c->defp(), defp, c->n3));
   if (tmp) {
@@ -1217,7 +1222,8 @@ unsigned long long mmh_launch_count(void) { return mmh::launch_count(); }
 int mmh_profile_start(int kind) { return mmh::prof_start(kind) == 0 ? MMH_OK : MMH_ERR_CUDA; }
 int mmh_profile_stop(int* launches, double* ms, long long* cells) {
   int r = mmh::prof_stop(launches, ms, cells);
-  return r < 0 ? MMH_ERR_CUDA : MMH_OK;
+  // r == 1: launches went untimed (no event could be created for them)
+  return r < 0 ? MMH_ERR_CUDA : (r > 0 ? MMH_ERR_NOMEM : MMH_OK);
 }
 
 int mmh_destroy(mmh_ctx* c) {
@@ -1455,6 +1461,25 @@ int mmh_iterate_adjoint_f64(mmh_ctx* c, int niter, int checkpoint_every, const d
   if (gdef) RET(download(c, dw + 3 * n3, gdef, n3));
   return MMH_OK;
 }
+int mmh_keep_masks(mmh_ctx* c, int on) {
+  if (!c) return MMH_ERR_ARG;
+  if (on && !c->masks) {
+    RET(c->alloc(&c->masks, 3 * c->n3));
+    CK(cudaMemsetAsync(c->masks, 0, (size_t)(3 * c->n3), c->s));
+  }
+  c->keep_masks = on != 0;
+  return MMH_OK;
+}
+
+int mmh_masks(mmh_ctx* c, unsigned char* expand, unsigned char* compress1, unsigned char* compress2) {
+  if (!c || !c->keep_masks) return MMH_ERR_ARG;
+  unsigned char* out[3] = {expand, compress1, compress2};
+  for (int q = 0; q < 3; ++q)
+    if (out[q]) CK(cudaMemcpyAsync(out[q], c->masks + q * c->n3, (size_t)c->n3, cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  return MMH_OK;
+}
+
 int mmh_state_stats(mmh_ctx* c, mmh_stats* out) {
   if (!c || !out) return MMH_ERR_ARG;
   StatsDev* st = nullptr;
@@ -1587,7 +1612,8 @@ int mmh_metric_f64(mmh_ctx* c, const double* deformpot, const double* rho, doubl
   i64 n3 = (i64)n * n * n;
   RET(upload(c, deformpot, c->defl[l], n3));
   RET(upload(c, rho, c->rhol[l], n3));
-  launch_metric<double>(c->defl[l], c->rhol[l], n, dx, c->h64.coef[l], c->s);
+  // the context's form: the reference's six divisions (FP64) or one (mixed)
+  launch_metric<double>(c->defl[l], c->rhol[l], n, dx, c->h64.coef[l], c->s, c->cfg.precision == MMH_MIXED);
   return download(c, c->h64.coef[l], coef, 6 * n3);
 }
 
@@ -1643,7 +1669,11 @@ int mmh_nsmooth_f64(mmh_ctx* c, double* a, int n) {
   RET(check_cube(c, n, n, n));
   i64 n3 = (i64)n * n * n;
   RET(upload(c, a, c->scr, n3));
-  launch_smooth27<double>(c->scr, n, c->det, c->s);
+  // the context's form: the 27-point sum (FP64) or three axis passes (mixed)
+  if (c->cfg.precision == MMH_MIXED)
+    launch_smooth_sep(c->scr, n, c->det, c->s);
+  else
+    launch_smooth27<double>(c->scr, n, c->det, c->s);
   return download(c, c->det, a, n3);
 }
 
@@ -1721,7 +1751,7 @@ int mmh_iterate(mmh_ctx* c, int niter, mmh_diag* d) {
   int st = MMH_OK;
   for (int it = 0; it < niter; ++it) {
     mmh_diag dd{};
-    st = calcdefp_dev(c, 1.0, 1.0, nullptr, nullptr, nullptr, &dd);
+    st = calcdefp_dev(c, 1.0, 1.0, c->mask(0), c->mask(1), c->mask(2), &dd);
     if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
     launch_add(c->def, c->defp(), c->n3, c->s);
     RET(relaxing_dev(c, 1.0));

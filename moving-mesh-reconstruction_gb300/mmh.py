@@ -44,7 +44,7 @@ EXPORTS = (
     "mmh_relax_noalloc_f64", "mmh_batch_run", "mmh_calcdefp_adjoint_f64",
     "mmh_relaxing_adjoint_f64", "mmh_iterate_adjoint_f64", "mmh_state_stats",
     "mmh_power_spectrum_f64", "mmh_haloden", "mmh_coarsen",
-    "mmh_column_density", "mmh_gridfigure",
+    "mmh_column_density", "mmh_gridfigure", "mmh_keep_masks", "mmh_masks",
 )
 
 # kernel kinds for the timing hooks
@@ -424,6 +424,18 @@ class Context:
         m = np.zeros(nbins, dtype=np.int64)
         _chk(lib().mmh_power_spectrum_f64(self._h, _p(a), _p(b), int(nbins), _p(k), _p(p), _p(m)), "power_spectrum")
         return k, p, m
+
+    def keep_masks(self, on=True):
+        """Arm (or disarm) keeping the limiter masks of every calcdefp."""
+        _chk(lib().mmh_keep_masks(self._h, int(bool(on))), "keep_masks")
+
+    def masks(self):
+        """Limiter masks of the last calcdefp: dict of expand, compress1,
+        compress2 (uint8, Fortran order), as the oracle's calcdefp returns them."""
+        shape = (self.n,) * 3
+        m = [np.zeros(shape, dtype=np.uint8, order="F") for _ in range(3)]
+        _chk(lib().mmh_masks(self._h, _p(m[0]), _p(m[1]), _p(m[2])), "masks")
+        return {"expand": m[0], "compress1": m[1], "compress2": m[2]}
 
     def stats(self):
         """main.f90's iteration diagnostics of the resident state (mmh_state_stats)."""

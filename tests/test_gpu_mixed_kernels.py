@@ -1,0 +1,57 @@
+"""The mixed form's own FP64 kernels against the oracle, one by one.
+
+In an MMH_MIXED context the drop-in entry points run the kernels mmh_iterate
+runs in that form, which are not bit-matched to the reference:
+* the metric (cbajraw, mmh/gauss1.f90:1107-1210) takes rho_bar/det once and
+  six products instead of six divisions: each coefficient within 4 ulp;
+* nsmooth (mmh/limiter.f90:677-781) runs as three axis passes of
+  [1/4, 1/2, 1/4] instead of the 27-point sum: within 1e-15 of max |a|;
+* relaxing (mmh/relaxing.f90:21-1139) takes one reciprocal per division
+  site: the density within 1e-13 relative after one step.
+The float-float outer residual (k_residual_ff) is checked against an FP64
+recomputation in test_gpu_parity.py::test_multigrid_mixed_float_float_outer_loop.
+"""
+import numpy as np
+import pytest
+
+from conftest import smooth_field
+
+pytestmark = pytest.mark.gpu
+
+EPS = np.finfo(np.float64).eps
+
+
+@pytest.mark.parametrize("n", [16, 32, 64])
+def test_mixed_metric_one_division(mmh, oracle, fields, n):
+    defpot = smooth_field(n, 0.3, 11 + n)
+    rho = fields.lognormal_density(n, sigma=1.0, seed=12 + n)
+    with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL) as ctx:
+        for dx in (1.0, 2.0):
+            g = ctx.metric(defpot, rho, dx)
+            o = oracle.metric(defpot, rho, dx)
+            assert np.all(np.abs(g - o) <= 4 * EPS * np.abs(o)), np.abs(g - o).max()
+
+
+@pytest.mark.parametrize("n", [16, 32, 64])
+def test_mixed_nsmooth_axis_passes(mmh, oracle, n):
+    a = np.asfortranarray(np.random.default_rng(n).standard_normal((n, n, n)))
+    with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL) as ctx:
+        g = a.copy(order="F")
+        ctx.nsmooth(g)
+    o = oracle.nsmooth(a)
+    assert np.abs(g - o).max() <= 1e-15 * np.abs(a).max()
+
+
+@pytest.mark.parametrize("n", [16, 32, 64])
+def test_mixed_relaxing_one_reciprocal(mmh, oracle, fields, n):
+    defpot = smooth_field(n, 0.3, 8)
+    defp = smooth_field(n, 0.05, 9)
+    _, u = fields.initial_state(n, sigma=1.0, seed=10)
+    uo = oracle.relaxing(u, defpot, defp)
+    ug = u.copy(order="F")
+    with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL) as ctx:
+        ctx.relaxing(ug, defpot, defp)
+    err = np.abs(ug[0] - uo[0]).max() / np.abs(uo[0]).max()
+    print(f"mixed relaxing {n}^3: {err:.2e}")
+    assert err <= 1e-13
+    assert np.all(ug[1:] == 0)

@@ -158,7 +158,7 @@ def test_multigrid_mixed_converges(mmh, oracle, fields, n, sched):
     assert rel(ug, uo) <= 1e-9
 
 
-@pytest.mark.parametrize("n", [32, 64])
+@pytest.mark.parametrize("n", [32, 64, 128])
 def test_multigrid_mixed_float_float_outer_loop(mmh, oracle, fields, n):
     """Mixed form at a tolerance the float-float outer residual serves
     (>= 1e-10): the solve reaches it, the residual it reports agrees with an

@@ -63,3 +63,18 @@ def test_noalloc_rejects_grids_above_its_scratch(mmh):
     assert rc == -10
     lib.mmh_strerror.restype = C.c_char_p
     assert b"n <= 64" in lib.mmh_strerror(rc)
+
+
+@pytest.mark.parametrize("iopt", [274, 19, 17, -2])
+def test_noalloc_rejects_what_the_allocating_relax_rejects(mmh, iopt):
+    """iresidopt values mmh_relax_f64 refuses (above 256, or a residual mode
+    that needs the coarse resid array this entry point does not take) are
+    refused here too, before any work."""
+    torch = pytest.importorskip("torch")
+    lib = mmh.lib()
+    n = 16
+    buf = torch.zeros(n ** 3, dtype=torch.float64, device="cuda")
+    rinf = C.c_double(0.0)
+    p = C.c_void_p(buf.data_ptr())
+    rc = lib.mmh_relax_noalloc_f64(p, p, p, p, C.c_double(1.0), n, 1, iopt, C.byref(rinf), None)
+    assert rc == -1  # MMH_ERR_ARG
