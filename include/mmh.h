@@ -129,8 +129,10 @@ int mmh_defp2delta_f64(mmh_ctx* ctx, const double* indata, double* outdata, cons
 /* ---- reference subroutines on the path (FP64 host arrays) ------------- */
 /* Each computes in the context's precision form: in an MMH_MIXED context
  * mmh_metric_f64 takes one division per cell, mmh_nsmooth_f64 runs three axis
- * passes and mmh_relaxing_f64 one reciprocal per division site (the kernels
- * mmh_iterate runs in that form; not bit-matched to the reference). */
+ * passes, mmh_relaxing_f64 one reciprocal per division site and
+ * mmh_relax_f64 runs the FP32 Gauss-Seidel sweeps and FP32 residual of the
+ * V-cycle on FP32 copies of its arrays (the kernels mmh_iterate runs in that
+ * form; not bit-matched to the reference). */
 /* relax(arr,resid,rhs,deformpot,u,rinf,dx,n,n,n,1,nrelax,iopt)  gauss1.f90:64
  * iopt = 8*isolver + iresidopt with isolver = 2; resid((n/2)^3) is written
  * when iresidopt is 1 or 3. */

@@ -1590,6 +1590,31 @@ int mmh_relax_f64(mmh_ctx* c, double* arr, double* resid, const double* rhs, con
   RET(upload(c, rhs, c->h64.rhs[l], n3));
   RET(upload(c, deformpot, c->defl[l], n3));
   RET(upload(c, rho, c->rhol[l], n3));
+  if (c->cfg.precision == MMH_MIXED) {
+    // the mixed form's smoother: FP32 sweeps (and FP32 residual) on FP32
+    // copies of phi, rhs and the coefficients, as inside its V-cycles
+    Hier<float>& F = c->h32;
+    launch_metric<double>(c->defl[l], c->rhol[l], n, dx, c->h64.coef[l], c->s, true);
+    launch_d2f(c->h64.coef[l], F.coef[l], 6 * n3, c->s);
+    launch_d2f(c->h64.u[l], F.u[l], n3, c->s);
+    launch_d2f(c->h64.rhs[l], F.rhs[l], n3, c->s);
+    launch_gs_sweeps<float>(F.u[l], F.rhs[l], F.coef[l], n, (float)dx, nrelax, F.r[l], c->s);
+    CK(cudaMemsetAsync(c->sc->errbits, 0, 8, c->s));
+    if (ir != 0) {
+      launch_residual<float>(F.u[l], F.rhs[l], F.coef[l], n, (float)dx, ir == 3 ? F.r[l] : nullptr, nullptr,
+                             c->sc->errbits, c->s);
+      if (ir == 3) {
+        launch_restrict_resid<float>(F.r[l], n, special_plane(nrelax, n), F.rhs[l + 1], c->s);
+        launch_f2d(F.rhs[l + 1], c->scr, n3 / 8, c->s);
+      }
+    }
+    launch_f2d(F.u[l], c->h64.u[l], n3, c->s);
+    RET(pull_scal(c));
+    *rinf = ir >= 2 ? bits_to_double(c->hsc->errbits[0]) : 0.0;
+    RET(download(c, c->h64.u[l], arr, n3));
+    if (ir == 3) RET(download(c, c->scr, resid, n3 / 8));
+    return MMH_OK;
+  }
   launch_metric<double>(c->defl[l], c->rhol[l], n, dx, c->h64.coef[l], c->s);
   launch_gs_sweeps<double>(c->h64.u[l], c->h64.rhs[l], c->h64.coef[l], n, dx, nrelax, c->h64.r[l], c->s);
   CK(cudaMemsetAsync(c->sc->errbits, 0, 8, c->s));

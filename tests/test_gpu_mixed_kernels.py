@@ -55,3 +55,29 @@ def test_mixed_relaxing_one_reciprocal(mmh, oracle, fields, n):
     print(f"mixed relaxing {n}^3: {err:.2e}")
     assert err <= 1e-13
     assert np.all(ug[1:] == 0)
+
+
+@pytest.mark.parametrize("n,nrelax,iopt", [(64, 1, 18), (64, 3, 18), (128, 2, 18), (256, 2, 18), (32, 2, 18),
+                                           (128, 2, 19)])
+def test_mixed_relax_fp32_sweeps(mmh, oracle, fields, n, nrelax, iopt):
+    """The mixed form's FP32 Gauss-Seidel sweeps (one launch per whole sweep
+    from 64^3 up) against the oracle's FP64 relax in the reference's plane
+    order: every cell within 1e-5 of max |phi| (FP32 rounding), the residual
+    norm within 1e-4 relative."""
+    defpot = smooth_field(n, 0.05, 5 + n)
+    rho = fields.lognormal_density(n, sigma=0.5, seed=6 + n)
+    rng = np.random.default_rng(n + nrelax)
+    rhs = np.asfortranarray(rng.standard_normal((n, n, n)))
+    phi0 = np.asfortranarray(rng.standard_normal((n, n, n)))
+    coef = oracle.metric(defpot, rho, 1.0)
+    a = phi0.copy(order="F")
+    ro, rio = oracle.relax(a, rhs, coef, 1.0, nrelax, iopt, colour8=True)
+    b = phi0.copy(order="F")
+    with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL) as ctx:
+        rg, rig = ctx.relax(b, rhs, defpot, rho, 1.0, nrelax, iopt)
+    err = np.abs(b - a).max() / np.abs(a).max()
+    print(f"FP32 relax {n}^3 x{nrelax}: phi {err:.2e}, rinf {rio:.6e} vs {rig:.6e}")
+    assert err <= 1e-5
+    assert abs(rig - rio) <= 1e-4 * rio
+    if iopt % 8 == 3:
+        assert np.abs(rg - ro).max() <= 1e-4 * np.abs(ro).max()

@@ -9,10 +9,11 @@
   - C1 as configured: 64^3, sigma_lnrho 1.0, V(2,2) cycles to 1e-10,
     10 iterations, limiter on.
   - The reference's own schedule (one V-cycle of 4*NG/n sweeps per level per
-    iteration, mgtemplate.f90) at 128^3 over 20 iterations (sigma 0.75), and at
-    sigma 1.0 over 10 iterations, where the compression limiter fires in the
-    last iterations (the field is then going unstable, as the reference's own
-    algorithm does on it).
+    iteration, mgtemplate.f90): C2 at 256^3 over 20 iterations at the largest
+    stable field strength (sigma 0.5), 128^3 over 20 iterations (sigma 0.75),
+    and runs where the compression limiter fires in the last iterations
+    (128^3 sigma 1.0, 256^3 sigma 0.75; the field is then going unstable, as
+    the reference's own algorithm does on it).
 * Mixed form (the benchmark's): FP32 V-cycles inside the float-float outer
   loop, solves to 1e-8, against the FP64 oracle solved to 1e-11 after 10
   iterations; the bound on each field is stated below and the measured
@@ -30,7 +31,11 @@ TOL_SPECTRAL = 1e-10
 # Mixed form (solves to 1e-8, FP32 V-cycles, float-float outer residual)
 # against the FP64 oracle converged to 1e-11, after 10 iterations: max
 # |difference| / max |oracle| per field.
-MIXED_BOUND = {"def": 2e-7, "rho": 2e-6, "grad": 2e-7, "delta": 2e-6}
+# Measured on one GB300: at most 1.8e-12 (64^3 and 128^3, sigma 0.5 and 1.0).
+# The FP64 GPU form solved to the same 1e-8 differs from the oracle by up to
+# 2.4e-10: the mixed form's float-float outer loop ends well below its
+# tolerance.
+MIXED_BOUND = {"def": 1e-11, "rho": 1e-11, "grad": 1e-11, "delta": 1e-11}
 
 
 def _check_fp64(res):
@@ -61,20 +66,25 @@ def test_c1_vcycle_schedule_64cube(mmh, oracle, fields):
     print("C1 64^3 errors", err)
 
 
-@pytest.mark.parametrize("sigma,niter", [(0.75, 20), (1.0, 10)])
-def test_reference_schedule_128cube(mmh, oracle, fields, sigma, niter):
-    """The reference's schedule (mg128: one V-cycle, 4*NG/n sweeps per level)
-    over whole iterations at 128^3."""
-    n = 128
+@pytest.mark.parametrize("n,sigma,niter", [(128, 0.75, 20), (128, 1.0, 10), (256, 0.5, 20), (256, 0.75, 11)])
+def test_reference_schedule(mmh, oracle, fields, n, sigma, niter):
+    """The reference's schedule (mgN: one V-cycle, 4*NG/n sweeps per level)
+    over whole iterations.  256^3 at sigma_lnrho 0.5 over 20 iterations is C2
+    at the largest field strength the reference algorithm stays stable for on
+    that grid (0.6 turns the density negative after 8 iterations, C2's 1.5
+    after one; test_instability.py); 0.75 over 11 iterations runs into the
+    compression limiter (thousands of cells in the last one) as the field
+    goes unstable."""
     defpot, u = fields.initial_state(n, sigma=sigma, seed=1000)
     res = run_side_by_side(mmh, oracle, defpot, u, niter, gpu_kw=dict(precision=mmh.MMH_FP64),
                            oracle_kw=dict(sched=oracle.SCHED_REF))
     err = _check_fp64(res)
-    if sigma >= 1.0:
+    if sigma >= 0.75 and niter < 20:
         # the compression limiter and its FFT Poisson correction took part
         assert any_fft_correction(res)
         assert sum(r["mask_count"]["compress2"] for r in res["records"]) > 0
-    print(f"REF 128^3 sigma {sigma} errors", err)
+    print(f"REF {n}^3 sigma {sigma} x{niter}: errors {err}; masks {[r['mask_count'] for r in res['records']]}; "
+          f"oracle {res['t_oracle']:.1f} s, GPU {res['t_gpu']:.1f} s")
 
 
 @pytest.mark.parametrize("n,sigma", [(64, 0.5), (64, 1.0), (128, 0.5)])
