@@ -65,6 +65,10 @@ void launch_d2f(const double* a, float* b, i64 count, cudaStream_t s);
 void launch_f2d(const float* a, double* b, i64 count, cudaStream_t s);
 void launch_add_f2d(double* a, const float* b, i64 count, cudaStream_t s);
 void launch_add(double* a, const double* b, i64 count, cudaStream_t s);  // a = a + b
+// exact FP64 solve of the 4^3 level (mixed form): M (64 x 64) from the level's
+// FP64 coefficients once per metric; z = M (r - mean r) per application
+void launch_coarse_inverse(const double* coef, double dx, double* M, cudaStream_t s);
+void launch_coarse_apply(const float* r, const double* M, float* z, cudaStream_t s);
 
 // limiter / spectral / relaxing (FP64)
 struct LimDev;

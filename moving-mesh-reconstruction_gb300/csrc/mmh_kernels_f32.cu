@@ -1,5 +1,7 @@
 // FP32 kernels of the mixed-precision inner V-cycle (smoother, residual,
 // restriction, prolongation, zero-mean).  FMA contraction stays enabled here.
+#include <cmath>
+
 #include "mmh_gs_fused.cuh"
 #include "mmh_launch.cuh"
 #include "mmh_pcg.cuh"
@@ -8,17 +10,27 @@ namespace mmh {
 MMH_INSTANTIATE(float)
 MMH_INSTANTIATE_PCG(float)
 
-// Planes per CTA of the fused sweep: long segments (each recomputes one extra
-// even plane and stages three extra planes) while the grid still fills the
-// GPU several times over.
+// Planes per CTA of the fused sweep.  A segment of S planes stages S + 3
+// planes and recomputes one even plane; the grid runs in waves of two CTAs
+// per SM.  S maximises (S / (S + 3)) x (filled fraction of the last wave).
 static int gs_fused_segment(int n) {
   const int tiles = (n / gsf::TX) * (n / gsf::TY);
-  int S = n;
-  while (S > 8 && (long long)tiles * (n / S) < 3 * 152) S /= 2;
-  return S;
+  int best = 8;
+  double best_eff = -1.0;
+  for (int S = n; S >= 8; S /= 2) {
+    const double waves = (double)tiles * (n / S) / (2.0 * 152.0);
+    const double eff = (waves / std::ceil(waves)) * (S / (S + 3.0));
+    if (eff > best_eff) {
+      best_eff = eff;
+      best = S;
+    }
+  }
+  return best;
 }
 
-bool gs_fused_applies(int n) { return n >= 64 && n % gsf::TX == 0 && n % gsf::TY == 0; }
+// The fused sweep from 256^3 up; smaller levels (a few CTAs of tile columns
+// would leave most of the GPU idle) keep the plane kernels.
+bool gs_fused_applies(int n) { return n >= 256 && n % gsf::TX == 0 && n % gsf::TY == 0; }
 
 // nsweeps whole sweeps, one launch each, alternating between phi and scratch;
 // the result ends in phi.

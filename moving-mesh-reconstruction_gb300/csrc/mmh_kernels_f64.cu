@@ -151,6 +151,94 @@ void launch_f2d(const float* a, double* b, i64 count, cudaStream_t s) {
   k_f2d<<<grid_of(count, kBlock), kBlock, 0, s>>>(a, b, count);
   count_launch();
 }
+// ---------------------------------------------------------------------------
+// Exact solve of the coarsest level (4^3 = 64 cells) in the mixed form's
+// preconditioner, in FP64.  The level's operator L (the 19-point stencil of
+// relaxplane, gauss1.f90:950-980, on the restricted metric) is singular with
+// the constants as its null space and symmetric negative semi-definite, so
+// A = L - beta 1 1^T (beta = mean |L_ii| / 64) is negative definite and
+// z = A^-1 (r - mean r) is the zero-mean solution of L z = r - mean r: what
+// the reference's 32 + 32 Gauss-Seidel sweeps and zerosum of mg4
+// (multigrid.f90:94-121) converge to.  M = A^-1 is formed once per metric.
+// ---------------------------------------------------------------------------
+constexpr int kCoarseN = 64;
+// L column by column (the operator applied to unit vectors, so it is exactly
+// the smoother's operator), then an in-place Gauss-Jordan inversion (no
+// pivoting: -A is symmetric positive definite).  One CTA of 256 threads.
+__global__ void __launch_bounds__(256) k_coarse_inverse(const double* __restrict__ coef, double di2,
+                                                        double* __restrict__ M) {
+  constexpr int N = kCoarseN;
+  __shared__ double A[N][N];
+  __shared__ double e[N];
+  __shared__ double colp[N];
+  __shared__ double piv_s;
+  const int tid = threadIdx.x;
+  for (int j = 0; j < N; ++j) {
+    if (tid < N) e[tid] = tid == j ? 1.0 : 0.0;
+    __syncthreads();
+    if (tid < N) {
+      int i, jj, k;
+      cell_of(tid, 4, i, jj, k);
+      double tdiag, t1, t2;
+      op_terms(e, coef, 4, (i64)N, i, jj, k, tdiag, t1, t2);
+      A[tid][j] = (t1 + t2 + tdiag * e[tid]) * di2;
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    double d = 0.0;
+    for (int i = 0; i < N; ++i) d += fabs(A[i][i]);
+    piv_s = d / N / N;  // beta
+  }
+  __syncthreads();
+  const double beta = piv_s;
+  for (int q = tid; q < N * N; q += blockDim.x) A[q / N][q % N] -= beta;
+  __syncthreads();
+  for (int p = 0; p < N; ++p) {
+    if (tid < N) colp[tid] = A[tid][p];
+    if (tid == 0) piv_s = 1.0 / A[p][p];
+    __syncthreads();
+    const double ip = piv_s;
+    if (tid < N) A[p][tid] = (tid == p ? 1.0 : A[p][tid]) * ip;
+    __syncthreads();
+    for (int q = tid; q < N * N; q += blockDim.x) {
+      const int i = q / N, j = q % N;
+      if (i != p) A[i][j] = (j == p ? 0.0 : A[i][j]) - colp[i] * A[p][j];
+    }
+    __syncthreads();
+  }
+  for (int q = tid; q < N * N; q += blockDim.x) M[q] = A[q / N][q % N];
+}
+
+// z = M (r - mean r) on the 64 cells: one CTA of 64 threads, FP64 sums.
+__global__ void __launch_bounds__(64) k_coarse_apply(const float* __restrict__ r, const double* __restrict__ M,
+                                                     float* __restrict__ z) {
+  constexpr int N = kCoarseN;
+  __shared__ double b[N];
+  __shared__ double wsum[2];
+  const int tid = threadIdx.x;
+  double v = (double)r[tid];
+  double sv = v;
+  for (int d = 16; d > 0; d >>= 1) sv += __shfl_down_sync(0xffffffffu, sv, d);
+  if ((tid & 31) == 0) wsum[tid >> 5] = sv;
+  __syncthreads();
+  b[tid] = v - (wsum[0] + wsum[1]) / N;
+  __syncthreads();
+  double acc = 0.0;
+#pragma unroll 8
+  for (int j = 0; j < N; ++j) acc += M[tid * N + j] * b[j];
+  z[tid] = (float)acc;
+}
+
+void launch_coarse_inverse(const double* coef, double dx, double* M, cudaStream_t s) {
+  k_coarse_inverse<<<1, 256, 0, s>>>(coef, 1.0 / (dx * dx), M);
+  count_launch();
+}
+void launch_coarse_apply(const float* r, const double* M, float* z, cudaStream_t s) {
+  k_coarse_apply<<<1, kCoarseN, 0, s>>>(r, M, z);
+  count_launch();
+}
+
 void launch_add_f2d(double* a, const float* b, i64 count, cudaStream_t s) {
   k_add_f2d<<<grid_of(count, kBlock), kBlock, 0, s>>>(a, b, count);
   count_launch();

@@ -134,6 +134,9 @@ struct mmh_ctx {
   // compression test; n^3 bytes each), kept once mmh_keep_masks armed them
   uint8_t* masks = nullptr;
   bool keep_masks = false;
+  // mixed form: inverse of the coarsest (4^3) level's operator, formed with
+  // each metric (64 x 64 FP64)
+  double* coarse_inv = nullptr;
   uint8_t* mask(int q) { return keep_masks ? masks + q * n3 : nullptr; }
 
   double* defp() { return h64.u[0]; }
@@ -240,8 +243,13 @@ int vcycle(mmh_ctx* c, int l) {
   const int post = (guard || c->cfg.schedule != MMH_SCHED_TOL) ? 2 : 0;
   if (n == 4) {
     if constexpr (std::is_same<T, float>::value) {
-      // coarsest grid solved in FP64
       Hier<float>& F = c->h32;
+      if (c->coarse_inv && !guard) {
+        // exact FP64 solve with the level's inverse (zero-mean result)
+        launch_coarse_apply(F.rhs[l], c->coarse_inv, F.u[l], c->s);
+        return MMH_OK;
+      }
+      // coarsest grid solved in FP64 by the reference's sweeps
       i64 n3 = 64;
       launch_f2d(F.rhs[l], c->h64.rhs[l], n3, c->s);
       launch_f2d(F.u[l], c->h64.u[l], n3, c->s);
@@ -292,6 +300,8 @@ int build_levels(mmh_ctx* c, int l0) {
                           c->cfg.precision == MMH_MIXED);
     if (c->cfg.precision == MMH_MIXED) launch_d2f(c->h64.coef[l], c->h32.coef[l], 6 * (i64)n * n * n, c->s);
   }
+  if (c->coarse_inv && c->nl[c->nlev - 1] == 4)
+    launch_coarse_inverse(c->h64.coef[c->nlev - 1], double(1 << (c->nlev - 1)), c->coarse_inv, c->s);
   return MMH_OK;
 }
 
@@ -1333,6 +1343,7 @@ int mmh_create(mmh_ctx** out, const mmh_config* cfg) {
       }
     }
   }
+  if (cfg->precision == MMH_MIXED && c->nl[c->nlev - 1] == 4) A(&c->coarse_inv, 64 * 64);
   if (cfg->schedule == MMH_SCHED_TOL) {
     S(&c->px, n3);
     S(&c->pb, n3);

@@ -1,18 +1,25 @@
-"""The adjoint at full size (opt-in: MMH_TEST_C5=1; MMH_C5_DIRS directions,
-default 64): a 256^3 lognormal density, 20 deformation iterations with the
-forward states kept every 4, the loss sum_b w_b P_b of the reconstructed
-density's power in 16 log-spaced |k| bands (seeded weights), its gradient
-with respect to the input density from mmh_iterate_adjoint_f64 against central
-finite differences of the loss in smooth random directions.
+"""C5: the gradient of a band-power loss of the reconstructed density with
+respect to the input density, from mmh_iterate_adjoint_f64, against central
+finite differences of the loss in smooth random directions.  The loss is
+sum_b w_b P_b of the reconstructed density's power in 16 log-spaced |k| bands
+(seeded weights), after 20 deformation iterations with the forward states
+kept every 4.
 
-FP64 solves to 1e-11: the finite differences need a forward map that is
-smooth at the step (1e-7 of the direction's maximum), which the FP32 inner
-solves of the mixed form are not.  The map is piecewise smooth (minmod,
-cflkeuler and clip branches); at 256^3 some branch edges lie within the step,
-and the differences then move by a few 1e-7 of the gradient's scale whatever
-the solver tolerance (1e-10 .. 1e-12 give the same differences).  Each
-direction's difference is bounded by 1e-6 of the summed per-cell
-contributions sum |g v|; the plain relative difference is printed beside it.
+* 64^3 (default, 16 directions): every direction's plain relative
+  difference |fd - adjoint| / |adjoint| within the benchmark spec's 1e-6.
+* 256^3 (opt-in: MMH_TEST_C5=1; MMH_C5_DIRS directions, default 64): at this
+  size some branch edges of the piecewise smooth forward map (minmod,
+  cflkeuler and clip branches) lie within the finite-difference step, and the
+  differences then move by a few 1e-7 of the gradient's scale whatever the
+  solver tolerance (1e-10 .. 1e-12 give the same differences).  Each
+  direction's difference is bounded by 1e-6 of the summed per-cell
+  contributions sum |g v|; the plain relative difference is printed beside
+  it, and the benchmark spec's 1e-6 on it is not met by every direction there
+  (worst measured 6.6e-6, a direction whose derivative cancels across cells).
+
+FP64 solves: the finite differences need a forward map that is smooth at the
+step (1e-7 of the direction's maximum), which the FP32 inner solves of the
+mixed form are not.
 """
 import os
 import time
@@ -21,8 +28,6 @@ import numpy as np
 import pytest
 
 from conftest import smooth_field
-
-pytestmark = pytest.mark.skipif(os.environ.get("MMH_TEST_C5") != "1", reason="256^3 adjoint: set MMH_TEST_C5=1")
 
 
 def band_weights(n, seed):
@@ -46,9 +51,12 @@ def band_loss(delta, W):
 
 
 @pytest.mark.gpu
-def test_c5_adjoint_256(mmh, fields):
-    n, niter, every = 256, 20, 4
-    ndirs = int(os.environ.get("MMH_C5_DIRS", "64"))
+@pytest.mark.parametrize("n", [64, pytest.param(256, marks=pytest.mark.skipif(
+    os.environ.get("MMH_TEST_C5") != "1", reason="256^3 adjoint: set MMH_TEST_C5=1"))])
+def test_c5_adjoint(mmh, fields, n):
+    niter, every = 20, 4
+    ndirs = 16 if n == 64 else int(os.environ.get("MMH_C5_DIRS", "64"))
+    tol = 1e-12 if n == 64 else 1e-11
     rho0 = fields.lognormal_density(n, sigma=0.5, seed=5)
     W = band_weights(n, 55)
     z = np.zeros((n, n, n), order="F")
@@ -58,7 +66,7 @@ def test_c5_adjoint_256(mmh, fields):
         u[0] = r
         return u
 
-    with mmh.Context(n, precision=mmh.MMH_FP64, schedule=mmh.MMH_SCHED_TOL, tol=1e-11, max_cycles=400) as ctx:
+    with mmh.Context(n, precision=mmh.MMH_FP64, schedule=mmh.MMH_SCHED_TOL, tol=tol, max_cycles=400) as ctx:
 
         def forward(r):
             ctx.load(z, u_of(r))
@@ -75,7 +83,7 @@ def test_c5_adjoint_256(mmh, fields):
         t0 = time.perf_counter()
         grho, _, _ = ctx.iterate_adjoint(niter, wdelta=seed, checkpoint_every=every)
         t_adj = time.perf_counter() - t0
-        print(f"C5 256^3: loss {loss:.10e}; forward {t_fwd:.2f} s, forward+adjoint {t_adj:.2f} s")
+        print(f"C5 {n}^3: loss {loss:.10e}; forward {t_fwd:.2f} s, forward+adjoint {t_adj:.2f} s")
 
         rels, scaled = [], []
         for q in range(ndirs):
@@ -90,3 +98,5 @@ def test_c5_adjoint_256(mmh, fields):
         print(f"C5 over {ndirs} directions: relative difference median {np.median(rels):.2e} max {max(rels):.2e}; "
               f"of sum |g v| max {max(scaled):.2e}")
         assert max(scaled) <= 1e-6
+        if n == 64:
+            assert max(rels) <= 1e-6
