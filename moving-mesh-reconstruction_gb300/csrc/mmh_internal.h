@@ -33,10 +33,6 @@ void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_
 void launch_residual_fma(const double* phi, const double* rhs, const double* coef, int n, double dx, float* r32,
                          unsigned long long* maxbits, cudaStream_t s);
 template <class T> void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, T* scratch, cudaStream_t s);
-// FP32 sweeps of 64^3 and up: one launch per whole 8-colour sweep (mmh_gs_fused.cuh)
-bool gs_fused_applies(int n);
-void launch_gs_fused(float* phi, const float* rhs, const float* coef, int n, float dx, int nsweeps, float* scratch,
-                     cudaStream_t s);
 template <class T>
 void launch_residual(const T* phi, const T* rhs, const T* coef, int n, T dx, T* r, float* r32,
                      unsigned long long* maxbits, cudaStream_t s);

@@ -1,61 +1,11 @@
 // FP32 kernels of the mixed-precision inner V-cycle (smoother, residual,
 // restriction, prolongation, zero-mean).  FMA contraction stays enabled here.
-#include <cmath>
-
-#include "mmh_gs_fused.cuh"
 #include "mmh_launch.cuh"
 #include "mmh_pcg.cuh"
 
 namespace mmh {
 MMH_INSTANTIATE(float)
 MMH_INSTANTIATE_PCG(float)
-
-// Planes per CTA of the fused sweep.  A segment of S planes stages S + 3
-// planes and recomputes one even plane; the grid runs in waves of two CTAs
-// per SM.  S maximises (S / (S + 3)) x (filled fraction of the last wave).
-static int gs_fused_segment(int n) {
-  const int tiles = (n / gsf::TX) * (n / gsf::TY);
-  int best = 8;
-  double best_eff = -1.0;
-  for (int S = n; S >= 8; S /= 2) {
-    const double waves = (double)tiles * (n / S) / (2.0 * 152.0);
-    const double eff = (waves / std::ceil(waves)) * (S / (S + 3.0));
-    if (eff > best_eff) {
-      best_eff = eff;
-      best = S;
-    }
-  }
-  return best;
-}
-
-// The fused sweep from 256^3 up; smaller levels (a few CTAs of tile columns
-// would leave most of the GPU idle) keep the plane kernels.
-bool gs_fused_applies(int n) { return n >= 256 && n % gsf::TX == 0 && n % gsf::TY == 0; }
-
-// nsweeps whole sweeps, one launch each, alternating between phi and scratch;
-// the result ends in phi.
-void launch_gs_fused(float* phi, const float* rhs, const float* coef, int n, float dx, int nsweeps, float* scratch,
-                     cudaStream_t s) {
-  static std::atomic<unsigned long long> attr_done{0};
-  const int smem = (int)sizeof(float) * gsf::SMEM_WORDS;
-  smem_attr_once(k_gs_sweep, smem, attr_done);
-  const int S = gs_fused_segment(n);
-  const dim3 grid(n / gsf::TX, n / gsf::TY, n / S);
-  const float dx2 = dx * dx;
-  const i64 n3 = (i64)n * n * n;
-  float* a = phi;
-  float* b = scratch;
-  for (int sw = 0; sw < nsweeps; ++sw) {
-    prof_begin(kk<float>(KK_GS), s, n3, n);
-    k_gs_sweep<<<grid, gsf::NT, smem, s>>>(a, b, rhs, coef, n, dx2, S);
-    prof_end(kk<float>(KK_GS), s, n);
-    count_launch();
-    float* t = a;
-    a = b;
-    b = t;
-  }
-  if (a != phi) cudaMemcpyAsync(phi, a, sizeof(float) * (size_t)n3, cudaMemcpyDeviceToDevice, s);
-}
 
 // Dot product of two FP32 vectors for the mixed form's inner solve, whose
 // results are not bit-matched to the oracle: a fixed grid of kDotBlocks

@@ -2,7 +2,6 @@
 // unit includes this file and instantiates the launchers explicitly.
 #pragma once
 #include <atomic>
-#include <type_traits>
 
 #include "mmh_kernels.cuh"
 
@@ -43,20 +42,13 @@ template <class T> struct GsTile;
 template <> struct GsTile<float> { static const int TX = 32, TY = 16; };
 template <> struct GsTile<double> { static const int TX = 32, TY = 8; };
 
-// nsweeps 8-colour Gauss-Seidel sweeps.  FP32 grids of 64^3 and up run one
-// launch per whole sweep (launch_gs_fused); FP64 grids of 64^3 and up one
+// nsweeps 8-colour Gauss-Seidel sweeps.  Grids of 64^3 and up run one fused
 // launch per half sweep (all in-plane colours of every plane of one parity);
 // smaller grids run one launch per colour.
 template <class T>
 void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, T* scratch, cudaStream_t s) {
   i64 h3 = (i64)(n / 2) * (n / 2) * (n / 2);
   T dx2 = dx * dx;
-  if constexpr (std::is_same<T, float>::value) {
-    if (gs_fused_applies(n)) {
-      launch_gs_fused(phi, rhs, coef, n, dx, nsweeps, scratch, s);
-      return;
-    }
-  }
   if (n >= 64) {
     constexpr int TX = GsTile<T>::TX, TY = GsTile<T>::TY;
     const size_t smem = sizeof(T) * GsGeom<T, TX, TY>::WORDS;
