@@ -83,6 +83,10 @@ void launch_relax_flux(const double* u1, const double* defp, const double* baj, 
                        cudaStream_t s, bool fast_div = false);
 void launch_relax_dpv(const double* sd, const double* cc, int n, const double* ubase, double dt, double* out,
                       double* gface, cudaStream_t s);
+// the mixed form's relaxing of the density (mmh_relax32.cu): FP32 fluxes, FP64
+// update; geo (n^3 float4), uf0, uf1 (n^3 floats) are scratch
+void launch_relax32(double* rho, const double* def, const double* defp, int n, double dt, float4* geo, float* uf0,
+                    float* uf1, cudaStream_t s);
 // u(nf,n^3) (float or double) <-> density; flag |= 1 when a component 2..nf is not zero
 void launch_extract_density_f(const float* u, int nf, i64 n3, double* rho, int* flag, cudaStream_t s);
 void launch_extract_density_d(const double* u, int nf, i64 n3, double* rho, int* flag, cudaStream_t s);

@@ -268,6 +268,12 @@ __device__ __forceinline__ void op_eval(const Stencil<T>& s, T& tdiag, T& t1, T&
         - (s.imkp - s.imkm) * s.f3im) * T(0.25);
 }
 
+// The Gauss-Seidel update's division: IEEE in FP64 (the oracle's bits); the
+// fast reciprocal-based division in FP32 (the mixed form's smoother, which is
+// not bit-matched; within 2 ulp).
+__device__ __forceinline__ double gs_div(double a, double b) { return a / b; }
+__device__ __forceinline__ float gs_div(float a, float b) { return __fdividef(a, b); }
+
 // Gather the stencil of cell (i,j,k) from global memory.
 template <class T>
 __device__ __forceinline__ void op_terms(const T* __restrict__ phi, const T* __restrict__ coef, int n, i64 n3, int i,
@@ -317,7 +323,7 @@ __global__ void k_gs_colour(T* __restrict__ phi, const T* __restrict__ rhs, cons
   T tdiag, t1, t2;
   op_terms(phi, coef, n, n3, i, j, k, tdiag, t1, t2);
   i64 c = IDX(i, j, k, n);
-  phi[c] = (rhs[c] * dx2 - t1 - t2) / tdiag;
+  phi[c] = gs_div(rhs[c] * dx2 - t1 - t2, tdiag);
 }
 
 // nsweeps full 8-colour sweeps of a small grid (n <= 16) by one CTA: the
@@ -337,7 +343,7 @@ __global__ void __launch_bounds__(512) k_gs_small(T* __restrict__ phi, const T* 
         T tdiag, t1, t2;
         op_terms(phi, coef, n, n3, i, j, k, tdiag, t1, t2);
         i64 c = IDX(i, j, k, n);
-        phi[c] = (rhs[c] * dx2 - t1 - t2) / tdiag;
+        phi[c] = gs_div(rhs[c] * dx2 - t1 - t2, tdiag);
       }
       __syncthreads();
     }
@@ -372,7 +378,7 @@ __global__ void __launch_bounds__(512) k_gs_small_sm(T* __restrict__ phi, const 
         T tdiag, t1, t2;
         op_terms(sp, sc, n, (i64)n3, i, j, k, tdiag, t1, t2);
         i64 c = IDX(i, j, k, n);
-        sp[c] = (sr[c] * dx2 - t1 - t2) / tdiag;
+        sp[c] = gs_div(sr[c] * dx2 - t1 - t2, tdiag);
       }
       __syncthreads();
     }
@@ -549,7 +555,7 @@ __global__ void __launch_bounds__(256, 4) k_gs_plane(const T* __restrict__ src, 
       st.f3ip = F3[cxp]; st.f3im = F3[cxm];
       T tdiag, t1, t2;
       op_eval(st, tdiag, t1, t2);
-      sP[c] = (r * dx2 - t1 - t2) / tdiag;
+      sP[c] = gs_div(r * dx2 - t1 - t2, tdiag);
     }
     __syncthreads();
   }

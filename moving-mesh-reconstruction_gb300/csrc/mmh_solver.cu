@@ -733,10 +733,15 @@ int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t
 int relaxing_dev(mmh_ctx* c, double dt) {
   Stage stage_("mmh relaxing");
   int n = c->n;
-  const bool fast = c->cfg.precision == MMH_MIXED;  // one reciprocal per division site
-  launch_relax_stage1(c->rho, c->def, c->defp(), n, c->baj, c->cc, c->vt, c->s, fast);
+  if (c->cfg.precision == MMH_MIXED) {
+    // FP32 fluxes, FP64 update (the relaxing buffers hold the FP32 scratch)
+    launch_relax32(c->rho, c->def, c->defp(), n, dt, reinterpret_cast<float4*>(c->baj), reinterpret_cast<float*>(c->cc),
+                   reinterpret_cast<float*>(c->u1), c->s);
+    return MMH_OK;
+  }
+  launch_relax_stage1(c->rho, c->def, c->defp(), n, c->baj, c->cc, c->vt, c->s);
   launch_relax_dpv(c->vt, c->cc, n, c->rho, dt / 2.0, c->u1, c->gface, c->s);
-  launch_relax_flux(c->u1, c->defp(), c->baj, c->cc, n, c->vt, c->s, fast);
+  launch_relax_flux(c->u1, c->defp(), c->baj, c->cc, n, c->vt, c->s);
   launch_relax_dpv(c->vt, c->cc, n, c->rho, dt, c->rho, c->gface, c->s);
   return MMH_OK;
 }

@@ -6,8 +6,10 @@ runs in that form, which are not bit-matched to the reference:
   six products instead of six divisions: each coefficient within 4 ulp;
 * nsmooth (mmh/limiter.f90:677-781) runs as three axis passes of
   [1/4, 1/2, 1/4] instead of the 27-point sum: within 1e-15 of max |a|;
-* relaxing (mmh/relaxing.f90:21-1139) takes one reciprocal per division
-  site: the density within 1e-13 relative after one step.
+* relaxing (mmh/relaxing.f90:21-1139) forms its fluxes in FP32 and the
+  update in FP64: the density within 5e-8 relative after one step (an FP32
+  restatement in numpy gives 6e-9 at 32^3 for a step that moves the density
+  by 0.2).
 The float-float outer residual (k_residual_ff) is checked against an FP64
 recomputation in test_gpu_parity.py::test_multigrid_mixed_float_float_outer_loop.
 """
@@ -43,7 +45,7 @@ def test_mixed_nsmooth_axis_passes(mmh, oracle, n):
 
 
 @pytest.mark.parametrize("n", [16, 32, 64])
-def test_mixed_relaxing_one_reciprocal(mmh, oracle, fields, n):
+def test_mixed_relaxing_fp32_fluxes(mmh, oracle, fields, n):
     defpot = smooth_field(n, 0.3, 8)
     defp = smooth_field(n, 0.05, 9)
     _, u = fields.initial_state(n, sigma=1.0, seed=10)
@@ -53,7 +55,7 @@ def test_mixed_relaxing_one_reciprocal(mmh, oracle, fields, n):
         ctx.relaxing(ug, defpot, defp)
     err = np.abs(ug[0] - uo[0]).max() / np.abs(uo[0]).max()
     print(f"mixed relaxing {n}^3: {err:.2e}")
-    assert err <= 1e-13
+    assert err <= 5e-8
     assert np.all(ug[1:] == 0)
 
 
