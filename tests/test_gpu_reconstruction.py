@@ -15,9 +15,9 @@
     (128^3 sigma 1.0, 256^3 sigma 0.75; the field is then going unstable, as
     the reference's own algorithm does on it).
 * Mixed form (the benchmark's): FP32 V-cycles inside the float-float outer
-  loop, solves to 1e-8, against the FP64 oracle solved to 1e-11 after 10
-  iterations; the bound on each field is stated below and the measured
-  errors are printed.
+  loop, solves to 1e-8, relaxing with FP32 fluxes, against the FP64 oracle
+  solved to 1e-11 after 10 iterations; the bound on each field is stated
+  below and the measured errors are printed.
 """
 import numpy as np
 import pytest
@@ -28,14 +28,16 @@ pytestmark = pytest.mark.gpu
 
 TOL_SPECTRAL = 1e-10
 
-# Mixed form (solves to 1e-8, FP32 V-cycles, float-float outer residual)
-# against the FP64 oracle converged to 1e-11, after 10 iterations: max
-# |difference| / max |oracle| per field.
-# Measured on one GB300: at most 1.8e-12 (64^3 and 128^3, sigma 0.5 and 1.0).
+# Mixed form (solves to 1e-8, FP32 V-cycles, float-float outer residual,
+# relaxing with FP32 fluxes and an FP64 update) against the FP64 oracle
+# converged to 1e-11, after 10 iterations: max |difference| / max |oracle|
+# per field.  Measured on one GB300 (64^3 and 128^3, sigma 0.5 and 1.0): def
+# 9.2e-10, density 5.0e-8, displacement 3.1e-9, reconstructed density 8.5e-9.
+# The density carries the FP32 rounding of relaxing's fluxes (about 6e-9 of
+# it per step); def, which integrates the solves, stays near the tolerance.
 # The FP64 GPU form solved to the same 1e-8 differs from the oracle by up to
-# 2.4e-10: the mixed form's float-float outer loop ends well below its
-# tolerance.
-MIXED_BOUND = {"def": 1e-11, "rho": 1e-11, "grad": 1e-11, "delta": 1e-11}
+# 2.4e-10.
+MIXED_BOUND = {"def": 5e-9, "rho": 2e-7, "grad": 2e-8, "delta": 5e-8}
 
 
 def _check_fp64(res):
