@@ -652,6 +652,88 @@ __device__ __forceinline__ FF ff_of(double x) {
   return {h, (float)(x - (double)h)};
 }
 
+__device__ __forceinline__ FF ff_div(FF a, FF b) {
+  const float q1 = a.hi / b.hi;
+  const FF r = ff_sub(a, ff_mul({q1, 0.0f}, b));
+  return ff_quick(q1, r.hi / b.hi);
+}
+
+// The mixed form's finest-level metric (cbajraw, gauss1.f90:1107-1210) in
+// float-float, for the outer residual: rho_bar * cof(A) / det as (hi, lo)
+// pairs in `coef` (six planes of n^3 pairs, the layout k_ff_split makes) and
+// the hi parts, the FP32 V-cycle's coefficients, in coef32.  The Hessian of
+// def and the 27-cell density sum are formed in FP64 as in k_metric (their
+// operands are far larger than the results); A, its cofactors and
+// determinant, rho_bar / det and the six products in float-float (about 48
+// significant bits, all on the FP32 pipes).  det <= 1e-5 takes the
+// reference's fallback (unit cofactors, det = 1).
+__global__ void __launch_bounds__(256) k_metric_ff(const double* __restrict__ def, const double* __restrict__ rho,
+                                                   int n, double di2, float2* __restrict__ coef,
+                                                   float* __restrict__ coef32) {
+  const i64 n3 = (i64)n * n * n;
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  int i, j, k;
+  cell_of(t, n, i, j, k);
+  const int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
+  const double c = def[t];
+  const double pxx = (def[IDX(ip, j, k, n)] - 2.0 * c + def[IDX(im, j, k, n)]) * di2;
+  const double pyy = (def[IDX(i, jp, k, n)] - 2.0 * c + def[IDX(i, jm, k, n)]) * di2;
+  const double pzz = (def[IDX(i, j, kp, n)] - 2.0 * c + def[IDX(i, j, km, n)]) * di2;
+  const double pxy =
+      (def[IDX(ip, jp, k, n)] - def[IDX(im, jp, k, n)] - def[IDX(ip, jm, k, n)] + def[IDX(im, jm, k, n)]) * di2 * 0.25;
+  const double pyz =
+      (def[IDX(i, jp, kp, n)] - def[IDX(i, jp, km, n)] - def[IDX(i, jm, kp, n)] + def[IDX(i, jm, km, n)]) * di2 * 0.25;
+  const double pxz =
+      (def[IDX(ip, j, kp, n)] - def[IDX(im, j, kp, n)] - def[IDX(ip, j, km, n)] + def[IDX(im, j, km, n)]) * di2 * 0.25;
+  const FF one = {1.0f, 0.0f};
+  const FF a11 = ff_add(one, ff_of(pxx)), a22 = ff_add(one, ff_of(pyy)), a33 = ff_add(one, ff_of(pzz));
+  const FF a12 = ff_of(pxy), a13 = ff_of(pxz), a23 = ff_of(pyz);
+  FF b[6];
+  b[0] = ff_sub(ff_mul(a22, a33), ff_mul(a23, a23));
+  b[1] = ff_sub(ff_mul(a13, a23), ff_mul(a12, a33));
+  b[2] = ff_sub(ff_mul(a12, a23), ff_mul(a13, a22));
+  b[3] = ff_sub(ff_mul(a11, a33), ff_mul(a13, a13));
+  b[4] = ff_sub(ff_mul(a12, a13), ff_mul(a11, a23));
+  b[5] = ff_sub(ff_mul(a11, a22), ff_mul(a12, a12));
+  FF det = ff_add(ff_add(ff_mul(a11, b[0]), ff_mul(a12, b[1])), ff_mul(a13, b[2]));
+  if (det.hi + det.lo <= 1.e-5f) {
+    b[0] = one; b[1] = {0.0f, 0.0f}; b[2] = {0.0f, 0.0f}; b[3] = one; b[4] = {0.0f, 0.0f}; b[5] = one;
+    det = one;
+  }
+  const int is[3] = {im, i, ip}, js[3] = {jm, j, jp}, ks[3] = {km, k, kp};
+  double urg = rho[IDX(im, jm, km, n)];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        if (a == 0 && bb == 0 && d == 0) continue;
+        urg = urg + rho[IDX(is[a], js[bb], ks[d], n)];
+      }
+  // 1/27 as a float-float constant
+  const double r27 = 1.0 / 27.0;
+  const float r27h = (float)r27;
+  const FF w = ff_div(ff_mul(ff_of(urg), {r27h, (float)(r27 - (double)r27h)}), det);
+#pragma unroll
+  for (int f = 0; f < 6; ++f) {
+    const FF cf = ff_mul(w, b[f]);
+    coef[(i64)f * n3 + t] = make_float2(cf.hi, cf.lo);
+    coef32[(i64)f * n3 + t] = cf.hi;
+  }
+}
+
+void launch_metric_ff(const double* def, const double* rho, int n, double dx, double* coef, float* coef32,
+                      cudaStream_t s) {
+  const i64 n3 = (i64)n * n * n;
+  prof_begin(KK_METRIC, s, n3, n);
+  k_metric_ff<<<grid_of(n3, kBlock), kBlock, 0, s>>>(def, rho, n, 1.0 / (dx * dx), reinterpret_cast<float2*>(coef),
+                                                     coef32);
+  prof_end(KK_METRIC, s, n);
+  count_launch();
+}
+
 // in place: doubles -> (hi, lo) pairs in the same 8 bytes, and back
 __global__ void k_ff_split(double* __restrict__ a, i64 count) {
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;

@@ -137,6 +137,8 @@ struct mmh_ctx {
   // mixed form: inverse of the coarsest (4^3) level's operator, formed with
   // each metric (64 x 64 FP64)
   double* coarse_inv = nullptr;
+  // the finest solve level's FP64 coefficient buffer holds float-float pairs
+  bool coef_ff = false;
   uint8_t* mask(int q) { return keep_masks ? masks + q * n3 : nullptr; }
 
   double* defp() { return h64.u[0]; }
@@ -217,6 +219,11 @@ int guard_or_zerosum(mmh_ctx* c, int l, double margin, double floor_, bool guard
   Hier<T>& H = hier<T>(c);
   int n = c->nl[l];
   i64 n3 = (i64)n * n * n;
+  // The mixed form's FP32 preconditioner keeps the constants its levels
+  // carry: they lie in the operator's null space (every row's coefficients
+  // sum to zero), so they change neither the PCG's residuals nor its dot
+  // products with them, and the outer loop removes the solution's mean.
+  if (!guard && std::is_same<T, float>::value && c->cfg.schedule == MMH_SCHED_TOL) return MMH_OK;
   if (!guard) return zerosum<T>(c, H.u[l], n3);
   launch_guard(&c->sc->r1bits[l], &c->sc->errbits[l], margin, floor_, &c->sc->gflag[l], &c->sc->guards, c->s);
   CK(cudaMemsetAsync(c->sc->acc[3], 0, 16, c->s));
@@ -287,15 +294,36 @@ int pull_scal(mmh_ctx* c) {
   return MMH_OK;
 }
 
+// Smallest tolerance the float-float outer residual of the mixed form
+// serves: its rounding is ~1e-12 of max|rhs| (terms of ~n/(2 pi) |rhs|, ~2^-45
+// each); tighter tolerances take the FP64 residual.
+const double kFFTolMin = 1e-10;
+
+// Whether the mixed form's finest-level coefficients of this solve are kept
+// as float-float pairs (the tolerance schedule above kFFTolMin).
+bool ff_outer(const mmh_ctx* c) {
+  return c->cfg.precision == MMH_MIXED && c->cfg.schedule == MMH_SCHED_TOL && c->cfg.tol >= kFFTolMin;
+}
+
 // Build the coarse geometry (restricted def and density) and the metric of
-// every level from l0 down (FP64; FP32 copies for the mixed form).
+// every level from l0 down (FP64; FP32 copies for the mixed form, whose
+// finest level's metric is formed as float-float pairs when its outer loop
+// keeps them).
 int build_levels(mmh_ctx* c, int l0) {
   for (int l = l0 + 1; l < c->nlev; ++l) {
     launch_restrict27<double>(c->defl[l - 1], c->nl[l - 1], c->defl[l], c->s);
     launch_restrict27<double>(c->rhol[l - 1], c->nl[l - 1], c->rhol[l], c->s);
   }
+  c->coef_ff = false;
   for (int l = l0; l < c->nlev; ++l) {
     int n = c->nl[l];
+    // (a solve on the coarsest level itself keeps FP64 coefficients: its exact
+    // coarse solve is formed from them)
+    if (l == l0 && l0 < c->nlev - 1 && ff_outer(c)) {
+      launch_metric_ff(c->defl[l], c->rhol[l], n, double(1 << l), c->h64.coef[l], c->h32.coef[l], c->s);
+      c->coef_ff = true;
+      continue;
+    }
     launch_metric<double>(c->defl[l], c->rhol[l], n, double(1 << l), c->h64.coef[l], c->s,
                           c->cfg.precision == MMH_MIXED);
     if (c->cfg.precision == MMH_MIXED) launch_d2f(c->h64.coef[l], c->h32.coef[l], 6 * (i64)n * n * n, c->s);
@@ -451,10 +479,6 @@ int true_residual(mmh_ctx* c, int l0, double dx, const double* x, const double* 
 // (FP32 V-cycle preconditioner) on the correction to a relative 1e-3, update
 // of the outer solution -- until the outer residual meets tol.
 const double kInnerTol = 1e-3;
-// Smallest tolerance the float-float outer residual serves: its rounding is
-// ~1e-12 of max|rhs| (terms of ~n/(2 pi) |rhs|, ~2^-45 each); tighter
-// tolerances take the FP64 residual.
-const double kFFTolMin = 1e-10;
 const int kInnerMax = 60;
 
 // the same from the float-float outer solution and coefficients (mixed form)
@@ -491,7 +515,8 @@ int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_
     // FP64 residual of an FP64 solution.
     const bool ff = c->cfg.tol >= kFFTolMin;
     if (ff) {
-      launch_ff_split(c->h64.coef[l0], 6 * n3, c->s);
+      if (!c->coef_ff) launch_ff_split(c->h64.coef[l0], 6 * n3, c->s);
+      c->coef_ff = true;
       launch_ff_split(c->px, n3, c->s);
     }
     auto outer_residual = [&](float* r32, double* r) {
@@ -511,7 +536,10 @@ int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_
       launch_fill<float>(c->pe32, n3, 0.0f, c->s);
       int it = 0;
       double rin = 0.0, r0 = 0.0;
-      int st = pcg_core<float>(c, l0, dx, c->pe32, c->pb32, c->pp32, c->pq32, rmax, kInnerTol, kInnerMax, &it, &rin,
+      // the inner solve reduces the residual by kInnerTol, or only as far as
+      // the outer tolerance still needs (with a margin) when that is less
+      const double inner_tol = std::max(kInnerTol, 0.3 * c->cfg.tol * rn / rmax);
+      int st = pcg_core<float>(c, l0, dx, c->pe32, c->pb32, c->pp32, c->pq32, rmax, inner_tol, kInnerMax, &it, &rin,
                                &r0);
       if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
       total += it;
@@ -521,12 +549,14 @@ int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_
         launch_add_f2d(c->px, c->pe32, n3, c->s);
     }
     if (ff) {
-      // zero mean (the exact sum of all hi and lo parts), residual, back to FP64
+      // zero mean (the exact sum of all hi and lo parts), back to FP64.  The
+      // operator annihilates constants (each row's coefficients sum to zero),
+      // so the residual reported is the last outer residual.
       CK(cudaMemsetAsync(c->sc->acc[0], 0, 16, c->s));
       launch_fxsum<float>(reinterpret_cast<const float*>(c->px), 2 * n3, c->sc->acc[0], &c->sc->bad, c->s);
       launch_fx_mean(c->sc->acc[0], (double)n3, &c->sc->mean, c->s);
       launch_ff_sub_mean(c->px, &c->sc->mean, n3, c->s);
-      RET(outer_residual(nullptr, &rt));
+      rt = rmax;
       launch_ff_join(c->px, n3, c->s);
     }
   }
