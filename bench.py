@@ -188,7 +188,30 @@ def cpu_sample(n_full, niter, sigma, seed, tol, n_sample=256):
                    f"spectral outputs ({t_out:.2f} s), scaled by {niter} iterations and by the cell count "
                    f"({n_full}/{n_sample})^3 = {scale:g}"),
         "sample_seconds": t_it + t_out,
+        "reference_schedule_fp32": reference_schedule_sample(n_full, niter, sigma, seed, n_sample),
     }
+
+
+def reference_schedule_sample(n_full, niter, sigma, seed, n_sample=256):
+    """The reference's own algorithm in its own precision, for context: the
+    oracle in FP32 with the reference schedule (one V-cycle per iteration,
+    4*NG/n sweeps per level, NG the sample's grid), one complete deformation
+    iteration and the outputs of the n_sample^3 instance, scaled like the
+    main sample.  Its solves are not run to the tolerance: this is what the
+    Fortran (FP32 default reals, mmh/Makefile:9) computes per iteration, not
+    the same work as the timed reconstruction."""
+    import oracle
+    import fields
+    defpot, u = fields.initial_state(n_sample, sigma=sigma, seed=seed, dtype=np.float32)
+    t = time.perf_counter()
+    d, _, _, _, diag = oracle.iteration(defpot, u, sched=oracle.SCHED_REF)
+    t_it = time.perf_counter() - t
+    t_out = _oracle_outputs_seconds(oracle, d)
+    scale = (n_full / n_sample) ** 3
+    return {"value": scale * (niter * t_it + t_out), "unit": UNIT,
+            "sample": (f"oracle FP32, reference schedule (one V-cycle of 4*NG/n sweeps per level, NG = {n_sample}): one "
+                       f"iteration of the {n_sample}^3 instance ({t_it:.2f} s, relative residual after it "
+                       f"{diag['resid_rel']:.2g}) and its outputs ({t_out:.2f} s), scaled as above")}
 
 
 def reference_arm(args):
@@ -225,12 +248,14 @@ def reference_arm(args):
               f"iterations of the {m}^3 instance, one per step (median {statistics.median(times):.2f} s, last solve "
               f"{diag['vcycles']} PCG iterations), spectral outputs {t_out:.2f} s; scaled by {args.niter} iterations "
               f"and by the cell count ({args.n}/{m})^3 = {scale:g}")
+    ref32 = reference_schedule_sample(args.n, args.niter, args.sigma, args.seed, m)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * wall / max(args.steps, 1), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args),
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "reference_schedule_fp32": ref32},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the Fortran reference cannot be compiled here (no Fortran compiler); the CPU restatement "
                 "in oracle/ stands in for it",
@@ -593,7 +618,7 @@ def main():
     cpu = None
     if args.cpu_sample != "none" and not dist:
         cpu = cpu_sample(n, args.niter, args.sigma, args.seed, args.tol, n_sample=args.cpu_n)
-        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "reference_schedule_fp32")}
 
     value = ms_mixed / 1000.0 / world  # whole-job seconds per reconstruction (replicas)
     line = {
