@@ -177,6 +177,94 @@ __global__ void k_adj_hess(const double* __restrict__ abar, int n, double* __res
   out[t] = add ? out[t] + r : r;
 }
 
+// Adjoint of the final compression test's correction (limiter.f90:425-597)
+// with its mask frozen.  On a limited cell defplim = tlim =
+// 3 (1/cmpmax - lambda_min(C)) / dtold, C = I + dtold Hess(defp_s) +
+// Hess(def) (as k_limiter_mask forms it), and for a simple smallest
+// eigenvalue d lambda_min / dC = v v^T, v its unit eigenvector (the cross
+// product of two rows of C - lambda_min I).  With g = mask . P w (P the
+// symmetric FFT Poisson operator), abar = dJ/dC for J = sum g defplim:
+// abar = -3 g / dtold (v1^2, 2 v1 v2, 2 v1 v3, v2^2, 2 v2 v3, v3^2), the
+// off-diagonal entries counting both places they occupy in C.
+__global__ void k_adj_limiter(const double* __restrict__ def, const double* __restrict__ defps,
+                              const double* __restrict__ pw, const uint8_t* __restrict__ mask, int n, double dtold,
+                              double* __restrict__ abar) {
+  const i64 n3 = (i64)n * n * n;
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  if (mask[t]) {
+    int i, j, k;
+    cell_of(t, n, i, j, k);
+    const int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
+#define P_(x, y, z) defps[IDX(x, y, z, n)]
+#define D_(x, y, z) def[IDX(x, y, z, n)]
+    double pxx = (P_(ip, j, k) - 2.0 * P_(i, j, k) + P_(im, j, k)) * dtold;
+    double pyy = (P_(i, jp, k) - 2.0 * P_(i, j, k) + P_(i, jm, k)) * dtold;
+    double pzz = (P_(i, j, kp) - 2.0 * P_(i, j, k) + P_(i, j, km)) * dtold;
+    double pxy = (P_(ip, jp, k) - P_(im, jp, k) - P_(ip, jm, k) + P_(im, jm, k)) * 0.25 * dtold;
+    double pyz = (P_(i, jp, kp) - P_(i, jp, km) - P_(i, jm, kp) + P_(i, jm, km)) * 0.25 * dtold;
+    double pxz = (P_(ip, j, kp) - P_(im, j, kp) - P_(ip, j, km) + P_(im, j, km)) * 0.25 * dtold;
+    pxx = pxx + (D_(ip, j, k) - 2.0 * D_(i, j, k) + D_(im, j, k));
+    pyy = pyy + (D_(i, jp, k) - 2.0 * D_(i, j, k) + D_(i, jm, k));
+    pzz = pzz + (D_(i, j, kp) - 2.0 * D_(i, j, k) + D_(i, j, km));
+    pxy = pxy + (D_(ip, jp, k) - D_(im, jp, k) - D_(ip, jm, k) + D_(im, jm, k)) * 0.25;
+    pyz = pyz + (D_(i, jp, kp) - D_(i, jp, km) - D_(i, jm, kp) + D_(i, jm, km)) * 0.25;
+    pxz = pxz + (D_(ip, j, kp) - D_(im, j, kp) - D_(ip, j, km) + D_(im, j, km)) * 0.25;
+#undef P_
+#undef D_
+    const double c11 = 1.0 + pxx, c22 = 1.0 + pyy, c33 = 1.0 + pzz, c12 = pxy, c13 = pxz, c23 = pyz;
+    // smallest eigenvalue (the trigonometric formula of the compression test)
+    const double pi = 3.14159265358979323846264338328;
+    const double mu = (c11 + c22 + c33) / 3.0;
+    const double d11 = c11 - mu, d22 = c22 - mu;
+    double aa = -(d11 * d11 + c12 * c12 + c13 * c13 + d11 * d22 + d22 * d22 + c23 * c23);
+    const double bb = -d11 * (c12 * c12) + d11 * d11 * d22 - c12 * c12 * d22 + c13 * c13 * d22 + d11 * (d22 * d22) -
+                      2.0 * c12 * c13 * c23 + d11 * (c23 * c23);
+    if (fabs(aa) < 1.e-20) aa = 1.e-20;
+    const double am = 2.0 * sqrt(fabs(-aa) / 3.0);
+    const double th = acos(fmax(-1.0, fmin(1.0, 3.0 * bb / aa / am))) / 3.0;
+    const double lam = fmin(fmin(am * cos(th), am * cos(th + 2.0 * pi / 3.0)), am * cos(th + 4.0 * pi / 3.0)) + mu;
+    // eigenvector: the longest cross product of two rows of C - lam I
+    const double r1[3] = {c11 - lam, c12, c13}, r2[3] = {c12, c22 - lam, c23}, r3[3] = {c13, c23, c33 - lam};
+    auto cross = [](const double* x, const double* y, double* z) {
+      z[0] = x[1] * y[2] - x[2] * y[1];
+      z[1] = x[2] * y[0] - x[0] * y[2];
+      z[2] = x[0] * y[1] - x[1] * y[0];
+    };
+    double v[3], w2[3], w3[3];
+    cross(r1, r2, v);
+    cross(r1, r3, w2);
+    cross(r2, r3, w3);
+    double nv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    const double n2 = w2[0] * w2[0] + w2[1] * w2[1] + w2[2] * w2[2];
+    const double n3v = w3[0] * w3[0] + w3[1] * w3[1] + w3[2] * w3[2];
+    if (n2 > nv) { v[0] = w2[0]; v[1] = w2[1]; v[2] = w2[2]; nv = n2; }
+    if (n3v > nv) { v[0] = w3[0]; v[1] = w3[1]; v[2] = w3[2]; nv = n3v; }
+    if (nv > 0.0) {
+      const double rn = 1.0 / sqrt(nv);
+      v[0] *= rn; v[1] *= rn; v[2] *= rn;
+      const double sc = -3.0 * pw[t] / dtold;
+      a[0] = sc * v[0] * v[0];
+      a[1] = sc * 2.0 * v[0] * v[1];
+      a[2] = sc * 2.0 * v[0] * v[2];
+      a[3] = sc * v[1] * v[1];
+      a[4] = sc * 2.0 * v[1] * v[2];
+      a[5] = sc * v[2] * v[2];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 6; ++q) abar[q * n3 + t] = a[q];
+}
+
+// out = a + s * b
+__global__ void k_adj_axpy(const double* __restrict__ a, double s, const double* __restrict__ b,
+                           double* __restrict__ out, i64 n3) {
+  i64 q = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n3) return;
+  out[q] = a[q] + s * b[q];
+}
+
 // out = a * b (op 1) or a - b (op 0), elementwise
 __global__ void k_adj_pair(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out,
                            int op, i64 n3) {
@@ -417,6 +505,17 @@ void launch_adj_metric(const double* def, const double* lam, const double* u, co
   k_adj_metric<<<grid_of(n3, kBlock), kBlock, 0, s>>>(def, lam, u, urg, y, rptr, n, abar);
   count_launch();
 }
+void launch_adj_limiter(const double* def, const double* defps, const double* pw, const uint8_t* mask, int n,
+                        double dtold, double* abar, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  k_adj_limiter<<<grid_of(n3, kBlock), kBlock, 0, s>>>(def, defps, pw, mask, n, dtold, abar);
+  count_launch();
+}
+void launch_adj_axpy(const double* a, double sc, const double* b, double* out, i64 n3, cudaStream_t s) {
+  k_adj_axpy<<<grid_of(n3, kBlock), kBlock, 0, s>>>(a, sc, b, out, n3);
+  count_launch();
+}
+
 void launch_adj_hess(const double* abar, int n, double* out, int add, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
   k_adj_hess<<<grid_of(n3, kBlock), kBlock, 0, s>>>(abar, n, out, add);

@@ -162,6 +162,11 @@ void launch_adj_sub(const double* a, const double* b, double* out, i64 n3, cudaS
 void launch_adj_metric(const double* def, const double* lam, const double* u, const double* urg, const double* y,
                        const double* rptr, int n, double* abar, cudaStream_t s);
 void launch_adj_hess(const double* abar, int n, double* out, int add, cudaStream_t s);
+// the final compression test's correction: abar = dJ/dC on the limited cells
+// (mask) for J = sum pw * defplim; out = a + s * b
+void launch_adj_limiter(const double* def, const double* defps, const double* pw, const uint8_t* mask, int n,
+                        double dtold, double* abar, cudaStream_t s);
+void launch_adj_axpy(const double* a, double sc, const double* b, double* out, i64 n3, cudaStream_t s);
 void launch_adj_alpha(const double* baj, const double* defp, const double* cc, int n, double* alpha, cudaStream_t s);
 void launch_adj_dpv(const double* sd, const double* cc, const double* alpha, const double* x, const double* rbar,
                     double scale, int n, double* xbar, double* alphabar, double* cbar, cudaStream_t s);

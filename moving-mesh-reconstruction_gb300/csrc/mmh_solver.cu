@@ -809,13 +809,12 @@ struct DevTemp {
 struct CalcKeep {
   double* pre;
   double* uf;
-  uint8_t* mk;
+  uint8_t* mk;   // 3 n^3 bytes: pass 1's expansion and compression masks, the final test's mask
   double* ratio;
+  long long* ncompress;  // host, may be null: cells the final compression test limited
 };
 
 // calcdefp_dev on the resident def and rho, keeping what the adjoint needs.
-// MMH_ERR_UNSUPPORTED when the final compression test limits a cell (that
-// correction is not transposed); defp is then not corrected either.
 int calcdefp_fwd_keep(mmh_ctx* c, double dtold, double dtaumesh, const CalcKeep& kp, mmh_diag* d) {
   int n = c->n;
   i64 n3 = c->n3;
@@ -837,10 +836,14 @@ int calcdefp_fwd_keep(mmh_ctx* c, double dtold, double dtaumesh, const CalcKeep&
   CK(cudaMemcpyAsync(kp.uf, defp, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
   smooth_step(c, defp, c->scr);
   smooth_step(c, c->scr, defp);
-  launch_limiter_mask(c->defplim, c->def, defp, n, dtold, &c->sc->lim, nullptr, c->s);
+  launch_limiter_mask(c->defplim, c->def, defp, n, dtold, &c->sc->lim, kp.mk + 2 * n3, c->s);
   RET(pull_scal(c));
+  if (c->hsc->lim.ncompress) {
+    RET(limiter_poisson(c, defp, c->defplim));
+    RET(pull_scal(c));
+  }
+  if (kp.ncompress) *kp.ncompress = (long long)c->hsc->lim.ncompress;
   lim_to_diag(c->hsc->lim, d);
-  if (c->hsc->lim.ncompress) return MMH_ERR_UNSUPPORTED;
   return MMH_OK;
 }
 
@@ -898,6 +901,39 @@ int calcdefp_adj_core(mmh_ctx* c, double dtold, double dtaumesh, const CalcKeep&
   return MMH_OK;
 }
 
+// calcdefp_adj_core for a forward pass whose final compression test limited
+// cells: defp = defp_s + P(mask . tlim(C)), C = I + dtold Hess(defp_s) +
+// Hess(def), defp_s = S^2 uf, P the FFT Poisson correction (a real even
+// Fourier multiplier, so P^T = P).  With abar = dJ/dC (k_adj_limiter) for the
+// seed g = mask . P w, the seed of defp_s is w + dtold Hess^T(abar) and def
+// receives Hess^T(abar) directly.  scratch: 10 n^3 (the core's 8 first).
+int calcdefp_adj_full(mmh_ctx* c, double dtold, double dtaumesh, const CalcKeep& kp, bool limited, const double* w,
+                      double* grho, double* gdef, double* scratch, mmh_diag* da) {
+  if (!limited) return calcdefp_adj_core(c, dtold, dtaumesh, kp, w, grho, gdef, scratch, da);
+  const int n = c->n;
+  const i64 n3 = c->n3;
+  if (dtold < 1.e-8) dtold = 1.0;
+  double* abar = scratch;        // 6 n^3
+  double* pw = scratch + 6 * n3;
+  double* ds = scratch + 7 * n3;
+  double* wl = scratch + 8 * n3;  // smoothing scratch, then the seed of defp_s
+  double* gl = scratch + 9 * n3;
+  // P w (the correction's transforms run whenever the count is non-zero)
+  CK(cudaMemsetAsync(&c->sc->lim.ncompress, 1, sizeof(c->sc->lim.ncompress), c->s));
+  launch_fill<double>(pw, n3, 0.0, c->s);
+  RET(limiter_poisson(c, pw, w));
+  // defp_s = S^2 uf, smoothed as the forward pass smoothed it
+  CK(cudaMemcpyAsync(ds, kp.uf, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
+  smooth_step(c, ds, wl);
+  smooth_step(c, wl, ds);
+  launch_adj_limiter(c->def, ds, pw, kp.mk + 2 * n3, n, dtold, abar, c->s);
+  launch_adj_hess(abar, n, gl, 0, c->s);
+  launch_adj_axpy(w, dtold, gl, wl, n3, c->s);
+  RET(calcdefp_adj_core(c, dtold, dtaumesh, kp, wl, grho, gdef, scratch, da));
+  if (gdef) launch_add(gdef, gl, n3, c->s);
+  return MMH_OK;
+}
+
 // Gradients of J = w^T defp with respect to the density and to def for one
 // calcdefp increment on the resident def and rho (no counterpart in the
 // reference), the limiter's branch choices those of this forward pass.  w
@@ -910,16 +946,18 @@ int calcdefp_adjoint_dev(mmh_ctx* c, double dtold, double dtaumesh, const double
   i64 n3 = c->n3;
   DevTemp buf;
   buf.s = c->s;
-  if (cudaMallocAsync(&buf.p, sizeof(double) * (10 * n3 + 1) + 2 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
-  double* scratch = (double*)buf.p;  // 8 n^3
+  if (cudaMallocAsync(&buf.p, sizeof(double) * (12 * n3 + 1) + 3 * n3, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
+  double* scratch = (double*)buf.p;  // 10 n^3
+  long long nc = 0;
   CalcKeep kp;
-  kp.pre = scratch + 8 * n3;
+  kp.pre = scratch + 10 * n3;
   kp.uf = kp.pre + n3;
   kp.ratio = kp.uf + n3;
   kp.mk = (uint8_t*)(kp.ratio + 1);
+  kp.ncompress = &nc;
   RET(calcdefp_fwd_keep(c, dtold, dtaumesh, kp, d));
   mmh_diag da{};
-  RET(calcdefp_adj_core(c, dtold, dtaumesh, kp, w, grho, gdef, scratch, &da));
+  RET(calcdefp_adj_full(c, dtold, dtaumesh, kp, nc > 0, w, grho, gdef, scratch, &da));
   if (d) d->vcycles += da.vcycles;
   return MMH_OK;
 }
@@ -994,7 +1032,7 @@ int iterate_adjoint_dev(mmh_ctx* c, int niter, int every, const double* wdef, co
   // calcdefp forward's pre, uf | final state | rhobar, rhobar_next, defbar,
   // four gradient parts | adjoint scratch (15: relaxing's, or calcdefp's 8) |
   // segment ratios and masks
-  const i64 words = (2 * (i64)ncp + 5 * (i64)seg + 2 + 7 + 15) * n3 + seg + (2 * (i64)seg * n3 + 7) / 8;
+  const i64 words = (2 * (i64)ncp + 5 * (i64)seg + 2 + 7 + 15) * n3 + seg + (3 * (i64)seg * n3 + 7) / 8;
   if (cudaMallocAsync(&buf.p, sizeof(double) * words, c->s) != cudaSuccess) return MMH_ERR_NOMEM;
   double* ckpt = (double*)buf.p;
   double* segst = ckpt + 2 * (i64)ncp * n3;
@@ -1010,13 +1048,15 @@ int iterate_adjoint_dev(mmh_ctx* c, int niter, int every, const double* wdef, co
   double* ratios = scratch + 15 * n3;
   uint8_t* masks = (uint8_t*)(ratios + seg);
   double* defp = c->defp();
+  std::vector<long long> limited(seg, 0);  // cells each segment iteration's final test limited
   auto keep = [&](int q) {
     CalcKeep kp;
     double* sk = segst + 5 * (i64)q * n3;
     kp.pre = sk + 3 * n3;
     kp.uf = sk + 4 * n3;
     kp.ratio = ratios + q;
-    kp.mk = masks + 2 * (i64)q * n3;
+    kp.mk = masks + 3 * (i64)q * n3;
+    kp.ncompress = &limited[q];
     return kp;
   };
   // forward pass with checkpoints
@@ -1028,7 +1068,6 @@ int iterate_adjoint_dev(mmh_ctx* c, int niter, int every, const double* wdef, co
     mmh_diag dd{};
     int st = calcdefp_dev(c, 1.0, 1.0, nullptr, nullptr, nullptr, &dd);
     if (st != MMH_OK) return st;
-    if (dd.ncompress) return MMH_ERR_UNSUPPORTED;
     launch_add(c->def, defp, n3, c->s);
     RET(relaxing_dev(c, 1.0));
     if (d) *d = dd;
@@ -1076,7 +1115,7 @@ int iterate_adjoint_dev(mmh_ctx* c, int niter, int every, const double* wdef, co
       launch_add(gb, dbar, n3, c->s);
       // calcdefp: defp_k = calcdefp(def_k, rho_k)
       CK(cudaMemcpyAsync(c->def, sk, f, cudaMemcpyDeviceToDevice, c->s));
-      RET(calcdefp_adj_core(c, 1.0, 1.0, keep(k - k0), gb, gc, gd, scratch, nullptr));
+      RET(calcdefp_adj_full(c, 1.0, 1.0, keep(k - k0), limited[k - k0] > 0, gb, gc, gd, scratch, nullptr));
       launch_add(rbar, gc, n3, c->s);
       launch_add(dbar, gd, n3, c->s);
     }

@@ -183,3 +183,53 @@ def test_relaxing_adjoint_matches_finite_differences(mmh, fields):
             print(f"relaxing d/d{name}: fd {fd:.12e} adjoint {ad:.12e} rel {abs(fd - ad) / abs(ad):.2e} "
                   f"of sum {abs(fd - ad) / scale:.2e}")
             assert abs(fd - ad) <= 1e-6 * max(abs(ad), scale), (name, fd, ad)
+
+
+@pytest.mark.gpu
+def test_calcdefp_adjoint_through_the_compression_correction(mmh, fields):
+    """A compressing region (a bump in def with centre curvature -0.95, so the
+    smallest eigenvalue of C = I + Hess(def) + dtold Hess(defp) falls below
+    1/cmpmax = 0.1): the final compression test limits cells and its FFT
+    Poisson correction (limiter.f90:425-597) enters defp.  The adjoint through
+    it (mask frozen, d lambda_min / dC = v v^T, the correction's operator
+    symmetric) against central differences; the masks of all three limiter
+    tests are checked unchanged at the perturbed inputs."""
+    n, dtold, dtaumesh, h = 32, 1.0, 1.0, 1e-5
+    rho = fields.lognormal_density(n, sigma=0.4, seed=71)
+    defpot = _bump(n, kappa=-0.95, width=3.0)
+    rng = np.random.default_rng(72)
+    w = _s3(rng.standard_normal((n, n, n)))
+    w = np.asfortranarray(w - w.mean())
+    dirs = [np.asfortranarray(_s3(rng.standard_normal((n, n, n)))) for _ in range(2)]
+    ddirs = []
+    for q in range(2):
+        v = smooth_field(n, 1.0, 80 + q)
+        ddirs.append(np.asfortranarray(v / _max_hessian(v)))
+    edge = np.abs(np.abs(1.0 - rho) - 2.0).min()
+    assert edge > 20 * h * max(np.abs(v).max() for v in dirs)
+    with mmh.Context(n, precision=mmh.MMH_FP64, schedule=mmh.MMH_SCHED_TOL, tol=1e-13, max_cycles=400) as ctx:
+        grho, gdef, d = ctx.calcdefp_adjoint(defpot, rho, w, dtold, dtaumesh, nfluid=1)
+        assert d["ncompress"] > 0
+        ctx.keep_masks(True)
+
+        def J(dp, r):
+            defp = np.zeros((n, n, n), order="F")
+            ctx.calcdefp(defp, None, None, np.asfortranarray(dp), np.asfortranarray(r), dtold, dtaumesh, nfluid=1)
+            return float(np.sum(w * defp)), ctx.masks()
+
+        _, m0 = J(defpot, rho)
+        assert m0["compress2"].sum() > 0
+        for name, g, vs in (("rho", grho, dirs), ("def", gdef, ddirs)):
+            for v in vs:
+                if name == "rho":
+                    (jp, mp), (jm, mm) = J(defpot, rho + h * v), J(defpot, rho - h * v)
+                else:
+                    (jp, mp), (jm, mm) = J(defpot + h * v, rho), J(defpot - h * v, rho)
+                for key in m0:
+                    assert np.array_equal(mp[key], m0[key]) and np.array_equal(mm[key], m0[key]), (name, key)
+                fd = (jp - jm) / (2 * h)
+                ad = float(np.sum(g * v))
+                scale = float(np.sum(np.abs(g * v)))
+                print(f"compression correction d/d{name}: fd {fd:.12e} adjoint {ad:.12e} "
+                      f"rel {abs(fd - ad) / abs(ad):.2e} of sum {abs(fd - ad) / scale:.2e}")
+                assert abs(fd - ad) <= 1e-6 * max(abs(ad), 1e-3 * scale), (name, fd, ad)
