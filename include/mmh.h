@@ -292,10 +292,12 @@ int mmh_relax_noalloc_f64(const double* d_deformpot, const double* d_rho, double
  * (expansion and compression masks, flux clamps, the density clip, the
  * metric's tangle fallback) frozen where this forward pass took them.  defp
  * is defined up to a constant, so w counts through its deviation from its
- * mean.  Needs a solving schedule (MMH_SCHED_TOL or MMH_SCHED_VCYCLE;
- * MMH_SCHED_REF gives MMH_ERR_UNSUPPORTED), and returns MMH_ERR_UNSUPPORTED
- * when the final compression test limits a cell.  The diag is that of the
- * forward pass; vcycles adds the adjoint solve's. */
+ * mean.  Where the final compression test limits cells, the gradient runs
+ * through its FFT Poisson correction with the mask frozen (the smallest
+ * eigenvalue's derivative v v^T; a repeated smallest eigenvalue has none).
+ * Needs a solving schedule (MMH_SCHED_TOL or MMH_SCHED_VCYCLE; MMH_SCHED_REF
+ * gives MMH_ERR_UNSUPPORTED).  The diag is that of the forward pass; vcycles
+ * adds the adjoint solve's. */
 int mmh_calcdefp_adjoint_f64(mmh_ctx* ctx, const double* def, const double* u, int nfluid, double dtold1,
                              double dtaumesh, const double* w, double* grho, double* gdef, mmh_diag* diag);
 
