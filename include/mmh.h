@@ -321,6 +321,18 @@ int mmh_relaxing_adjoint_f64(mmh_ctx* ctx, const double* u, const double* def, c
 int mmh_iterate_adjoint_f64(mmh_ctx* ctx, int niter, int checkpoint_every, const double* wdef, const double* wdelta,
                             double* grho, double* gdef, mmh_diag* diag);
 
+/* ---- Gauss-Seidel tile tuning (no counterpart in the reference) -------- */
+/* The FP32 plane Gauss-Seidel kernel (the mixed form's smoother on grids of
+ * 64^3 and up) has four tile shapes (TX x TY cells: 0 = 32x16, 1 = 64x8,
+ * 2 = 16x32, 3 = 32x8).  All of them compute the same bits; the first sweep on
+ * a grid size and device outside a stream capture times those that fit (three
+ * half sweeps each, phi untouched) and keeps the fastest.  mmh_gs_tile_pin
+ * pins one shape for every grid instead (-1: back to timing); mmh_gs_tile
+ * reports the shape in use for grid n on the current device (MMH_ERR_ARG when
+ * none has been chosen yet). */
+int mmh_gs_tile_pin(int shape);
+int mmh_gs_tile(int n, int* tx, int* ty);
+
 /* ---- kernel timing (no counterpart in the reference) -------------------- */
 /* Arm CUDA-event timing of one kernel kind (MMH_K_* | MMH_K_F32 for the FP32
  * instantiation) on the stream it is launched on; mmh_profile_stop returns the

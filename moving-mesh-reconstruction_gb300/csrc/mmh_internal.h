@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 namespace mmh {
 
 typedef long long i64;
@@ -33,6 +35,11 @@ void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_
 void launch_residual_fma(const double* phi, const double* rhs, const double* coef, int n, double dx, float* r32,
                          unsigned long long* maxbits, cudaStream_t s);
 template <class T> void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, T* scratch, cudaStream_t s);
+// FP32 plane-kernel tile autotuning: the shape pinned for every grid (-1:
+// timed per grid size and device), and the shape chosen for n (-1: none yet)
+constexpr int kGsShapes = 4;
+extern std::atomic<int> gs_tile_override;
+int gs_tile_chosen(int n, int* tx, int* ty);
 template <class T>
 void launch_residual(const T* phi, const T* rhs, const T* coef, int n, T dx, T* r, float* r32,
                      unsigned long long* maxbits, cudaStream_t s);

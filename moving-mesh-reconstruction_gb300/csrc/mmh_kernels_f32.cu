@@ -1,9 +1,80 @@
 // FP32 kernels of the mixed-precision inner V-cycle (smoother, residual,
 // restriction, prolongation, zero-mean).  FMA contraction stays enabled here.
+#include <mutex>
+
 #include "mmh_launch.cuh"
 #include "mmh_pcg.cuh"
 
 namespace mmh {
+
+// Tile autotuning of the FP32 plane kernel (see gs_tile_choice), per device
+// (up to 64) and grid size (2^0 .. 2^15).
+static std::mutex g_tile_mu;
+static signed char g_tile[64][16];
+static bool g_tile_init = false;
+std::atomic<int> gs_tile_override{-1};
+
+int gs_tile_choice(int n, const float* phi, const float* rhs, const float* coef, float dx2, float* scratch,
+                   cudaStream_t s) {
+  const int pin = gs_tile_override.load();
+  if (pin >= 0 && pin < kGsShapes && gs_shape_fits(pin, n)) return pin;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  int lg = 0;
+  while ((1 << lg) < n && lg < 15) ++lg;
+  {
+    std::lock_guard<std::mutex> lock(g_tile_mu);
+    if (!g_tile_init) {
+      for (auto& row : g_tile)
+        for (auto& x : row) x = -1;
+      g_tile_init = true;
+    }
+    if (g_tile[dev][lg] >= 0) return g_tile[dev][lg];
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) return 0;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return 0;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return 0;
+  }
+  int best = 0;
+  float best_ms = 0.f;
+  for (int v = 0; v < kGsShapes; ++v) {
+    if (!gs_shape_fits(v, n)) continue;
+    gs_plane_half<float>(v, phi, phi, scratch, rhs, coef, n, dx2, 0, s);  // warm-up (attribute, caches)
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < 3; ++r) gs_plane_half<float>(v, phi, phi, scratch, rhs, coef, n, dx2, 0, s);
+    cudaEventRecord(e1, s);
+    count_launch(4);
+    float ms = 0.f;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) continue;
+    if (v == 0 || ms < best_ms) {
+      best = v;
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  std::lock_guard<std::mutex> lock(g_tile_mu);
+  g_tile[dev][lg] = (signed char)best;
+  return best;
+}
+
+int gs_tile_chosen(int n, int* tx, int* ty) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+  int lg = 0;
+  while ((1 << lg) < n && lg < 15) ++lg;
+  std::lock_guard<std::mutex> lock(g_tile_mu);
+  if (!g_tile_init || g_tile[dev][lg] < 0) return -1;
+  const int v = g_tile[dev][lg];
+  *tx = kGsShape[v].tx;
+  *ty = kGsShape[v].ty;
+  return v;
+}
+
 MMH_INSTANTIATE(float)
 MMH_INSTANTIATE_PCG(float)
 

@@ -2,6 +2,7 @@
 // unit includes this file and instantiates the launchers explicitly.
 #pragma once
 #include <atomic>
+#include <type_traits>
 
 #include "mmh_kernels.cuh"
 
@@ -38,9 +39,53 @@ void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_
   count_launch();
 }
 
-template <class T> struct GsTile;
-template <> struct GsTile<float> { static const int TX = 32, TY = 16; };
-template <> struct GsTile<double> { static const int TX = 32, TY = 8; };
+// Tile shapes of the fused plane kernel.  Every shape updates every cell with
+// the same operations in the same colour order, so the swept field is the
+// same bit for bit whichever runs; the shapes differ in halo overhead, active
+// threads per colour phase and shared memory.  FP32 levels try the shapes
+// below once per grid size and device and keep the fastest (gs_tile_choice);
+// FP64 levels keep (32, 8).
+struct GsShape {
+  int tx, ty;
+};
+constexpr GsShape kGsShape[kGsShapes] = {{32, 16}, {64, 8}, {16, 32}, {32, 8}};
+
+template <class T, int TX, int TY>
+void gs_plane_launch(const T* src, const T* nbr, T* dst, const T* rhs, const T* coef, int n, T dx2, int kpar,
+                     cudaStream_t s) {
+  const size_t smem = sizeof(T) * GsGeom<T, TX, TY>::WORDS;
+  static std::atomic<unsigned long long> attr_done{0};
+  smem_attr_once(k_gs_plane<T, TX, TY>, (int)smem, attr_done);
+  k_gs_plane<T, TX, TY><<<dim3(n / TX, n / TY, n / 2), 256, smem, s>>>(src, nbr, dst, rhs, coef, n, dx2, kpar);
+}
+
+// one half sweep with tile shape v (FP64: always (32, 8))
+template <class T>
+void gs_plane_half(int v, const T* src, const T* nbr, T* dst, const T* rhs, const T* coef, int n, T dx2, int kpar,
+                   cudaStream_t s) {
+  if constexpr (std::is_same<T, double>::value) {
+    (void)v;
+    gs_plane_launch<T, 32, 8>(src, nbr, dst, rhs, coef, n, dx2, kpar, s);
+  } else {
+    switch (v) {
+      case 1: gs_plane_launch<T, 64, 8>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
+      case 2: gs_plane_launch<T, 16, 32>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
+      case 3: gs_plane_launch<T, 32, 8>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
+      default: gs_plane_launch<T, 32, 16>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
+    }
+  }
+}
+
+// the kernel needs n >= TX + 8 and n >= TY + 8
+inline bool gs_shape_fits(int v, int n) { return n >= kGsShape[v].tx + 8 && n >= kGsShape[v].ty + 8; }
+
+// Tile shape for an FP32 grid of size n on the current device: the one
+// chosen before, else (outside a stream capture) each shape is timed on
+// three half sweeps that read phi and write the sweep's scratch buffer
+// (phi is left as it was), and the fastest is kept.  gs_tile_override >= 0
+// pins a shape instead.
+int gs_tile_choice(int n, const float* phi, const float* rhs, const float* coef, float dx2, float* scratch,
+                   cudaStream_t s);
 
 // nsweeps 8-colour Gauss-Seidel sweeps.  Grids of 64^3 and up run one fused
 // launch per half sweep (all in-plane colours of every plane of one parity);
@@ -50,18 +95,17 @@ void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nswe
   i64 h3 = (i64)(n / 2) * (n / 2) * (n / 2);
   T dx2 = dx * dx;
   if (n >= 64) {
-    constexpr int TX = GsTile<T>::TX, TY = GsTile<T>::TY;
-    const size_t smem = sizeof(T) * GsGeom<T, TX, TY>::WORDS;
-    static std::atomic<unsigned long long> attr_done{0};
-    smem_attr_once(k_gs_plane<T, TX, TY>, (int)smem, attr_done);
-    dim3 grid(n / TX, n / TY, n / 2);
+    int v = 0;
+    if constexpr (std::is_same<T, float>::value) {
+      if (nsweeps > 0) v = gs_tile_choice(n, phi, rhs, coef, dx2, scratch, s);
+    }
     // double buffer: a sweep reads a and leaves the swept field in b
     T* a = phi;
     T* b = scratch;
     for (int sw = 0; sw < nsweeps; ++sw) {
       for (int kpar = 0; kpar < 2; ++kpar) {
         prof_begin(kk<T>(KK_GS), s, 4 * h3, n);
-        k_gs_plane<T, TX, TY><<<grid, 256, smem, s>>>(a, kpar == 0 ? a : b, b, rhs, coef, n, dx2, kpar);
+        gs_plane_half<T>(v, a, kpar == 0 ? a : b, b, rhs, coef, n, dx2, kpar, s);
         prof_end(kk<T>(KK_GS), s, n);
         count_launch();
       }

@@ -1546,6 +1546,18 @@ int mmh_iterate_adjoint_f64(mmh_ctx* c, int niter, int checkpoint_every, const d
   if (gdef) RET(download(c, dw + 3 * n3, gdef, n3));
   return MMH_OK;
 }
+int mmh_gs_tile_pin(int shape) {
+  if (shape < -1 || shape >= mmh::kGsShapes) return MMH_ERR_ARG;
+  mmh::gs_tile_override.store(shape);
+  return MMH_OK;
+}
+
+int mmh_gs_tile(int n, int* tx, int* ty) {
+  if (!tx || !ty) return MMH_ERR_ARG;
+  *tx = *ty = 0;
+  return mmh::gs_tile_chosen(n, tx, ty) >= 0 ? MMH_OK : MMH_ERR_ARG;
+}
+
 int mmh_keep_masks(mmh_ctx* c, int on) {
   if (!c) return MMH_ERR_ARG;
   if (on && !c->masks) {

@@ -44,7 +44,7 @@ EXPORTS = (
     "mmh_relax_noalloc_f64", "mmh_batch_run", "mmh_calcdefp_adjoint_f64",
     "mmh_relaxing_adjoint_f64", "mmh_iterate_adjoint_f64", "mmh_state_stats",
     "mmh_power_spectrum_f64", "mmh_haloden", "mmh_coarsen",
-    "mmh_column_density", "mmh_gridfigure", "mmh_keep_masks", "mmh_masks",
+    "mmh_column_density", "mmh_gridfigure", "mmh_keep_masks", "mmh_masks", "mmh_gs_tile_pin", "mmh_gs_tile",
 )
 
 # kernel kinds for the timing hooks
@@ -174,6 +174,18 @@ def strerror(code):
 
 def launch_count():
     return int(lib().mmh_launch_count())
+
+
+def gs_tile_pin(shape):
+    """Pin the FP32 plane Gauss-Seidel tile shape (0..3) for every grid; -1
+    returns to timing the shapes per grid size."""
+    _chk(lib().mmh_gs_tile_pin(int(shape)), "gs_tile_pin")
+
+
+def gs_tile(n):
+    """(TX, TY) of the FP32 plane Gauss-Seidel tile in use for grid n, or None."""
+    tx, ty = C.c_int(), C.c_int()
+    return (tx.value, ty.value) if lib().mmh_gs_tile(int(n), C.byref(tx), C.byref(ty)) == MMH_OK else None
 
 
 def profile_start(kind):

@@ -83,3 +83,35 @@ def test_mixed_relax_fp32_sweeps(mmh, oracle, fields, n, nrelax, iopt):
     assert abs(rig - rio) <= 1e-4 * rio
     if iopt % 8 == 3:
         assert np.abs(rg - ro).max() <= 1e-4 * np.abs(ro).max()
+
+
+def test_fp32_sweep_tile_shapes_agree_bit_for_bit(mmh, oracle, fields):
+    """The four tile shapes of the FP32 plane kernel compute the same bits
+    (each pinned in turn); left to itself, the library times them on a grid's
+    first sweeps and reports the one it keeps."""
+    n, nrelax = 128, 2
+    defpot = smooth_field(n, 0.05, 7)
+    rho = fields.lognormal_density(n, sigma=0.5, seed=8)
+    rng = np.random.default_rng(9)
+    rhs = np.asfortranarray(rng.standard_normal((n, n, n)))
+    phi0 = np.asfortranarray(rng.standard_normal((n, n, n)))
+    out = []
+    try:
+        with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL) as ctx:
+            for shape in range(4):
+                mmh.gs_tile_pin(shape)
+                b = phi0.copy(order="F")
+                _, rinf = ctx.relax(b, rhs, defpot, rho, 1.0, nrelax, 18)
+                out.append((b, rinf))
+            mmh.gs_tile_pin(-1)
+            b = phi0.copy(order="F")
+            ctx.relax(b, rhs, defpot, rho, 1.0, nrelax, 18)
+            out.append((b, None))
+            chosen = mmh.gs_tile(n)
+    finally:
+        mmh.gs_tile_pin(-1)
+    for b, rinf in out[1:]:
+        assert np.array_equal(b, out[0][0])
+    assert all(r == out[0][1] for _, r in out[1:4])
+    print("tile kept for 128^3:", chosen)
+    assert chosen in [(32, 16), (64, 8), (16, 32), (32, 8)]
