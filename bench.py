@@ -633,6 +633,7 @@ def main():
         "solve": {"vcycles_last": diags[-1]["vcycles"], "resid_rel_last": diags[-1]["resid_rel"],
                   "ncompress_last": diags[-1]["ncompress"], "guards_last": diags[-1]["guards"]},
         "cells_per_s": n3 * args.niter * world / (ms_mixed / 1000.0),
+        "gs_tiles": {str(m): mmh.gs_tile(m) for m in (512, 256, 128, 64) if m <= n},
     }
     print(json.dumps(line))
     if dist:
