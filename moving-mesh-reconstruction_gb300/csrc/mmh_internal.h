@@ -133,9 +133,10 @@ void launch_ff_sub_mean(double* x, const double* mean, i64 count, cudaStream_t s
 void launch_residual_ff(const double* phi, const double* rhs, const double* coef, int n, double dx, float* r32,
                         unsigned long long* maxbits, cudaStream_t s);
 // the finest level's metric straight into float-float pairs (coef, the layout
-// launch_ff_split makes) and their hi parts (coef32, FP32)
+// launch_ff_split makes) and their hi parts (coef32, FP32); det (may be null)
+// receives det(A) rounded to FP64
 void launch_metric_ff(const double* def, const double* rho, int n, double dx, double* coef, float* coef32,
-                      cudaStream_t s);
+                      double* det, cudaStream_t s);
 
 // main.f90's iteration diagnostics: exact sums (def, def^2, defp^2, rho,
 // (rho-1)^2), ord_of-encoded extrema of rho, count of rho < 0, range flag

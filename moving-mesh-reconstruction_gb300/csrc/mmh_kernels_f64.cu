@@ -301,7 +301,7 @@ __global__ void k_limiter_pass1(double* __restrict__ tmp, const double* __restri
     int i, j, km;
     cell_of(t, n, i, j, km);
     int k = wp(km, n);
-    LimM m = lim_metric(def, n, i, j, k);
+    LimM m = lim_hess_det(def, n, i, j, k);
     double det = m.det;
     double rl = rho[t];
     double q = rl * rl / det;
@@ -367,20 +367,23 @@ void launch_limiter_pass1(double* tmp, const double* def, const double* rho, int
 
 // Bounds of the smallest eigenvalue that compression_of computes, from the
 // values it computes first (mu = trace/3, am): every root r_i = am*cos(.)
-// lies in [-am, am] and rounding is monotone, so min_i fl(r_i + mu) >=
-// fl(mu - am) = lo.  The root through theta + 2pi/3 has cos <= -1/2 up to
-// rounding, so the minimum is <= mu - am/2 + rounding < hi.
-__device__ __forceinline__ void compression_bounds(double c11, double c12, double c13, double c22, double c23,
-                                                   double c33, double& lo, double& hi) {
-  double trace = c11 + c22 + c33;
-  double mu = trace / 3.0;
-  double d11 = c11 - mu;
-  double d22 = c22 - mu;
-  double a = -(d11 * d11 + c12 * c12 + c13 * c13 + d11 * d22 + d22 * d22 + c23 * c23);
-  if (fabs(a) < 1.e-20) a = 1.e-20;
-  double am = 2.0 * sqrt(fabs(-a) / 3.0);
-  lo = mu - am;
-  hi = (mu - 0.49 * am) + 1e-14 * (fabs(mu) + am);
+// lies in [-am, am], so min_i (r_i + mu) >= mu - am = lo.  The root through
+// theta + 2pi/3 has cos <= -1/2, so the minimum is <= mu - am/2 < hi.  The
+// bounds come from FP32 arithmetic on the FP64 entries rounded once, widened
+// by 1e-5 (|mu| + am): FP32 rounding moves mu and am by a few 1e-7 of
+// |mu| + am, so lo stays below and hi above the FP64 formula's smallest
+// eigenvalue.  They only decide which cells may skip the exact FP64 test; the
+// cells that take it, and therefore every output, are unchanged.
+__device__ __forceinline__ void compression_bounds32(const double* c, double& lo, double& hi) {
+  const float c11 = (float)c[0], c12 = (float)c[1], c13 = (float)c[2], c22 = (float)c[3], c23 = (float)c[4],
+              c33 = (float)c[5];
+  const float mu = (c11 + c22 + c33) * (1.0f / 3.0f);
+  const float d11 = c11 - mu, d22 = c22 - mu;
+  const float a = d11 * d11 + c12 * c12 + c13 * c13 + d11 * d22 + d22 * d22 + c23 * c23;
+  const float am = 2.0f * sqrtf(fabsf(a) * (1.0f / 3.0f));
+  const float margin = 1e-5f * (fabsf(mu) + am) + 1e-30f;
+  lo = (double)(mu - am - margin);
+  hi = (double)((mu - 0.49f * am) + margin);
 }
 
 // Final compression test (limiter.f90:498-533): defplim = tlim where tlim > 0,
@@ -425,7 +428,7 @@ __global__ void __launch_bounds__(256) k_limiter_mask(double* __restrict__ defpl
 #undef P_
 #undef D_
     c[0] = 1.0 + phixx; c[1] = phixy; c[2] = phixz; c[3] = 1.0 + phiyy; c[4] = phiyz; c[5] = 1.0 + phizz;
-    compression_bounds(c[0], c[1], c[2], c[3], c[4], c[5], lo, hi);
+    compression_bounds32(c, lo, hi);
   }
   const bool pd = t < n3 && lo > 0.0;
   // smallest upper bound of the block's positive definite cells
@@ -669,7 +672,7 @@ __device__ __forceinline__ FF ff_div(FF a, FF b) {
 // reference's fallback (unit cofactors, det = 1).
 __global__ void __launch_bounds__(256) k_metric_ff(const double* __restrict__ def, const double* __restrict__ rho,
                                                    int n, double di2, float2* __restrict__ coef,
-                                                   float* __restrict__ coef32) {
+                                                   float* __restrict__ coef32, double* __restrict__ det_out) {
   const i64 n3 = (i64)n * n * n;
   const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n3) return;
@@ -697,6 +700,8 @@ __global__ void __launch_bounds__(256) k_metric_ff(const double* __restrict__ de
   b[4] = ff_sub(ff_mul(a12, a13), ff_mul(a11, a23));
   b[5] = ff_sub(ff_mul(a11, a22), ff_mul(a12, a12));
   FF det = ff_add(ff_add(ff_mul(a11, b[0]), ff_mul(a12, b[1])), ff_mul(a13, b[2]));
+  // det(A) itself (before the tangle fallback) for rgzerosum
+  if (det_out) det_out[t] = (double)det.hi + (double)det.lo;
   if (det.hi + det.lo <= 1.e-5f) {
     b[0] = one; b[1] = {0.0f, 0.0f}; b[2] = {0.0f, 0.0f}; b[3] = one; b[4] = {0.0f, 0.0f}; b[5] = one;
     det = one;
@@ -725,11 +730,11 @@ __global__ void __launch_bounds__(256) k_metric_ff(const double* __restrict__ de
 }
 
 void launch_metric_ff(const double* def, const double* rho, int n, double dx, double* coef, float* coef32,
-                      cudaStream_t s) {
+                      double* det, cudaStream_t s) {
   const i64 n3 = (i64)n * n * n;
   prof_begin(KK_METRIC, s, n3, n);
   k_metric_ff<<<grid_of(n3, kBlock), kBlock, 0, s>>>(def, rho, n, 1.0 / (dx * dx), reinterpret_cast<float2*>(coef),
-                                                     coef32);
+                                                     coef32, det);
   prof_end(KK_METRIC, s, n);
   count_launch();
 }

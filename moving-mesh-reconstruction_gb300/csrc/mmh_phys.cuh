@@ -51,6 +51,24 @@ __device__ __forceinline__ LimM lim_metric(const double* __restrict__ def, int n
   return m;
 }
 
+// The Hessian entries and det of lim_metric alone, by the same operations
+// (the same bits), without the cofactors and their divisions.
+__device__ __forceinline__ LimM lim_hess_det(const double* __restrict__ def, int n, int i, int j, int k) {
+  int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
+  LimM m;
+  double c = def[IDX(i, j, k, n)];
+  m.phixx = (def[IDX(ip, j, k, n)] - 2.0 * c + def[IDX(im, j, k, n)]);
+  m.phiyy = (def[IDX(i, jp, k, n)] - 2.0 * c + def[IDX(i, jm, k, n)]);
+  m.phizz = (def[IDX(i, j, kp, n)] - 2.0 * c + def[IDX(i, j, km, n)]);
+  m.phixy = (def[IDX(ip, jp, k, n)] - def[IDX(im, jp, k, n)] - def[IDX(ip, jm, k, n)] + def[IDX(im, jm, k, n)]) * 0.25;
+  m.phiyz = (def[IDX(i, jp, kp, n)] - def[IDX(i, jp, km, n)] - def[IDX(i, jm, kp, n)] + def[IDX(i, jm, km, n)]) * 0.25;
+  m.phixz = (def[IDX(ip, j, kp, n)] - def[IDX(im, j, kp, n)] - def[IDX(ip, j, km, n)] + def[IDX(im, j, km, n)]) * 0.25;
+  double a11 = 1.0 + m.phixx, a12 = m.phixy, a13 = m.phixz, a22 = 1.0 + m.phiyy, a23 = m.phiyz, a33 = 1.0 + m.phizz;
+  m.det = a11 * a22 * a33 + 2.0 * a12 * a13 * a23 - a13 * a13 * a22 - a11 * (a23 * a23) - a12 * a12 * a33;
+  m.b11 = m.b12 = m.b13 = m.b22 = m.b23 = m.b33 = 0.0;
+  return m;
+}
+
 // 1/(smallest eigenvalue) of the symmetric matrix C by the trigonometric
 // cubic-root formula (limiter.f90:346-358 and 459-471).
 __device__ __forceinline__ double compression_of(double c11, double c12, double c13, double c22, double c23,

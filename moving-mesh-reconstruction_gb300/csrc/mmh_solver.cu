@@ -169,9 +169,9 @@ int zerosum(mmh_ctx* c, T* a, i64 count) {
 }
 
 // rgzerosum(arr, def, dx) at level l (FP64)
-int rgzerosum(mmh_ctx* c, double* arr, const double* def, int n, double dx) {
+int rgzerosum(mmh_ctx* c, double* arr, const double* def, int n, double dx, bool have_det = false) {
   i64 n3 = (i64)n * n * n;
-  launch_det<double>(def, n, dx, c->det, c->s);
+  if (!have_det) launch_det<double>(def, n, dx, c->det, c->s);
   CK(cudaMemsetAsync(c->sc->acc[0], 0, 32, c->s));
   launch_fxsum<double>(c->det, n3, c->sc->acc[0], &c->sc->bad, c->s);
   launch_fxsum<double>(arr, n3, c->sc->acc[1], &c->sc->bad, c->s);
@@ -320,7 +320,7 @@ int build_levels(mmh_ctx* c, int l0) {
     // (a solve on the coarsest level itself keeps FP64 coefficients: its exact
     // coarse solve is formed from them)
     if (l == l0 && l0 < c->nlev - 1 && ff_outer(c)) {
-      launch_metric_ff(c->defl[l], c->rhol[l], n, double(1 << l), c->h64.coef[l], c->h32.coef[l], c->s);
+      launch_metric_ff(c->defl[l], c->rhol[l], n, double(1 << l), c->h64.coef[l], c->h32.coef[l], c->det, c->s);
       c->coef_ff = true;
       continue;
     }
@@ -581,10 +581,14 @@ int multigrid_level(mmh_ctx* c, int l0, double dx, mmh_diag* d) {
   int n = c->nl[l0];
   i64 n3 = (i64)n * n * n;
   CK(cudaMemsetAsync(c->sc, 0, offsetof(Scal, lim), c->s));
-  RET(rgzerosum(c, c->h64.rhs[l0], c->defl[l0], n, dx));
+  // The mixed form's float-float metric also gives det(A) for rgzerosum, so
+  // the metric goes first there (it does not depend on rhs or u).
+  const bool det_from_metric = ff_outer(c) && l0 < c->nlev - 1 && dx == double(1 << l0);
+  if (det_from_metric) RET(build_levels(c, l0));
+  RET(rgzerosum(c, c->h64.rhs[l0], c->defl[l0], n, dx, det_from_metric));
   RET(usum_zerosum<double>(c, c->h64.u[l0], n3));
   launch_absmax<double>(c->h64.rhs[l0], n3, &c->sc->rhsbits, c->s);
-  RET(build_levels(c, l0));
+  if (!det_from_metric) RET(build_levels(c, l0));
   int cycles = 0;
   double rn = 0.0, rel = 0.0;
   int status = MMH_OK;
