@@ -5,11 +5,12 @@ Workload (the headline configuration): a 512^3 periodic lognormal density
 (sigma_lnrho = 0.5, P(k) ~ k^-1.5, Gaussian-smoothed at 2 cells, seeded;
 larger sigma makes the reference algorithm itself unstable at this size),
 20 mesh-deformation iterations (calcdefp, def += defp, relaxing), every
-multigrid solve run to ||r||_inf / ||rhs||_inf <= 1e-8 with the residual in
-FP64, followed by the spectral displacement and density outputs.  One "step"
+multigrid solve run to ||r||_inf / ||rhs||_inf <= 1e-8 (the outer residual in
+float-float, about 48 significant bits), followed by the spectral
+displacement and density outputs.  One "step"
 is one such reconstruction; the metric is seconds per reconstruction.
 
-  value   : mixed form (FP32 V-cycles in an FP64 defect-correction loop), input
+  value   : mixed form (FP32 V-cycles in a float-float defect-correction loop), input
             density resident in HBM, CUDA events on the library's stream,
             kernel timing hooks off (the production configuration).
   e2e     : the same through the C ABI with host buffers: H2D of the density
@@ -284,13 +285,15 @@ def workload_config(args):
     return {
         "workload": f"{args.n}^3 lognormal density, sigma_lnrho={args.sigma}, P(k)~k^-1.5, smoothed at 2 cells, "
                     f"seed {args.seed}; {args.niter} deformation iterations; each multigrid solve by flexible CG "
-                    f"preconditioned with one V(2,2) cycle to ||r||inf/||rhs||inf<={args.tol:g} (FP64 residual); "
+                    f"preconditioned with one V(2,2) cycle to ||r||inf/||rhs||inf<={args.tol:g} (outer residual in "
+                    f"float-float, about 48 bits); "
                     f"spectral displacement and density outputs",
         "n": args.n, "iterations": args.niter, "tol": args.tol, "sigma_lnrho": args.sigma,
         "sigma_note": "sigma_lnrho=1.5 (and >=0.75) makes the reference algorithm itself unstable at 512^3 "
                       "(mesh increments of several cells per step in deep voids violate relaxing's CFL limit; "
                       "CPU restatement and GPU agree); 0.5 is the largest value stable for 20 iterations",
-        "precision": "mixed (FP32 V-cycle, FP64 residual/limiter/relaxing/FFT)",
+        "precision": "mixed (FP32 V-cycles and relaxing fluxes; float-float outer residual and finest metric; FP64 "
+                     "limiter decisions, relaxing update, exact 4^3 coarsest solve and FFTs)",
         "l2": "inputs larger than L2 (one 512^3 FP64 field is 1 GiB vs 129 MB L2)",
         "parallelism": f"replicas x{args.gpus}",
     }
