@@ -79,6 +79,8 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--seed", type=int, default=1000)
     ap.add_argument("--max-cycles", type=int, default=200)
+    ap.add_argument("--nu1", type=int, default=1, help="pre-smoothing sweeps of the preconditioner's V-cycle")
+    ap.add_argument("--nu2", type=int, default=1, help="post-smoothing sweeps")
     ap.add_argument("--fp64-steps", type=int, default=1, help="timed FP64 reconstructions (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-sample", default="auto", choices=["auto", "none"])
@@ -161,7 +163,7 @@ def _oracle_outputs_seconds(oracle, d):
     return time.perf_counter() - t
 
 
-def cpu_sample(n_full, niter, sigma, seed, tol, n_sample=256):
+def cpu_sample(n_full, niter, sigma, seed, tol, n_sample=256, nu=(1, 1)):
     """Time the oracle (FP64, tolerance schedule as the GPU runs it, 8-colour
     order, all host threads) on complete work: one whole deformation
     iteration (calcdefp with its solve run to tol, def += defp, relaxing) of
@@ -170,12 +172,12 @@ def cpu_sample(n_full, niter, sigma, seed, tol, n_sample=256):
     it is the path's full work for one iteration.  It is scaled to one
     n_full^3 reconstruction by the cell count (n_full/n_sample)^3 and by the
     niter iterations; the solves' iteration counts at n_full are within a few
-    of n_sample's (13 and 14 PCG iterations at 256^3 and 512^3)."""
+    of n_sample's."""
     import oracle
     import fields
     threads = oracle.threads(0)
     defpot, u = fields.initial_state(n_sample, sigma=sigma, seed=seed)
-    kw = dict(sched=oracle.SCHED_TOL, tol=tol, maxcyc=500, colour8=True)
+    kw = dict(sched=oracle.SCHED_TOL, tol=tol, maxcyc=500, colour8=True, nu1=nu[0], nu2=nu[1])
     t = time.perf_counter()
     d, _, _, _, diag = oracle.iteration(defpot, u, **kw)
     t_it = time.perf_counter() - t
@@ -232,7 +234,7 @@ def reference_arm(args):
     threads = oracle.threads(0)
     m = args.cpu_n or 256
     defpot, u = fields.initial_state(m, sigma=args.sigma, seed=args.seed)
-    kw = dict(sched=oracle.SCHED_TOL, tol=args.tol, maxcyc=500, colour8=True)
+    kw = dict(sched=oracle.SCHED_TOL, tol=args.tol, maxcyc=500, colour8=True, nu1=args.nu1, nu2=args.nu2)
     for _ in range(args.warmup):
         defpot, u, _, _, _ = oracle.iteration(defpot, u, **kw)
     times = []
@@ -285,7 +287,7 @@ def workload_config(args):
     return {
         "workload": f"{args.n}^3 lognormal density, sigma_lnrho={args.sigma}, P(k)~k^-1.5, smoothed at 2 cells, "
                     f"seed {args.seed}; {args.niter} deformation iterations; each multigrid solve by flexible CG "
-                    f"preconditioned with one V(2,2) cycle to ||r||inf/||rhs||inf<={args.tol:g} (outer residual in "
+                    f"preconditioned with one V({args.nu1},{args.nu2}) cycle to ||r||inf/||rhs||inf<={args.tol:g} (outer residual in "
                     f"float-float, about 48 bits); "
                     f"spectral displacement and density outputs",
         "n": args.n, "iterations": args.niter, "tol": args.tol, "sigma_lnrho": args.sigma,
@@ -340,7 +342,8 @@ def batch_arm(args):
     rhos = [fields.lognormal_density(n, sigma=float(rng.uniform(0.4, 0.7)), ns=float(rng.uniform(-2.0, -1.0)),
                                      seed=args.seed + i) for i, n in enumerate(sizes)]
     cells = sum(n ** 3 for n in sizes) * args.batch_niter
-    kw = dict(precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL, tol=args.tol, max_cycles=args.max_cycles)
+    kw = dict(precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL, tol=args.tol, max_cycles=args.max_cycles,
+              nu1=args.nu1, nu2=args.nu2)
     mmh.batch_run(rhos[:3] + rhos[32:35] + rhos[64:67], 1, workers=args.batch_workers, **kw)  # warm-up
     res = {}
     for label, w in (("batch", args.batch_workers), ("loop", 1)):
@@ -391,7 +394,7 @@ def adjoint_arm(args):
         if name == "fp64" and args.fp64_steps <= 0:
             continue
         with mmh.Context(n, precision=prec, schedule=mmh.MMH_SCHED_TOL, tol=args.adj_tol,
-                         max_cycles=args.max_cycles) as ctx:
+                         max_cycles=args.max_cycles, nu1=args.nu1, nu2=args.nu2) as ctx:
             def forward():
                 ctx.load(z, u)
                 ctx.iterate(niter)
@@ -470,7 +473,8 @@ def main():
 
     def make_ctx(precision):
         return mmh.Context(n, precision=precision, schedule=mmh.MMH_SCHED_TOL, tol=args.tol,
-                           max_cycles=args.max_cycles, device=local, stream=stream.cuda_stream)
+                           max_cycles=args.max_cycles, nu1=args.nu1, nu2=args.nu2, device=local,
+                           stream=stream.cuda_stream)
 
     def recon(ctx):
         ctx.load_dev(None, rho_dev.data_ptr())
@@ -620,7 +624,7 @@ def main():
 
     cpu = None
     if args.cpu_sample != "none" and not dist:
-        cpu = cpu_sample(n, args.niter, args.sigma, args.seed, args.tol, n_sample=args.cpu_n)
+        cpu = cpu_sample(n, args.niter, args.sigma, args.seed, args.tol, n_sample=args.cpu_n, nu=(args.nu1, args.nu2))
         cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "reference_schedule_fp32")}
 
     value = ms_mixed / 1000.0 / world  # whole-job seconds per reconstruction (replicas)

@@ -40,7 +40,9 @@ extern "C" {
 
 /* precision forms */
 #define MMH_FP64 0  /* everything in FP64 (bit-identical to the CPU restatement) */
-#define MMH_MIXED 1 /* FP32 inner V-cycles inside an FP64 defect-correction loop */
+#define MMH_MIXED 1 /* FP32 inner V-cycles inside a defect-correction loop whose residual is
+                       float-float (MMH_SCHED_TOL with tol >= 1e-10) or FP64 (otherwise);
+                       relaxing with FP32 fluxes and an FP64 update */
 
 /* multigrid schedules */
 #define MMH_SCHED_REF 0    /* reference: one V-cycle, 4*NG/n sweeps per level (mgtemplate.f90) */
@@ -140,6 +142,12 @@ int mmh_relax_f64(mmh_ctx* ctx, double* arr, double* resid, const double* rhs, c
                   const double* rho, double* rinf, double dx, int n, int nrelax, int iopt);
 /* cbajraw for every plane: coef(n,n,n,6) = rho_bar*cof(A)/det    gauss1.f90:1027 */
 int mmh_metric_f64(mmh_ctx* ctx, const double* deformpot, const double* rho, double dx, int n, double* coef);
+/* The mixed form's float-float metric (the coefficients of its outer
+ * residual, about 48 significant bits): coef(n,n,n,6) as hi + lo rounded to
+ * FP64, det(n,n,n) (may be NULL) = det(A) before the tangle fallback.  dx a
+ * power of two; an MMH_MIXED context only (else MMH_ERR_UNSUPPORTED). */
+int mmh_metric_ff_f64(mmh_ctx* ctx, const double* deformpot, const double* rho, double dx, int n, double* coef,
+                      double* det);
 int mmh_restrict_f64(mmh_ctx* ctx, const double* u, int n, double* uhalf);       /* mgutil.f90:74 */
 int mmh_inject_f64(mmh_ctx* ctx, double* u, const double* uhalf, int n);         /* mgutil.f90:38 */
 int mmh_zerosum_f64(mmh_ctx* ctx, double* arr, int n);                           /* gauss1.f90:1420 */

@@ -75,7 +75,7 @@ void launch_coarse_apply(const float* r, const double* M, float* z, cudaStream_t
 
 // limiter / spectral / relaxing (FP64)
 struct LimDev;
-void launch_calcdefp_rhs(double* tmp, const double* rho, int n, double dtold, cudaStream_t s);
+void launch_calcdefp_rhs(double* tmp, const double* rho, int n, double dtold, bool mixed, cudaStream_t s);
 void launch_limiter_pass1(double* tmp, const double* def, const double* rho, int n, double dtold, double dtaumesh,
                           LimDev* st, uint8_t* maskx, uint8_t* maskc, cudaStream_t s);
 void launch_limiter_mask(double* defplim, const double* def, const double* defp, int n, double dtold, LimDev* st,

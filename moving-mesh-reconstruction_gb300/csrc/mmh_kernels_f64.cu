@@ -5,6 +5,7 @@
 #include <atomic>
 #include <vector>
 
+#include "mmh_ff.cuh"
 #include "mmh_launch.cuh"
 #include "mmh_pcg.cuh"
 #include "mmh_phys.cuh"
@@ -251,17 +252,25 @@ void launch_add(double* a, const double* b, i64 count, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // calcdefp right-hand side and limiter
 // ---------------------------------------------------------------------------
-__global__ void k_calcdefp_rhs(double* __restrict__ tmp, const double* __restrict__ rho, i64 n3, double dtold) {
+// tmp = clamp(1 - rho, +-2) / 30 / dtold (limiter.f90:153-166).  The mixed
+// form multiplies by 1 / (30 dtold) instead of dividing twice (an FP64
+// division is some ten FP64-pipe operations): within 2 ulp.
+template <bool MIXED>
+__global__ void k_calcdefp_rhs(double* __restrict__ tmp, const double* __restrict__ rho, i64 n3, double dtold,
+                               double rcp) {
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n3) return;
   double t1 = 1.0 - rho[t];
   const double xhigh = 2.0;
   if (fabs(t1) > xhigh) t1 = t1 >= 0.0 ? xhigh : -xhigh;
-  tmp[t] = t1 / 30.0 / dtold;
+  tmp[t] = MIXED ? t1 * rcp : t1 / 30.0 / dtold;
 }
-void launch_calcdefp_rhs(double* tmp, const double* rho, int n, double dtold, cudaStream_t s) {
+void launch_calcdefp_rhs(double* tmp, const double* rho, int n, double dtold, bool mixed, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
-  k_calcdefp_rhs<<<grid_of(n3, kBlock), kBlock, 0, s>>>(tmp, rho, n3, dtold);
+  if (mixed)
+    k_calcdefp_rhs<true><<<grid_of(n3, kBlock), kBlock, 0, s>>>(tmp, rho, n3, dtold, 1.0 / (30.0 * dtold));
+  else
+    k_calcdefp_rhs<false><<<grid_of(n3, kBlock), kBlock, 0, s>>>(tmp, rho, n3, dtold, 0.0);
   count_launch();
 }
 
@@ -608,70 +617,29 @@ void launch_power_bins(const void* A, const void* B, int n, int nb, const double
 }
 
 // ---------------------------------------------------------------------------
-// Float-float residual of the mixed form's outer loop.  A value is the
-// unevaluated sum hi + lo of two floats (|lo| <= ulp(hi)/2), about 48
-// significant bits; sums and products use the error-free transformations of
-// Knuth (TwoSum) and Dekker (TwoProduct, here with one fused multiply-add),
-// as in the double-double literature (Dekker 1971; Hida, Li and Bailey 2001).
-// This translation unit is compiled without FMA contraction, which the
-// transformations rely on.  The residual is formed from neighbour
-// differences, r = rhs - sum_f b_f (phi_nb - phi_c) - cross terms, so its
-// terms are ~ n/(2 pi) |rhs| and its error ~ 1e-12 |rhs| -- far below the
-// outer loop's tolerance -- while every product and sum runs on the FP32
-// pipes (the FP64 form of this kernel is bound by the FP64 rate).
+// Float-float kernels of the mixed form (arithmetic in mmh_ff.cuh).  The
+// outer residual is formed from neighbour differences, r = rhs - sum_f b_f
+// (phi_nb - phi_c) - cross terms, so its terms are ~ n/(2 pi) |rhs| and its
+// error ~ 1e-12 |rhs| -- far below the outer loop's tolerance -- while every
+// product and sum runs on the FP32 pipes (the FP64 form of this kernel is
+// bound by the FP64 rate).
 // ---------------------------------------------------------------------------
-struct FF {
-  float hi, lo;
-};
-__device__ __forceinline__ FF ff_two_sum(float a, float b) {
-  float s = a + b;
-  float bb = s - a;
-  float e = (a - (s - bb)) + (b - bb);
-  return {s, e};
-}
-__device__ __forceinline__ FF ff_quick(float a, float b) {  // |a| >= |b| or a == 0
-  float s = a + b;
-  return {s, b - (s - a)};
-}
-__device__ __forceinline__ FF ff_add(FF a, FF b) {
-  FF s = ff_two_sum(a.hi, b.hi), t = ff_two_sum(a.lo, b.lo);
-  s.lo = s.lo + t.hi;
-  s = ff_quick(s.hi, s.lo);
-  s.lo = s.lo + t.lo;
-  return ff_quick(s.hi, s.lo);
-}
-__device__ __forceinline__ FF ff_neg(FF a) { return {-a.hi, -a.lo}; }
-__device__ __forceinline__ FF ff_sub(FF a, FF b) { return ff_add(a, ff_neg(b)); }
-__device__ __forceinline__ FF ff_mul(FF a, FF b) {
-  float p = a.hi * b.hi;
-  float e = fmaf(a.hi, b.hi, -p);
-  e = fmaf(a.hi, b.lo, e);
-  e = fmaf(a.lo, b.hi, e);
-  return ff_quick(p, e);
-}
-__device__ __forceinline__ FF ff_scale(FF a, float p2) { return {a.hi * p2, a.lo * p2}; }  // p2 a power of two
-__device__ __forceinline__ FF ff_of(double x) {
-  float h = (float)x;
-  return {h, (float)(x - (double)h)};
-}
-
-__device__ __forceinline__ FF ff_div(FF a, FF b) {
-  const float q1 = a.hi / b.hi;
-  const FF r = ff_sub(a, ff_mul({q1, 0.0f}, b));
-  return ff_quick(q1, r.hi / b.hi);
-}
-
 // The mixed form's finest-level metric (cbajraw, gauss1.f90:1107-1210) in
 // float-float, for the outer residual: rho_bar * cof(A) / det as (hi, lo)
 // pairs in `coef` (six planes of n^3 pairs, the layout k_ff_split makes) and
-// the hi parts, the FP32 V-cycle's coefficients, in coef32.  The Hessian of
-// def and the 27-cell density sum are formed in FP64 as in k_metric (their
-// operands are far larger than the results); A, its cofactors and
-// determinant, rho_bar / det and the six products in float-float (about 48
-// significant bits, all on the FP32 pipes).  det <= 1e-5 takes the
-// reference's fallback (unit cofactors, det = 1).
+// the hi parts, the FP32 V-cycle's coefficients, in coef32.  Every input is
+// split into a float-float pair from its bit pattern (ff_of_bits), and the
+// whole metric runs on the FP32 and integer pipes: the Hessian of def from
+// neighbour differences (ff_diff), A, its cofactors and determinant,
+// rho_bar / det and the six products in float-float, the 27-cell density sum
+// by compensated summation (TwoSum of the high parts, Ogita-Rump-Oishi Sum2;
+// the densities are non-negative, so its error is ~2^-48 of the sum).  A
+// pair holds its double to 2^-48, so a Hessian entry carries ~2^-46 max|def|
+// / dx^2 and the coefficients about 48 significant bits otherwise.  det <=
+// 1e-5 takes the reference's fallback (unit cofactors, det = 1).  di2 =
+// 1/dx^2 is a power of two.
 __global__ void __launch_bounds__(256) k_metric_ff(const double* __restrict__ def, const double* __restrict__ rho,
-                                                   int n, double di2, float2* __restrict__ coef,
+                                                   int n, float di2, float2* __restrict__ coef,
                                                    float* __restrict__ coef32, double* __restrict__ det_out) {
   const i64 n3 = (i64)n * n * n;
   const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
@@ -679,19 +647,19 @@ __global__ void __launch_bounds__(256) k_metric_ff(const double* __restrict__ de
   int i, j, k;
   cell_of(t, n, i, j, k);
   const int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
-  const double c = def[t];
-  const double pxx = (def[IDX(ip, j, k, n)] - 2.0 * c + def[IDX(im, j, k, n)]) * di2;
-  const double pyy = (def[IDX(i, jp, k, n)] - 2.0 * c + def[IDX(i, jm, k, n)]) * di2;
-  const double pzz = (def[IDX(i, j, kp, n)] - 2.0 * c + def[IDX(i, j, km, n)]) * di2;
-  const double pxy =
-      (def[IDX(ip, jp, k, n)] - def[IDX(im, jp, k, n)] - def[IDX(ip, jm, k, n)] + def[IDX(im, jm, k, n)]) * di2 * 0.25;
-  const double pyz =
-      (def[IDX(i, jp, kp, n)] - def[IDX(i, jp, km, n)] - def[IDX(i, jm, kp, n)] + def[IDX(i, jm, km, n)]) * di2 * 0.25;
-  const double pxz =
-      (def[IDX(ip, j, kp, n)] - def[IDX(im, j, kp, n)] - def[IDX(ip, j, km, n)] + def[IDX(im, j, km, n)]) * di2 * 0.25;
+#define D_(x, y, z) ff_of_bits(def[IDX(x, y, z, n)])
+  const FF c = ff_of_bits(def[t]);
+  const FF pxx = ff_scale(ff_add(ff_diff(D_(ip, j, k), c), ff_diff(D_(im, j, k), c)), di2);
+  const FF pyy = ff_scale(ff_add(ff_diff(D_(i, jp, k), c), ff_diff(D_(i, jm, k), c)), di2);
+  const FF pzz = ff_scale(ff_add(ff_diff(D_(i, j, kp), c), ff_diff(D_(i, j, km), c)), di2);
+  const float q = 0.25f * di2;
+  const FF pxy = ff_scale(ff_sub(ff_diff(D_(ip, jp, k), D_(im, jp, k)), ff_diff(D_(ip, jm, k), D_(im, jm, k))), q);
+  const FF pyz = ff_scale(ff_sub(ff_diff(D_(i, jp, kp), D_(i, jp, km)), ff_diff(D_(i, jm, kp), D_(i, jm, km))), q);
+  const FF pxz = ff_scale(ff_sub(ff_diff(D_(ip, j, kp), D_(im, j, kp)), ff_diff(D_(ip, j, km), D_(im, j, km))), q);
+#undef D_
   const FF one = {1.0f, 0.0f};
-  const FF a11 = ff_add(one, ff_of(pxx)), a22 = ff_add(one, ff_of(pyy)), a33 = ff_add(one, ff_of(pzz));
-  const FF a12 = ff_of(pxy), a13 = ff_of(pxz), a23 = ff_of(pyz);
+  const FF a11 = ff_add(one, pxx), a22 = ff_add(one, pyy), a33 = ff_add(one, pzz);
+  const FF a12 = pxy, a13 = pxz, a23 = pyz;
   FF b[6];
   b[0] = ff_sub(ff_mul(a22, a33), ff_mul(a23, a23));
   b[1] = ff_sub(ff_mul(a13, a23), ff_mul(a12, a33));
@@ -707,20 +675,23 @@ __global__ void __launch_bounds__(256) k_metric_ff(const double* __restrict__ de
     det = one;
   }
   const int is[3] = {im, i, ip}, js[3] = {jm, j, jp}, ks[3] = {km, k, kp};
-  double urg = rho[IDX(im, jm, km, n)];
+  float sh = 0.0f, se = 0.0f;
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int bb = 0; bb < 3; ++bb)
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        if (a == 0 && bb == 0 && d == 0) continue;
-        urg = urg + rho[IDX(is[a], js[bb], ks[d], n)];
+        const FF v = ff_of_bits(rho[IDX(is[a], js[bb], ks[d], n)]);
+        const FF s2 = ff_two_sum(sh, v.hi);
+        sh = s2.hi;
+        se = se + (s2.lo + v.lo);
       }
+  const FF urg = ff_quick(sh, se);
   // 1/27 as a float-float constant
   const double r27 = 1.0 / 27.0;
   const float r27h = (float)r27;
-  const FF w = ff_div(ff_mul(ff_of(urg), {r27h, (float)(r27 - (double)r27h)}), det);
+  const FF w = ff_div(ff_mul(urg, {r27h, (float)(r27 - (double)r27h)}), det);
 #pragma unroll
   for (int f = 0; f < 6; ++f) {
     const FF cf = ff_mul(w, b[f]);
@@ -733,7 +704,7 @@ void launch_metric_ff(const double* def, const double* rho, int n, double dx, do
                       double* det, cudaStream_t s) {
   const i64 n3 = (i64)n * n * n;
   prof_begin(KK_METRIC, s, n3, n);
-  k_metric_ff<<<grid_of(n3, kBlock), kBlock, 0, s>>>(def, rho, n, 1.0 / (dx * dx), reinterpret_cast<float2*>(coef),
+  k_metric_ff<<<grid_of(n3, kBlock), kBlock, 0, s>>>(def, rho, n, (float)(1.0 / (dx * dx)), reinterpret_cast<float2*>(coef),
                                                      coef32, det);
   prof_end(KK_METRIC, s, n);
   count_launch();
@@ -743,7 +714,7 @@ void launch_metric_ff(const double* def, const double* rho, int n, double dx, do
 __global__ void k_ff_split(double* __restrict__ a, i64 count) {
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= count) return;
-  FF v = ff_of(a[t]);
+  FF v = ff_of_bits(a[t]);
   reinterpret_cast<float2*>(a)[t] = make_float2(v.hi, v.lo);
 }
 __global__ void k_ff_join(double* __restrict__ a, i64 count) {
@@ -764,19 +735,19 @@ __global__ void k_ff_sub_mean(float2* __restrict__ x, const double* __restrict__
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= count) return;
   float2 v = x[t];
-  FF r = ff_sub({v.x, v.y}, ff_of(*mean));
+  FF r = ff_sub({v.x, v.y}, ff_of_bits(*mean));
   x[t] = make_float2(r.hi, r.lo);
 }
 
 // r = rhs - L[phi] * di2 in float-float: phi and the six coefficient planes
 // as (hi, lo) pairs, rhs in FP64; r32 (may be null) = r rounded to float,
-// max |r| into maxbits.
+// max |r| into maxbits (from the high parts: within 2^-24 of itself).
 __global__ void __launch_bounds__(256) k_residual_ff(const float2* __restrict__ phi, const double* __restrict__ rhs,
                                                      const float2* __restrict__ coef, int n, float di2,
                                                      float* __restrict__ r32, unsigned long long* maxbits) {
   const i64 n3 = (i64)n * n * n;
   const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  double m = 0.0;
+  float m = 0.0f;
   if (t < n3) {
     int i, j, k;
     cell_of(t, n, i, j, k);
@@ -815,9 +786,9 @@ __global__ void __launch_bounds__(256) k_residual_ff(const float2* __restrict__ 
     x = ff_add(x, ff_mul(ff_sub(ipkp, ipkm), C(2, ip, j, k)));
     x = ff_sub(x, ff_mul(ff_sub(imkp, imkm), C(2, im, j, k)));
     L = ff_add(L, ff_scale(x, 0.25f));
-    const FF r = ff_sub(ff_of(rhs[t]), ff_scale(L, di2));
+    const FF r = ff_sub(ff_of_bits(rhs[t]), ff_scale(L, di2));
     if (r32) r32[t] = r.hi;
-    m = fabs((double)r.hi + (double)r.lo);
+    m = fabsf(r.hi);
   }
   if (maxbits) block_max_commit(m, maxbits);
 }
@@ -850,8 +821,12 @@ void launch_residual_ff(const double* phi, const double* rhs, const double* coef
 }
 
 // One axis of the smoother [1/4, 1/2, 1/4] (the 27-point nsmooth of
-// limiter.f90:677-781 is its product over the three axes), periodic:
-// out = (in(-1) + in(+1)) / 4 + in / 2.
+// limiter.f90:677-781 is its product over the three axes), periodic, as a
+// pass without its weights: out = in[-1] + in[+1] + 2 in (one add and one fused multiply-add; 2 in is exact).  The
+// last pass applies the three passes' weights, 1/64, at once.  Scaling by a
+// power of two is exact and commutes with rounding, so the result has the
+// bits of three passes of (in[-1] + in[+1]) / 4 + in / 2.
+template <bool LAST>
 __global__ void k_smooth_axis(const double* __restrict__ in, int n, int axis, double* __restrict__ out) {
   const i64 n3 = (i64)n * n * n;
   const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
@@ -861,16 +836,17 @@ __global__ void k_smooth_axis(const double* __restrict__ in, int n, int axis, do
   const i64 stride = axis == 0 ? 1 : (axis == 1 ? (i64)n : (i64)n * n);
   const i64 lo = c[axis] == 0 ? t + (i64)(n - 1) * stride : t - stride;
   const i64 hi = c[axis] == n - 1 ? t - (i64)(n - 1) * stride : t + stride;
-  out[t] = (in[lo] + in[hi]) * 0.25 + in[t] * 0.5;
+  const double v = __fma_rn(2.0, in[t], in[lo] + in[hi]);
+  out[t] = LAST ? v * 0.015625 : v;
 }
 // The 27-point smoother as three axis passes (the mixed form's nsmooth:
 // the same operator, other rounding): in -> out -> in -> out; in is
 // overwritten.
 void launch_smooth_sep(double* in, int n, double* out, cudaStream_t s) {
   const i64 n3 = (i64)n * n * n;
-  k_smooth_axis<<<grid_of(n3, kBlock), kBlock, 0, s>>>(in, n, 0, out);
-  k_smooth_axis<<<grid_of(n3, kBlock), kBlock, 0, s>>>(out, n, 1, in);
-  k_smooth_axis<<<grid_of(n3, kBlock), kBlock, 0, s>>>(in, n, 2, out);
+  k_smooth_axis<false><<<grid_of(n3, kBlock), kBlock, 0, s>>>(in, n, 0, out);
+  k_smooth_axis<false><<<grid_of(n3, kBlock), kBlock, 0, s>>>(out, n, 1, in);
+  k_smooth_axis<true><<<grid_of(n3, kBlock), kBlock, 0, s>>>(in, n, 2, out);
   count_launch(3);
 }
 

@@ -13,14 +13,16 @@
 // c and the metric from the pre-step state in both stages.
 //
 // Precision: the second differences of def and the central differences of
-// defp are formed in FP64 (their operands are O(n) larger than the
-// differences) and rounded once to FP32; the metric, speeds, flux ratios and
+// defp are formed from float-float splits of the FP64 samples (their operands
+// are O(n) larger than the differences; the splits keep 48 bits) and rounded
+// once to FP32; the metric, speeds, flux ratios and
 // face fluxes are FP32; u' = u - dt R is formed in FP64.  R is small against u
 // (a few per cent per step), so the FP32 rounding of R moves u by ~1e-8 of
 // itself per step.  Cells where the reference's state is degenerate (zero or
 // non-finite density or det) get a NaN speed, as the reference's 0/0 does.
 #include <cuda_runtime.h>
 
+#include "mmh_ff.cuh"
 #include "mmh_kernels.cuh"
 
 namespace mmh {
@@ -60,31 +62,38 @@ __global__ void __launch_bounds__(256) k_relax32_geom(const double* __restrict__
   int i, j, k;
   cell_of(t, n, i, j, k);
   const int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
-  const double c0 = def[t];
-  const float pxx = (float)(def[IDX(ip, j, k, n)] - 2.0 * c0 + def[IDX(im, j, k, n)]);
-  const float pyy = (float)(def[IDX(i, jp, k, n)] - 2.0 * c0 + def[IDX(i, jm, k, n)]);
-  const float pzz = (float)(def[IDX(i, j, kp, n)] - 2.0 * c0 + def[IDX(i, j, km, n)]);
-  const float pxy = (float)((def[IDX(ip, jp, k, n)] - def[IDX(im, jp, k, n)]) -
-                            (def[IDX(ip, jm, k, n)] - def[IDX(im, jm, k, n)])) * 0.25f;
-  const float pyz = (float)((def[IDX(i, jp, kp, n)] - def[IDX(i, jp, km, n)]) -
-                            (def[IDX(i, jm, kp, n)] - def[IDX(i, jm, km, n)])) * 0.25f;
-  const float pxz = (float)((def[IDX(ip, j, kp, n)] - def[IDX(im, j, kp, n)]) -
-                            (def[IDX(ip, j, km, n)] - def[IDX(im, j, km, n)])) * 0.25f;
+  // second differences of def and central differences of defp from
+  // float-float splits of the samples (integer and FP32 operations; FP64
+  // runs at two operations per clock per SM on GB300), rounded once to FP32
+#define D_(x, y, z) ff_of_bits(def[IDX(x, y, z, n)])
+  const FF c0 = ff_of_bits(def[t]);
+  const float pxx = ff_sum_f(ff_diff(D_(ip, j, k), c0), ff_diff(D_(im, j, k), c0));
+  const float pyy = ff_sum_f(ff_diff(D_(i, jp, k), c0), ff_diff(D_(i, jm, k), c0));
+  const float pzz = ff_sum_f(ff_diff(D_(i, j, kp), c0), ff_diff(D_(i, j, km), c0));
+  const float pxy = ff_sum_f(ff_diff(D_(ip, jp, k), D_(im, jp, k)), ff_neg(ff_diff(D_(ip, jm, k), D_(im, jm, k)))) * 0.25f;
+  const float pyz = ff_sum_f(ff_diff(D_(i, jp, kp), D_(i, jp, km)), ff_neg(ff_diff(D_(i, jm, kp), D_(i, jm, km)))) * 0.25f;
+  const float pxz = ff_sum_f(ff_diff(D_(ip, j, kp), D_(im, j, kp)), ff_neg(ff_diff(D_(ip, j, km), D_(im, j, km)))) * 0.25f;
+#undef D_
   const float a11 = 1.f + pxx, a12 = pxy, a13 = pxz, a22 = 1.f + pyy, a23 = pyz, a33 = 1.f + pzz;
   const float b11 = a22 * a33 - a23 * a23, b12 = a13 * a23 - a12 * a33, b13 = a12 * a23 - a13 * a22;
   const float b22 = a11 * a33 - a13 * a13, b23 = a12 * a13 - a11 * a23, b33 = a11 * a22 - a12 * a12;
   const float det = a11 * b11 + a12 * b12 + a13 * b13;
-  // -grad defp (central differences in FP64)
-  const float gx = (float)((defp[IDX(im, j, k, n)] - defp[IDX(ip, j, k, n)]) * 0.5);
-  const float gy = (float)((defp[IDX(i, jm, k, n)] - defp[IDX(i, jp, k, n)]) * 0.5);
-  const float gz = (float)((defp[IDX(i, j, km, n)] - defp[IDX(i, j, kp, n)]) * 0.5);
+  // -grad defp (central differences)
+#define P_(x, y, z) ff_of_bits(defp[IDX(x, y, z, n)])
+  const float gx = ff_diff_f(P_(im, j, k), P_(ip, j, k)) * 0.5f;
+  const float gy = ff_diff_f(P_(i, jm, k), P_(i, jp, k)) * 0.5f;
+  const float gz = ff_diff_f(P_(i, j, km), P_(i, j, kp)) * 0.5f;
+#undef P_
   const float rd = 1.f / det;
   const float v1 = (b11 * gx + b12 * gy + b13 * gz) * rd;
   const float v2 = (b12 * gx + b22 * gy + b23 * gz) * rd;
   const float v3 = (b13 * gx + b23 * gy + b33 * gz) * rd;
   const double u0 = rho[t];
   float c = rmax(rmax(fabsf(v1), fabsf(v2)), fabsf(v3));
-  const bool sound = u0 != 0.0 && isfinite(u0) && det != 0.f && isfinite(det);
+  // u0 != 0 and finite, from its bits
+  const unsigned long long ub = (unsigned long long)__double_as_longlong(u0);
+  const bool u_ok = (ub << 1) != 0ull && ((ub >> 52) & 0x7ffull) != 0x7ffull;
+  const bool sound = u_ok && det != 0.f && isfinite(det);
   if (!sound) c = __int_as_float(0x7fffffff);  // NaN
   const float rc = 1.f / c;
   geo[t] = make_float4(v1 * rc, v2 * rc, v3 * rc, c);

@@ -739,7 +739,7 @@ int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t
   if (dtold < 1.e-8) dtold = 1.0;
   double* tmp = c->tmp();
   double* defp = c->defp();
-  launch_calcdefp_rhs(tmp, c->rho, n, dtold, c->s);
+  launch_calcdefp_rhs(tmp, c->rho, n, dtold, c->cfg.precision == MMH_MIXED, c->s);
   smooth_step(c, tmp, c->scr);
   smooth_step(c, c->scr, tmp);
   smooth_step(c, tmp, c->scr);
@@ -825,7 +825,7 @@ int calcdefp_fwd_keep(mmh_ctx* c, double dtold, double dtaumesh, const CalcKeep&
   if (dtold < 1.e-8) dtold = 1.0;
   double* tmp = c->tmp();
   double* defp = c->defp();
-  launch_calcdefp_rhs(tmp, c->rho, n, dtold, c->s);
+  launch_calcdefp_rhs(tmp, c->rho, n, dtold, c->cfg.precision == MMH_MIXED, c->s);
   smooth_step(c, tmp, c->scr);
   smooth_step(c, c->scr, tmp);
   smooth_step(c, tmp, c->scr);
@@ -1740,6 +1740,23 @@ int mmh_metric_f64(mmh_ctx* c, const double* deformpot, const double* rho, doubl
   RET(upload(c, rho, c->rhol[l], n3));
   // the context's form: the reference's six divisions (FP64) or one (mixed)
   launch_metric<double>(c->defl[l], c->rhol[l], n, dx, c->h64.coef[l], c->s, c->cfg.precision == MMH_MIXED);
+  return download(c, c->h64.coef[l], coef, 6 * n3);
+}
+
+int mmh_metric_ff_f64(mmh_ctx* c, const double* deformpot, const double* rho, double dx, int n, double* coef,
+                      double* det) {
+  if (!c || !deformpot || !rho || !coef) return MMH_ERR_ARG;
+  if (c->cfg.precision != MMH_MIXED) return MMH_ERR_UNSUPPORTED;
+  RET(check_cube(c, n, n, n));
+  if (n < 4 || dx <= 0.0 || std::ldexp(1.0, std::ilogb(dx)) != dx) return MMH_ERR_ARG;
+  int l = ilog2(c->n / n);
+  i64 n3 = (i64)n * n * n;
+  RET(upload(c, deformpot, c->defl[l], n3));
+  RET(upload(c, rho, c->rhol[l], n3));
+  launch_metric_ff(c->defl[l], c->rhol[l], n, dx, c->h64.coef[l], c->h32.coef[l], det ? c->det : nullptr, c->s);
+  launch_ff_join(c->h64.coef[l], 6 * n3, c->s);
+  c->coef_ff = false;
+  if (det) RET(download(c, c->det, det, n3));
   return download(c, c->h64.coef[l], coef, 6 * n3);
 }
 

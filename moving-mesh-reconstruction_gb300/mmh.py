@@ -37,7 +37,7 @@ EXPORTS = (
     "mmh_config_default", "mmh_create", "mmh_destroy", "mmh_strerror", "mmh_sync", "mmh_launch_count",
     "mmh_calcdefp", "mmh_calcdefp_f64", "mmh_multigrid", "mmh_multigrid_f64", "mmh_relaxing", "mmh_relaxing_f64",
     "mmh_scalar2gradient", "mmh_scalar2gradient_f64", "mmh_defp2delta", "mmh_defp2delta_f64",
-    "mmh_relax_f64", "mmh_metric_f64", "mmh_restrict_f64", "mmh_inject_f64", "mmh_zerosum_f64",
+    "mmh_relax_f64", "mmh_metric_f64", "mmh_metric_ff_f64", "mmh_restrict_f64", "mmh_inject_f64", "mmh_zerosum_f64",
     "mmh_rgzerosum_f64", "mmh_nsmooth_f64", "mmh_limiter_pass1_f64", "mmh_limiter_mask_f64",
     "mmh_limiter_poisson_f64", "mmh_load_f64", "mmh_load_dev", "mmh_iterate", "mmh_store_f64",
     "mmh_outputs_f64", "mmh_outputs_dev", "mmh_state_dev", "mmh_profile_start", "mmh_profile_stop",
@@ -368,6 +368,15 @@ class Context:
         _chk(lib().mmh_metric_f64(self._h, _p(_farr(deformpot, np.float64)), _p(_farr(rho, np.float64)),
                                   C.c_double(dx), n, _p(coef)), "metric")
         return coef
+
+    def metric_ff(self, deformpot, rho, dx=1.0):
+        """The mixed form's float-float metric (mmh_metric_ff_f64): (coef, det)."""
+        n = deformpot.shape[0]
+        coef = np.zeros((n, n, n, 6), dtype=np.float64, order="F")
+        det = np.zeros((n, n, n), dtype=np.float64, order="F")
+        _chk(lib().mmh_metric_ff_f64(self._h, _p(_farr(deformpot, np.float64)), _p(_farr(rho, np.float64)),
+                                     C.c_double(dx), n, _p(coef), _p(det)), "metric_ff")
+        return coef, det
 
     def restrict(self, u):
         n = u.shape[0]

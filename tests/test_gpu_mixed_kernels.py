@@ -10,6 +10,8 @@ runs in that form, which are not bit-matched to the reference:
   update in FP64: the density within 5e-8 relative after one step (an FP32
   restatement in numpy gives 6e-9 at 32^3 for a step that moves the density
   by 0.2).
+* the float-float metric of the outer residual (k_metric_ff) within
+  1e-13 + 2^-44 max|def| of the largest coefficient.
 The float-float outer residual (k_residual_ff) is checked against an FP64
 recomputation in test_gpu_parity.py::test_multigrid_mixed_float_float_outer_loop.
 """
@@ -32,6 +34,49 @@ def test_mixed_metric_one_division(mmh, oracle, fields, n):
             g = ctx.metric(defpot, rho, dx)
             o = oracle.metric(defpot, rho, dx)
             assert np.all(np.abs(g - o) <= 4 * EPS * np.abs(o)), np.abs(g - o).max()
+
+
+def _det_numpy(defpot, dx):
+    """det(I + Hess(def)) with the reference's central differences, FP64 numpy."""
+    d = defpot
+    r = lambda a, s, ax: np.roll(a, -s, axis=ax)
+    di2 = 1.0 / (dx * dx)
+    hxx = (r(d, 1, 0) - 2 * d + r(d, -1, 0)) * di2
+    hyy = (r(d, 1, 1) - 2 * d + r(d, -1, 1)) * di2
+    hzz = (r(d, 1, 2) - 2 * d + r(d, -1, 2)) * di2
+    hxy = (r(r(d, 1, 0), 1, 1) - r(r(d, -1, 0), 1, 1) - r(r(d, 1, 0), -1, 1) + r(r(d, -1, 0), -1, 1)) * di2 * 0.25
+    hyz = (r(r(d, 1, 1), 1, 2) - r(r(d, 1, 1), -1, 2) - r(r(d, -1, 1), 1, 2) + r(r(d, -1, 1), -1, 2)) * di2 * 0.25
+    hxz = (r(r(d, 1, 0), 1, 2) - r(r(d, -1, 0), 1, 2) - r(r(d, 1, 0), -1, 2) + r(r(d, -1, 0), -1, 2)) * di2 * 0.25
+    a11, a22, a33 = 1 + hxx, 1 + hyy, 1 + hzz
+    return a11 * (a22 * a33 - hyz * hyz) + hxy * (hxz * hyz - hxy * a33) + hxz * (hxy * hyz - hxz * a22)
+
+
+@pytest.mark.parametrize("n", [16, 32, 64])
+def test_mixed_metric_float_float(mmh, oracle, fields, n):
+    """The mixed form's float-float metric (k_metric_ff: inputs split into
+    float pairs from their bit patterns, everything on the FP32 pipes)
+    against the oracle's FP64 metric.  A pair holds a double to 2^-48 of its
+    magnitude, so a Hessian entry (differences of four samples of def) is
+    within ~2^-46 max|def| / dx^2: every coefficient must be within
+    1e-13 + 2^-44 max|def| of the largest coefficient, and det likewise of
+    max |det|.  A deformation potential offset by 300 shows that term."""
+    for amp, off in ((0.3, 0.0), (0.3, 300.0)):
+        defpot = np.asfortranarray(smooth_field(n, amp, 21 + n) + off)
+        rho = fields.lognormal_density(n, sigma=1.0, seed=22 + n)
+        with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL) as ctx:
+            for dx in (1.0, 2.0):
+                g, det = ctx.metric_ff(defpot, rho, dx)
+                o = oracle.metric(defpot, rho, dx)
+                err = np.abs(g - o).max() / np.abs(o).max()
+                dn = _det_numpy(defpot, dx)
+                derr = np.abs(det - dn).max() / np.abs(dn).max()
+                bound = 1e-13 + 2.0 ** -44 * np.abs(defpot).max()
+                print(f"metric_ff {n}^3 offset {off} dx {dx}: coefficients {err:.2e}, det {derr:.2e} "
+                      f"(bound {bound:.1e})")
+                assert err <= bound and derr <= bound, (err, derr, bound)
+    with mmh.Context(n, precision=mmh.MMH_FP64) as ctx:
+        with pytest.raises(mmh.MMHError):
+            ctx.metric_ff(defpot, rho, 1.0)
 
 
 @pytest.mark.parametrize("n", [16, 32, 64])
