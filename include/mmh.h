@@ -134,7 +134,11 @@ int mmh_defp2delta_f64(mmh_ctx* ctx, const double* indata, double* outdata, cons
  * passes, mmh_relaxing_f64 one reciprocal per division site and
  * mmh_relax_f64 runs the FP32 Gauss-Seidel sweeps and FP32 residual of the
  * V-cycle on FP32 copies of its arrays (the kernels mmh_iterate runs in that
- * form; not bit-matched to the reference). */
+ * form; not bit-matched to the reference).  mmh_limiter_pass1_f64 and
+ * mmh_limiter_mask_f64 give the FP64 form's decisions, fluxes and defplim in
+ * both forms (the mixed form screens cells in FP32 and evaluates in FP64 only
+ * where a decision is close); in the mixed form pass 1's det extrema and rho2
+ * come from the float-float det (not bit-matched). */
 /* relax(arr,resid,rhs,deformpot,u,rinf,dx,n,n,n,1,nrelax,iopt)  gauss1.f90:64
  * iopt = 8*isolver + iresidopt with isolver = 2; resid((n/2)^3) is written
  * when iresidopt is 1 or 3. */

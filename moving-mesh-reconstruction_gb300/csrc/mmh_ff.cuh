@@ -80,6 +80,22 @@ __device__ __forceinline__ FF ff_of_bits(double x) {
   const float lo = __fmul_rn(r, __uint_as_float((unsigned)(E - 948) << 23));
   return {hi, sign ? -lo : lo};
 }
+// x truncated to a float from its bit pattern (integer operations only):
+// |x - f| < 2^-23 |x| + 2^-126.  Returns false (f = 0) for Inf, NaN and
+// |x| >= 2^128.
+__device__ __forceinline__ bool f32_trunc_bits(double x, float& f) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned h32 = (unsigned)(b >> 32), l32 = (unsigned)b;
+  const int E = (int)((h32 >> 20) & 0x7ffu);
+  if (E > 1150) {
+    f = 0.0f;
+    return false;
+  }
+  f = E < 897 ? __uint_as_float(h32 & 0x80000000u)
+              : __uint_as_float((h32 & 0x80000000u) | ((unsigned)(E - 896) << 23) | ((h32 & 0xfffffu) << 3) |
+                                (l32 >> 29));
+  return true;
+}
 // a - b for two float-float values of like magnitude (neighbouring samples
 // of a smooth field): TwoSum of the high parts, low parts added after.
 // Error ~2^-48 max(|a|, |b|).

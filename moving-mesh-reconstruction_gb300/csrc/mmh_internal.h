@@ -78,8 +78,17 @@ struct LimDev;
 void launch_calcdefp_rhs(double* tmp, const double* rho, int n, double dtold, bool mixed, cudaStream_t s);
 void launch_limiter_pass1(double* tmp, const double* def, const double* rho, int n, double dtold, double dtaumesh,
                           LimDev* st, uint8_t* maskx, uint8_t* maskc, cudaStream_t s);
+// the mixed form's pass 1: the same decisions and fluxes, FP32 screening and
+// FP64 only where a decision is close; detff = the float-float metric's det
+// of the same def
+void launch_limiter_pass1_mixed(double* tmp, const double* def, const double* rho, const double* detff, int n,
+                                double dtold, double dtaumesh, LimDev* st, uint8_t* maskx, uint8_t* maskc,
+                                cudaStream_t s);
 void launch_limiter_mask(double* defplim, const double* def, const double* defp, int n, double dtold, LimDev* st,
                          uint8_t* mask, cudaStream_t s);
+// the same outputs, FP32 screening and FP64 only for the cells that may matter
+void launch_limiter_mask_mixed(double* defplim, const double* def, const double* defp, int n, double dtold, LimDev* st,
+                               uint8_t* mask, cudaStream_t s);
 void launch_lim_reset(LimDev* st, cudaStream_t s);
 void launch_spec_tables(double* tab, int n, cudaStream_t s);
 void launch_spec_pack(const void* Xc, int n, int mode, void* Z, const LimDev* st, const double* tab, cudaStream_t s);

@@ -72,6 +72,24 @@ __device__ __forceinline__ __int128 fx_bits(double x, int sh) {
   return (b >> 63) ? -(__int128)v : (__int128)v;
 }
 __device__ __forceinline__ __int128 fx_of(double x) { return fx_bits(x, 64); }
+// trunc(x * 2^64) for a float, from its bits
+__device__ __forceinline__ __int128 fx_of_f(float x) {
+  const unsigned b = __float_as_uint(x);
+  int ex = (int)((b >> 23) & 0xffu);
+  unsigned m = b & 0x7fffffu;
+  if (ex == 0) {
+    if (m == 0) return 0;
+    ex = 1;
+  } else {
+    m |= 0x800000u;
+  }
+  const int s = ex - 150 + 64;
+  unsigned __int128 v;
+  if (s >= 0) v = (unsigned __int128)m << s;
+  else if (s > -32) v = (unsigned __int128)(m >> (-s));
+  else v = 0;
+  return (b >> 31) ? -(__int128)v : (__int128)v;
+}
 __device__ __forceinline__ double fx_to(unsigned long long lo, unsigned long long hi) {
   __int128 s = (__int128)(((unsigned __int128)hi << 64) | (unsigned __int128)lo);
   bool neg = s < 0;

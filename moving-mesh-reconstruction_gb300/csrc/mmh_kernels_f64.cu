@@ -296,81 +296,241 @@ __device__ __forceinline__ unsigned long long block_u64(unsigned long long v, un
   return v;
 }
 
+// Pass 1 of the limiter at one cell in FP64 (limiter.f90:268-372), the
+// reference's order: det from the Hessian of def, rho^2/det for rho2, the
+// expansion clamp (det > 10), the compression test, the flux clamps.
+struct Pass1Cell {
+  double eflux, det;
+  __int128 r2;
+  bool bad;
+  uint8_t mx, mc;
+};
+__device__ __forceinline__ Pass1Cell pass1_cell_fp64(const double* __restrict__ tmp, const double* __restrict__ def,
+                                                     const double* __restrict__ rho, int n, i64 t, double dtold,
+                                                     double dtaumesh, double cmpmaxglobal) {
+  Pass1Cell o;
+  int i, j, km;
+  cell_of(t, n, i, j, km);
+  int k = wp(km, n);
+  LimM m = lim_hess_det(def, n, i, j, k);
+  o.det = m.det;
+  double rl = rho[t];
+  double q = rl * rl / o.det;
+  o.bad = false;
+  o.r2 = 0;
+  if (!(fabs(q) < 4294967296.0)) o.bad = true;
+  else o.r2 = fx_of(q);
+  // momentum-flux divergence of a state at rest is zero (u(2:4) = 0)
+  double eflux = 0.0 + tmp[t];
+  o.mx = 0;
+  o.mc = 0;
+  const double densinit = 1.0;
+  if (o.det > 10.0 * densinit) {
+    eflux = -2.0 * fabs(eflux);
+    o.mx = 1;
+  }
+  // Only the sign of tlim is used here.  When the Gershgorin lower bound of
+  // the smallest eigenvalue of C = I + Hess(def) exceeds 1/cmpmax by a wide
+  // margin, tlim < 0 for certain and the trigonometric evaluation is skipped.
+  double c11 = 1.0 + m.phixx, c22 = 1.0 + m.phiyy, c33 = 1.0 + m.phizz;
+  double g = fmin(fmin(c11 - fabs(m.phixy) - fabs(m.phixz), c22 - fabs(m.phixy) - fabs(m.phiyz)),
+                  c33 - fabs(m.phixz) - fabs(m.phiyz));
+  double cmpmax = cmpmaxglobal * 1.0;
+  if (!(g > 1.0 / cmpmax + 1e-6)) {
+    double compression = compression_of(c11, m.phixy, m.phixz, c22, m.phiyz, c33);
+    double tlim = 3.0 * (1.0 / cmpmax - 1.0 / compression) / dtold;
+    if (tlim > 0.0) {
+      eflux = fmax(0.0, eflux);
+      o.mc = 1;
+    }
+  }
+  eflux = fmin(1.0 / dtaumesh, eflux);
+  eflux = fmax(-1.0 / dtaumesh, eflux);
+  o.eflux = eflux;
+  return o;
+}
+
+// The statistics of pass 1: one block reduction and one atomic per block and
+// statistic.  Every thread of the block calls it.
+__device__ __forceinline__ void pass1_commit(LimDev* st, unsigned long long nexp, unsigned long long dmax,
+                                             unsigned long long dmin, unsigned long long fmx, unsigned long long fmn,
+                                             bool bad, __int128 r2, unsigned long long* s_buf) {
+  unsigned long long v;
+  v = block_u64(nexp, s_buf, 0);
+  if (threadIdx.x == 0 && v) atomicAdd(&st->nexpand, v);
+  v = block_u64(dmax, s_buf, 1);
+  if (threadIdx.x == 0) atomicMax(&st->detmax, v);
+  v = block_u64(dmin, s_buf, 2);
+  if (threadIdx.x == 0) atomicMin(&st->detmin, v);
+  v = block_u64(fmx, s_buf, 1);
+  if (threadIdx.x == 0) atomicMax(&st->fluxmax, v);
+  v = block_u64(fmn, s_buf, 2);
+  if (threadIdx.x == 0) atomicMin(&st->fluxmin, v);
+  if (bad) atomicOr(&st->flag, 2);
+  fx_block_commit(r2, st->rho2);
+}
+
 __global__ void k_limiter_pass1(double* __restrict__ tmp, const double* __restrict__ def,
                                 const double* __restrict__ rho, int n, double dtold, double dtaumesh,
                                 double cmpmaxglobal, LimDev* st, uint8_t* __restrict__ maskx,
                                 uint8_t* __restrict__ maskc) {
+  __shared__ unsigned long long s_buf[32];
   i64 n3 = (i64)n * n * n;
   i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   __int128 r2 = 0;
   bool bad = false;
   unsigned long long nexp = 0;
-  double dmax = 0.0, dmin = 1.0, fmx = 0.0, fmn = 0.0;
+  unsigned long long dmax = ord_of(0.0), dmin = ord_of(1.0), fmx = ord_of(0.0), fmn = ord_of(0.0);
+  if (t < n3) {
+    const Pass1Cell o = pass1_cell_fp64(tmp, def, rho, n, t, dtold, dtaumesh, cmpmaxglobal);
+    tmp[t] = o.eflux;
+    r2 = o.r2;
+    bad = o.bad;
+    nexp = o.mx;
+    dmax = dmin = ord_of(o.det);
+    fmx = ord_of(fmax(0.0, o.eflux * dtold));
+    fmn = ord_of(fmin(0.0, o.eflux * dtold));
+    if (maskx) maskx[t] = o.mx;
+    if (maskc) maskc[t] = o.mc;
+  }
+  pass1_commit(st, nexp, dmax, dmin, fmx, fmn, bad, r2, s_buf);
+}
+
+// Pass 1 in the mixed form: the same decisions and fluxes as the FP64 pass,
+// with FP64 arithmetic only where a decision is close.  Every cell is first
+// screened in FP32 from its def samples truncated to floats (bit operations):
+// each sample is within 2^-23 |x| + 2^-126 of its double, so every entry of
+// C = I + Hess(def) is within E = 2^-18 max|sample| + 2^-20 (1 + sum |C_ij|)
+// of the FP64 one (about 4x the worst case of truncation and rounding), and
+// the Gershgorin bound g within 3E.  A cell with g - 3E above the FP64
+// shortcut's threshold skips the compression test in the FP64 pass too, so
+// its mc is 0; a cell whose float-float det(A) (detff, from the metric of the
+// same def: within 2^-40 (1 + max|sample|) (1 + sum|C_ij|)^2 of the FP64 det)
+// is that far from 10 has the FP64 expansion decision.  Cells where either
+// decision is close take pass1_cell_fp64, compacted so whole warps evaluate
+// it.  The flux is the FP64 pass's: the clamps only select values, -2|e| is
+// exact.  The statistics of the screened cells come from detff (det min and
+// max) and rho^2 / det in float-float (rho2): not bit-matched.
+__global__ void __launch_bounds__(256) k_limiter_pass1_mixed(double* __restrict__ tmp, const double* __restrict__ def,
+                                                             const double* __restrict__ rho,
+                                                             const double* __restrict__ detff, int n, double dtold,
+                                                             double dtaumesh, double lim, double cmpmaxglobal,
+                                                             float gthr,
+                                                             LimDev* st, uint8_t* __restrict__ maskx,
+                                                             uint8_t* __restrict__ maskc) {
+  __shared__ unsigned long long s_buf[32];
+  __shared__ int s_list[256];
+  __shared__ int s_cnt;
+  const i64 n3 = (i64)n * n * n;
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (threadIdx.x == 0) s_cnt = 0;
+  __syncthreads();
+  __int128 r2 = 0;
+  bool bad = false;
+  unsigned long long nexp = 0;
+  unsigned long long dmax = ord_of(0.0), dmin = ord_of(1.0), fmx = ord_of(0.0), fmn = ord_of(0.0);
+  const unsigned long long oL = ord_of(lim), onL = ord_of(-lim);  // lim = 1 / dtaumesh
   if (t < n3) {
     int i, j, km;
     cell_of(t, n, i, j, km);
-    int k = wp(km, n);
-    LimM m = lim_hess_det(def, n, i, j, k);
-    double det = m.det;
-    double rl = rho[t];
-    double q = rl * rl / det;
-    if (!(fabs(q) < 4294967296.0)) bad = true;
-    else r2 = fx_of(q);
-    // momentum-flux divergence of a state at rest is zero (u(2:4) = 0)
-    double eflux = 0.0 + tmp[t];
-    uint8_t mx = 0, mc = 0;
-    const double densinit = 1.0;
-    if (det > 10.0 * densinit) {
-      eflux = -2.0 * fabs(eflux);
-      nexp = 1;
-      mx = 1;
+    const int k = wp(km, n);
+    const int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), kq = wm(k, n);
+    bool ok = true;
+    float M = 0.0f;
+    auto S = [&](int x, int y, int z) {
+      float f;
+      ok = f32_trunc_bits(def[IDX(x, y, z, n)], f) && ok;
+      M = fmaxf(M, fabsf(f));
+      return f;
+    };
+    const float c0 = S(i, j, k);
+    const float hxx = (S(ip, j, k) - c0) + (S(im, j, k) - c0);
+    const float hyy = (S(i, jp, k) - c0) + (S(i, jm, k) - c0);
+    const float hzz = (S(i, j, kp) - c0) + (S(i, j, kq) - c0);
+    const float hxy = ((S(ip, jp, k) - S(im, jp, k)) - (S(ip, jm, k) - S(im, jm, k))) * 0.25f;
+    const float hyz = ((S(i, jp, kp) - S(i, jp, kq)) - (S(i, jm, kp) - S(i, jm, kq))) * 0.25f;
+    const float hxz = ((S(ip, j, kp) - S(im, j, kp)) - (S(ip, j, kq) - S(im, j, kq))) * 0.25f;
+    const float c11 = 1.0f + hxx, c22 = 1.0f + hyy, c33 = 1.0f + hzz;
+    const float sc = 1.0f + fabsf(c11) + fabsf(c22) + fabsf(c33) + 2.0f * (fabsf(hxy) + fabsf(hyz) + fabsf(hxz));
+    const float E = 3.814697265625e-6f * M + 9.5367431640625e-7f * sc;  // 2^-18 M + 2^-20 sc
+    const float g = fminf(fminf(c11 - fabsf(hxy) - fabsf(hxz), c22 - fabsf(hxy) - fabsf(hyz)),
+                          c33 - fabsf(hxz) - fabsf(hyz));
+    const bool gsure = g - 3.0f * E > gthr;
+    // pass 1 evaluates the metric at (i, j, k = km + 1) for the cell (i, j, km)
+    const double det = detff[IDX(i, j, k, n)];
+    float d32;
+    ok = f32_trunc_bits(det, d32) && ok;
+    const float Ed = 9.094947017729282e-13f * (1.0f + M) * sc * sc + 4.76837158203125e-6f * (1.0f + fabsf(d32));
+    const bool dsure = fabsf(d32 - 10.0f) > Ed;  // 2^-40 (1+M) sc^2 + 2^-21 (1 + |det|)
+    if (ok && gsure && dsure) {
+      const uint8_t mx = d32 > 10.0f;
+      // 0.0 + e: -0 becomes +0, everything else is kept
+      unsigned long long eb = (unsigned long long)__double_as_longlong(tmp[t]);
+      if (eb == 0x8000000000000000ull) eb = 0;
+      double e = __longlong_as_double((long long)eb);
+      if (mx) e = -2.0 * fabs(e);
+      // fmin(1/dtaumesh, e), then fmax(-1/dtaumesh, .): a NaN flux becomes 1/dtaumesh
+      const unsigned long long ebits = (unsigned long long)__double_as_longlong(e);
+      const bool nan = ((ebits >> 52) & 0x7ffull) == 0x7ffull && (ebits & 0xfffffffffffffull);
+      unsigned long long oe = ord_of(e);
+      if (nan || oe > oL) oe = oL;
+      if (oe < onL) oe = onL;
+      e = from_ord(oe);
+      tmp[t] = e;
+      if (maskx) maskx[t] = mx;
+      if (maskc) maskc[t] = 0;
+      nexp = mx;
+      dmax = dmin = ord_of(det);
+      const double ed = dtold == 1.0 ? e : e * dtold;
+      const unsigned long long oed = ord_of(ed);
+      fmx = oed > ord_of(0.0) ? oed : ord_of(0.0);
+      fmn = oed < ord_of(0.0) ? oed : ord_of(0.0);
+      // rho^2 / det in float-float, into the exact fixed-point sum
+      const FF rl = ff_of_bits(rho[t]);
+      const FF qq = ff_div(ff_mul(rl, rl), ff_of_bits(det));
+      if (!(fabsf(qq.hi) < 4294967296.0f)) bad = true;
+      else r2 = fx_of_f(qq.hi) + fx_of_f(qq.lo);
+    } else {
+      s_list[atomicAdd(&s_cnt, 1)] = threadIdx.x;
     }
-    // Only the sign of tlim is used here.  When the Gershgorin lower bound of
-    // the smallest eigenvalue of C = I + Hess(def) exceeds 1/cmpmax by a wide
-    // margin, tlim < 0 for certain and the trigonometric evaluation is skipped.
-    double c11 = 1.0 + m.phixx, c22 = 1.0 + m.phiyy, c33 = 1.0 + m.phizz;
-    double g = fmin(fmin(c11 - fabs(m.phixy) - fabs(m.phixz), c22 - fabs(m.phixy) - fabs(m.phiyz)),
-                    c33 - fabs(m.phixz) - fabs(m.phiyz));
-    double cmpmax = cmpmaxglobal * 1.0;
-    if (!(g > 1.0 / cmpmax + 1e-6)) {
-      double compression = compression_of(c11, m.phixy, m.phixz, c22, m.phiyz, c33);
-      double tlim = 3.0 * (1.0 / cmpmax - 1.0 / compression) / dtold;
-      if (tlim > 0.0) {
-        eflux = fmax(0.0, eflux);
-        mc = 1;
-      }
-    }
-    dmax = det;
-    dmin = det;
-    eflux = fmin(1.0 / dtaumesh, eflux);
-    eflux = fmax(-1.0 / dtaumesh, eflux);
-    tmp[t] = eflux;
-    fmx = fmax(0.0, eflux * dtold);
-    fmn = fmin(0.0, eflux * dtold);
-    if (maskx) maskx[t] = mx;
-    if (maskc) maskc[t] = mc;
   }
-  // block reductions, one atomic per block and statistic
-  __shared__ unsigned long long s_buf[32];
-  unsigned long long v;
-  v = block_u64(nexp, s_buf, 0);
-  if (threadIdx.x == 0 && v) atomicAdd(&st->nexpand, v);
-  v = block_u64(ord_of(dmax), s_buf, 1);
-  if (threadIdx.x == 0) atomicMax(&st->detmax, v);
-  v = block_u64(ord_of(dmin), s_buf, 2);
-  if (threadIdx.x == 0) atomicMin(&st->detmin, v);
-  v = block_u64(ord_of(fmx), s_buf, 1);
-  if (threadIdx.x == 0) atomicMax(&st->fluxmax, v);
-  v = block_u64(ord_of(fmn), s_buf, 2);
-  if (threadIdx.x == 0) atomicMin(&st->fluxmin, v);
-  if (bad) atomicOr(&st->flag, 2);
-  fx_block_commit(r2, st->rho2);
+  __syncthreads();
+  const int ncand = s_cnt;
+  for (int q = threadIdx.x; q < ncand; q += blockDim.x) {
+    const i64 tt = (i64)blockIdx.x * blockDim.x + s_list[q];
+    const Pass1Cell o = pass1_cell_fp64(tmp, def, rho, n, tt, dtold, dtaumesh, cmpmaxglobal);
+    tmp[tt] = o.eflux;
+    if (maskx) maskx[tt] = o.mx;
+    if (maskc) maskc[tt] = o.mc;
+    nexp += o.mx;
+    const unsigned long long od = ord_of(o.det);
+    dmax = od > dmax ? od : dmax;
+    dmin = od < dmin ? od : dmin;
+    const unsigned long long ox = ord_of(fmax(0.0, o.eflux * dtold)), on = ord_of(fmin(0.0, o.eflux * dtold));
+    fmx = ox > fmx ? ox : fmx;
+    fmn = on < fmn ? on : fmn;
+    bad = bad || o.bad;
+    r2 += o.r2;
+  }
+  pass1_commit(st, nexp, dmax, dmin, fmx, fmn, bad, r2, s_buf);
 }
 
 void launch_limiter_pass1(double* tmp, const double* def, const double* rho, int n, double dtold, double dtaumesh,
                           LimDev* st, uint8_t* maskx, uint8_t* maskc, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
   k_limiter_pass1<<<grid_of(n3, kBlock), kBlock, 0, s>>>(tmp, def, rho, n, dtold, dtaumesh, 10.0, st, maskx, maskc);
+  count_launch();
+}
+void launch_limiter_pass1_mixed(double* tmp, const double* def, const double* rho, const double* detff, int n,
+                                double dtold, double dtaumesh, LimDev* st, uint8_t* maskx, uint8_t* maskc,
+                                cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  // a float at or above the FP64 shortcut's threshold 1/cmpmax + 1e-6
+  const double thr = 1.0 / 10.0 + 1e-6;
+  float gthr = (float)thr;
+  if ((double)gthr < thr) gthr = nextafterf(gthr, 1.0f);
+  k_limiter_pass1_mixed<<<grid_of(n3, kBlock), kBlock, 0, s>>>(tmp, def, rho, detff, n, dtold, dtaumesh,
+                                                               1.0 / dtaumesh, 10.0, gthr, st, maskx, maskc);
   count_launch();
 }
 
@@ -383,16 +543,47 @@ void launch_limiter_pass1(double* tmp, const double* def, const double* rho, int
 // |mu| + am, so lo stays below and hi above the FP64 formula's smallest
 // eigenvalue.  They only decide which cells may skip the exact FP64 test; the
 // cells that take it, and therefore every output, are unchanged.
-__device__ __forceinline__ void compression_bounds32(const double* c, double& lo, double& hi) {
-  const float c11 = (float)c[0], c12 = (float)c[1], c13 = (float)c[2], c22 = (float)c[3], c23 = (float)c[4],
-              c33 = (float)c[5];
+__device__ __forceinline__ void compression_bounds_f(float c11, float c12, float c13, float c22, float c23, float c33,
+                                                     float& lo, float& hi) {
   const float mu = (c11 + c22 + c33) * (1.0f / 3.0f);
   const float d11 = c11 - mu, d22 = c22 - mu;
   const float a = d11 * d11 + c12 * c12 + c13 * c13 + d11 * d22 + d22 * d22 + c23 * c23;
   const float am = 2.0f * sqrtf(fabsf(a) * (1.0f / 3.0f));
   const float margin = 1e-5f * (fabsf(mu) + am) + 1e-30f;
-  lo = (double)(mu - am - margin);
-  hi = (double)((mu - 0.49f * am) + margin);
+  lo = mu - am - margin;
+  hi = (mu - 0.49f * am) + margin;
+}
+__device__ __forceinline__ void compression_bounds32(const double* c, double& lo, double& hi) {
+  float l, h;
+  compression_bounds_f((float)c[0], (float)c[1], (float)c[2], (float)c[3], (float)c[4], (float)c[5], l, h);
+  lo = (double)l;
+  hi = (double)h;
+}
+
+// C = I + Hess(def + dtold defp) at cell t in FP64, the reference's order
+// (limiter.f90:498-520): c = (C11, C12, C13, C22, C23, C33).
+__device__ __forceinline__ void mask_c64(const double* __restrict__ def, const double* __restrict__ defp, int n, i64 t,
+                                         double dtold, double* c) {
+  int i, j, k;
+  cell_of(t, n, i, j, k);
+  int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
+#define P_(x, y, z) defp[IDX(x, y, z, n)]
+#define D_(x, y, z) def[IDX(x, y, z, n)]
+  double phixx = (P_(ip, j, k) - 2.0 * P_(i, j, k) + P_(im, j, k)) * dtold;
+  double phiyy = (P_(i, jp, k) - 2.0 * P_(i, j, k) + P_(i, jm, k)) * dtold;
+  double phizz = (P_(i, j, kp) - 2.0 * P_(i, j, k) + P_(i, j, km)) * dtold;
+  double phixy = (P_(ip, jp, k) - P_(im, jp, k) - P_(ip, jm, k) + P_(im, jm, k)) * 0.25 * dtold;
+  double phiyz = (P_(i, jp, kp) - P_(i, jp, km) - P_(i, jm, kp) + P_(i, jm, km)) * 0.25 * dtold;
+  double phixz = (P_(ip, j, kp) - P_(im, j, kp) - P_(ip, j, km) + P_(im, j, km)) * 0.25 * dtold;
+  phixx = phixx + (D_(ip, j, k) - 2.0 * D_(i, j, k) + D_(im, j, k));
+  phiyy = phiyy + (D_(i, jp, k) - 2.0 * D_(i, j, k) + D_(i, jm, k));
+  phizz = phizz + (D_(i, j, kp) - 2.0 * D_(i, j, k) + D_(i, j, km));
+  phixy = phixy + (D_(ip, jp, k) - D_(im, jp, k) - D_(ip, jm, k) + D_(im, jm, k)) * 0.25;
+  phiyz = phiyz + (D_(i, jp, kp) - D_(i, jp, km) - D_(i, jm, kp) + D_(i, jm, km)) * 0.25;
+  phixz = phixz + (D_(ip, j, kp) - D_(im, j, kp) - D_(ip, j, km) + D_(im, j, km)) * 0.25;
+#undef P_
+#undef D_
+  c[0] = 1.0 + phixx; c[1] = phixy; c[2] = phixz; c[3] = 1.0 + phiyy; c[4] = phiyz; c[5] = 1.0 + phizz;
 }
 
 // Final compression test (limiter.f90:498-533): defplim = tlim where tlim > 0,
@@ -417,26 +608,7 @@ __global__ void __launch_bounds__(256) k_limiter_mask(double* __restrict__ defpl
   double c[6] = {0, 0, 0, 0, 0, 0};
   double lo = 0.0, hi = 0.0;
   if (t < n3) {
-    int i, j, k;
-    cell_of(t, n, i, j, k);
-    int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
-#define P_(x, y, z) defp[IDX(x, y, z, n)]
-#define D_(x, y, z) def[IDX(x, y, z, n)]
-    double phixx = (P_(ip, j, k) - 2.0 * P_(i, j, k) + P_(im, j, k)) * dtold;
-    double phiyy = (P_(i, jp, k) - 2.0 * P_(i, j, k) + P_(i, jm, k)) * dtold;
-    double phizz = (P_(i, j, kp) - 2.0 * P_(i, j, k) + P_(i, j, km)) * dtold;
-    double phixy = (P_(ip, jp, k) - P_(im, jp, k) - P_(ip, jm, k) + P_(im, jm, k)) * 0.25 * dtold;
-    double phiyz = (P_(i, jp, kp) - P_(i, jp, km) - P_(i, jm, kp) + P_(i, jm, km)) * 0.25 * dtold;
-    double phixz = (P_(ip, j, kp) - P_(im, j, kp) - P_(ip, j, km) + P_(im, j, km)) * 0.25 * dtold;
-    phixx = phixx + (D_(ip, j, k) - 2.0 * D_(i, j, k) + D_(im, j, k));
-    phiyy = phiyy + (D_(i, jp, k) - 2.0 * D_(i, j, k) + D_(i, jm, k));
-    phizz = phizz + (D_(i, j, kp) - 2.0 * D_(i, j, k) + D_(i, j, km));
-    phixy = phixy + (D_(ip, jp, k) - D_(im, jp, k) - D_(ip, jm, k) + D_(im, jm, k)) * 0.25;
-    phiyz = phiyz + (D_(i, jp, kp) - D_(i, jp, km) - D_(i, jm, kp) + D_(i, jm, km)) * 0.25;
-    phixz = phixz + (D_(ip, j, kp) - D_(im, j, kp) - D_(ip, j, km) + D_(im, j, km)) * 0.25;
-#undef P_
-#undef D_
-    c[0] = 1.0 + phixx; c[1] = phixy; c[2] = phixz; c[3] = 1.0 + phiyy; c[4] = phiyz; c[5] = 1.0 + phizz;
+    mask_c64(def, defp, n, t, dtold, c);
     compression_bounds32(c, lo, hi);
   }
   const bool pd = t < n3 && lo > 0.0;
@@ -489,6 +661,122 @@ void launch_limiter_mask(double* defplim, const double* def, const double* defp,
                          uint8_t* mask, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
   k_limiter_mask<<<grid_of(n3, kBlock), kBlock, 0, s>>>(defplim, def, defp, n, dtold, 10.0, st, mask);
+  count_launch();
+}
+
+// The final compression test in the mixed form: the same outputs as
+// k_limiter_mask, with FP64 arithmetic only for the cells that may matter.
+// The bounds lo and hi come from C in FP32, formed from the samples of def
+// and defp truncated to floats (bit operations): every entry is within E =
+// 2^-18 (max|def sample| + |dtold| max|defp sample|) + 2^-20 (1 + sum|C_ij|)
+// of the FP64 one (about 4x the worst case of truncation and rounding), so
+// the smallest eigenvalue within 3E, by which lo and hi are widened.  The
+// cells that are not skipped form C in FP64 (mask_c64) after compaction.
+// inv_tight = (1/cmpmax)(1 + 1e-12), formed on the host.
+__global__ void __launch_bounds__(256) k_limiter_mask_mixed(double* __restrict__ defplim,
+                                                            const double* __restrict__ def,
+                                                            const double* __restrict__ defp, int n, double dtold,
+                                                            double cmpmaxglobal, double inv_tight, LimDev* st,
+                                                            uint8_t* __restrict__ mask) {
+  __shared__ int s_list[256];
+  __shared__ int s_cnt;
+  __shared__ unsigned long long s_buf[32];
+  __shared__ unsigned long long s_lam;
+  __shared__ double s_lam_g;
+  const i64 n3 = (i64)n * n * n;
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (threadIdx.x == 0) {
+    s_cnt = 0;
+    // the largest compression folded in so far (exact values of evaluated cells)
+    const double tg = from_ord(*(volatile unsigned long long*)&st->cmax);
+    s_lam_g = tg > 0.0 ? (1.0 / tg) * (1.0 + 1e-15) : INFINITY;
+  }
+  const double cmpmax = cmpmaxglobal * 1.0;
+  const float dtf = (float)dtold;
+  float lo = 0.0f, hi = 0.0f;
+  bool ok = true;
+  if (t < n3) {
+    int i, j, k;
+    cell_of(t, n, i, j, k);
+    const int ip = wp(i, n), im = wm(i, n), jp = wp(j, n), jm = wm(j, n), kp = wp(k, n), km = wm(k, n);
+    float Md = 0.0f, Mp = 0.0f;
+    auto D = [&](int x, int y, int z) {
+      float f;
+      ok = f32_trunc_bits(def[IDX(x, y, z, n)], f) && ok;
+      Md = fmaxf(Md, fabsf(f));
+      return f;
+    };
+    auto P = [&](int x, int y, int z) {
+      float f;
+      ok = f32_trunc_bits(defp[IDX(x, y, z, n)], f) && ok;
+      Mp = fmaxf(Mp, fabsf(f));
+      return f;
+    };
+    const float pc = P(i, j, k), dc = D(i, j, k);
+    const float pxx = ((P(ip, j, k) - pc) + (P(im, j, k) - pc)) * dtf;
+    const float pyy = ((P(i, jp, k) - pc) + (P(i, jm, k) - pc)) * dtf;
+    const float pzz = ((P(i, j, kp) - pc) + (P(i, j, km) - pc)) * dtf;
+    const float pxy = ((P(ip, jp, k) - P(im, jp, k)) - (P(ip, jm, k) - P(im, jm, k))) * 0.25f * dtf;
+    const float pyz = ((P(i, jp, kp) - P(i, jp, km)) - (P(i, jm, kp) - P(i, jm, km))) * 0.25f * dtf;
+    const float pxz = ((P(ip, j, kp) - P(im, j, kp)) - (P(ip, j, km) - P(im, j, km))) * 0.25f * dtf;
+    const float c11 = 1.0f + (pxx + ((D(ip, j, k) - dc) + (D(im, j, k) - dc)));
+    const float c22 = 1.0f + (pyy + ((D(i, jp, k) - dc) + (D(i, jm, k) - dc)));
+    const float c33 = 1.0f + (pzz + ((D(i, j, kp) - dc) + (D(i, j, km) - dc)));
+    const float c12 = pxy + ((D(ip, jp, k) - D(im, jp, k)) - (D(ip, jm, k) - D(im, jm, k))) * 0.25f;
+    const float c23 = pyz + ((D(i, jp, kp) - D(i, jp, km)) - (D(i, jm, kp) - D(i, jm, km))) * 0.25f;
+    const float c13 = pxz + ((D(ip, j, kp) - D(im, j, kp)) - (D(ip, j, km) - D(im, j, km))) * 0.25f;
+    const float sc = 1.0f + fabsf(c11) + fabsf(c22) + fabsf(c33) + 2.0f * (fabsf(c12) + fabsf(c23) + fabsf(c13));
+    const float E = 3.814697265625e-6f * (Md + fabsf(dtf) * Mp) + 9.5367431640625e-7f * sc;  // 2^-18, 2^-20
+    compression_bounds_f(c11, c12, c13, c22, c23, c33, lo, hi);
+    lo -= 3.0f * E;
+    hi += 3.0f * E;
+  }
+  const bool pd = t < n3 && ok && lo > 0.0f;
+  // smallest upper bound of the block's positive definite cells
+  unsigned long long lam = block_u64(pd ? ord_of((double)hi) : ord_of(INFINITY), s_buf, 2);
+  if (threadIdx.x == 0) s_lam = lam;
+  __syncthreads();
+  const double lam_b = from_ord(s_lam), lam_g = s_lam_g, lod = (double)lo;
+  const bool skip = pd && dtold > 0.0 && lod > inv_tight && (lod > lam_b || lod >= lam_g);
+  if (t < n3) {
+    if (skip) {
+      defplim[t] = 0.0;
+      if (mask) mask[t] = 0;
+    } else {
+      s_list[atomicAdd(&s_cnt, 1)] = threadIdx.x;
+    }
+  }
+  __syncthreads();
+  unsigned long long cnt = 0, cm = ord_of(0.0);
+  const int ncand = s_cnt;
+  for (int q = threadIdx.x; q < ncand; q += blockDim.x) {
+    const i64 tt = (i64)blockIdx.x * blockDim.x + s_list[q];
+    double c[6];
+    mask_c64(def, defp, n, tt, dtold, c);
+    double compression = compression_of(c[0], c[1], c[2], c[3], c[4], c[5]);
+    double tlim = 3.0 * (1.0 / cmpmax - 1.0 / compression) / dtold;
+    unsigned long long o = ord_of(fmax(0.0, compression));
+    cm = o > cm ? o : cm;
+    double v = 0.0;
+    uint8_t mk = 0;
+    if (tlim > 0.0) {
+      cnt += 1;
+      v = tlim;
+      mk = 1;
+    }
+    defplim[tt] = v;
+    if (mask) mask[tt] = mk;
+  }
+  unsigned long long r = block_u64(cnt, s_buf, 0);
+  if (threadIdx.x == 0 && r) atomicAdd(&st->ncompress, r);
+  r = block_u64(cm, s_buf, 1);
+  if (threadIdx.x == 0) atomicMax(&st->cmax, r);
+}
+void launch_limiter_mask_mixed(double* defplim, const double* def, const double* defp, int n, double dtold, LimDev* st,
+                               uint8_t* mask, cudaStream_t s) {
+  i64 n3 = (i64)n * n * n;
+  k_limiter_mask_mixed<<<grid_of(n3, kBlock), kBlock, 0, s>>>(defplim, def, defp, n, dtold, 10.0,
+                                                              (1.0 / 10.0) * (1.0 + 1e-12), st, mask);
   count_launch();
 }
 

@@ -139,6 +139,9 @@ struct mmh_ctx {
   double* coarse_inv = nullptr;
   // the finest solve level's FP64 coefficient buffer holds float-float pairs
   bool coef_ff = false;
+  // the finest metric of the resident def is built (calcdefp's mixed pass 1
+  // reads its det); the next multigrid call at level 0 uses it as it is
+  bool levels_ready = false;
   uint8_t* mask(int q) { return keep_masks ? masks + q * n3 : nullptr; }
 
   double* defp() { return h64.u[0]; }
@@ -584,7 +587,9 @@ int multigrid_level(mmh_ctx* c, int l0, double dx, mmh_diag* d) {
   // The mixed form's float-float metric also gives det(A) for rgzerosum, so
   // the metric goes first there (it does not depend on rhs or u).
   const bool det_from_metric = ff_outer(c) && l0 < c->nlev - 1 && dx == double(1 << l0);
-  if (det_from_metric) RET(build_levels(c, l0));
+  const bool ready = c->levels_ready && l0 == 0;
+  c->levels_ready = false;
+  if (det_from_metric && !ready) RET(build_levels(c, l0));
   RET(rgzerosum(c, c->h64.rhs[l0], c->defl[l0], n, dx, det_from_metric));
   RET(usum_zerosum<double>(c, c->h64.u[l0], n3));
   launch_absmax<double>(c->h64.rhs[l0], n3, &c->sc->rhsbits, c->s);
@@ -744,14 +749,26 @@ int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t
   smooth_step(c, c->scr, tmp);
   smooth_step(c, tmp, c->scr);
   launch_lim_reset(&c->sc->lim, c->s);
-  launch_limiter_pass1(c->scr, c->def, c->rho, n, dtold, dtaumesh, &c->sc->lim, mx, mc1, c->s);
+  c->levels_ready = false;
+  if (ff_outer(c) && c->nlev > 1) {
+    // The float-float metric of def (which calcdefp does not change) is
+    // built first: pass 1 screens its expansion test with its det.
+    RET(build_levels(c, 0));
+    c->levels_ready = true;
+    launch_limiter_pass1_mixed(c->scr, c->def, c->rho, c->det, n, dtold, dtaumesh, &c->sc->lim, mx, mc1, c->s);
+  } else {
+    launch_limiter_pass1(c->scr, c->def, c->rho, n, dtold, dtaumesh, &c->sc->lim, mx, mc1, c->s);
+  }
   smooth_step(c, c->scr, tmp);
   launch_fill<double>(defp, n3, 0.0, c->s);
   int st = multigrid_level(c, 0, 1.0, d);
   if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
   smooth_step(c, defp, c->scr);
   smooth_step(c, c->scr, defp);
-  launch_limiter_mask(c->defplim, c->def, defp, n, dtold, &c->sc->lim, mc2, c->s);
+  if (c->cfg.precision == MMH_MIXED)
+    launch_limiter_mask_mixed(c->defplim, c->def, defp, n, dtold, &c->sc->lim, mc2, c->s);
+  else
+    launch_limiter_mask(c->defplim, c->def, defp, n, dtold, &c->sc->lim, mc2, c->s);
   // The FFT Poisson correction adds F^-1[F[defplim]/kernel], which is zero
   // when no cell was limited: its transforms run only when one was.
   RET(pull_scal(c));
@@ -1831,7 +1848,16 @@ int mmh_limiter_pass1_f64(mmh_ctx* c, double* tmp, const double* def, const doub
   uint8_t* dm = nullptr;
   CK(cudaMallocAsync((void**)&dm, 2 * n3, c->s));
   launch_lim_reset(&c->sc->lim, c->s);
-  launch_limiter_pass1(c->scr, c->def, c->rho, n, dtold, dtaumesh, &c->sc->lim, dm, dm + n3, c->s);
+  if (c->cfg.precision == MMH_MIXED) {
+    // the mixed form screens with the float-float metric's det (the metric
+    // of level 0 is rebuilt by the next solve)
+    launch_metric_ff(c->def, c->rho, n, 1.0, c->h64.coef[0], c->h32.coef[0], c->det, c->s);
+    c->coef_ff = true;
+    c->levels_ready = false;
+    launch_limiter_pass1_mixed(c->scr, c->def, c->rho, c->det, n, dtold, dtaumesh, &c->sc->lim, dm, dm + n3, c->s);
+  } else {
+    launch_limiter_pass1(c->scr, c->def, c->rho, n, dtold, dtaumesh, &c->sc->lim, dm, dm + n3, c->s);
+  }
   RET(download(c, c->scr, tmp, n3));
   if (maskx) CK(cudaMemcpyAsync(maskx, dm, n3, cudaMemcpyDeviceToHost, c->s));
   if (maskc) CK(cudaMemcpyAsync(maskc, dm + n3, n3, cudaMemcpyDeviceToHost, c->s));
@@ -1851,7 +1877,10 @@ int mmh_limiter_mask_f64(mmh_ctx* c, double* defplim, const double* def, const d
   uint8_t* dm = nullptr;
   CK(cudaMallocAsync((void**)&dm, n3, c->s));
   launch_lim_reset(&c->sc->lim, c->s);
-  launch_limiter_mask(c->defplim, c->def, c->scr, n, dtold, &c->sc->lim, dm, c->s);
+  if (c->cfg.precision == MMH_MIXED)
+    launch_limiter_mask_mixed(c->defplim, c->def, c->scr, n, dtold, &c->sc->lim, dm, c->s);
+  else
+    launch_limiter_mask(c->defplim, c->def, c->scr, n, dtold, &c->sc->lim, dm, c->s);
   RET(download(c, c->defplim, defplim, n3));
   if (mask) CK(cudaMemcpyAsync(mask, dm, n3, cudaMemcpyDeviceToHost, c->s));
   CK(cudaFreeAsync(dm, c->s));

@@ -11,7 +11,10 @@ runs in that form, which are not bit-matched to the reference:
   restatement in numpy gives 6e-9 at 32^3 for a step that moves the density
   by 0.2).
 * the float-float metric of the outer residual (k_metric_ff) within
-  1e-13 + 2^-44 max|def| of the largest coefficient.
+  1e-13 + 2^-44 max|def| of the largest coefficient;
+* the limiter's pass 1 and final compression test screen cells in FP32 and
+  evaluate in FP64 only where a decision is close: fluxes, masks and defplim
+  identical to the FP64 form's.
 The float-float outer residual (k_residual_ff) is checked against an FP64
 recomputation in test_gpu_parity.py::test_multigrid_mixed_float_float_outer_loop.
 """
@@ -77,6 +80,52 @@ def test_mixed_metric_float_float(mmh, oracle, fields, n):
     with mmh.Context(n, precision=mmh.MMH_FP64) as ctx:
         with pytest.raises(mmh.MMHError):
             ctx.metric_ff(defpot, rho, 1.0)
+
+
+@pytest.mark.parametrize("n,amp,off", [(16, 2.0, 0.0), (32, 4.0, 0.0), (32, 4.0, 300.0), (64, 3.0, 0.0)])
+def test_mixed_limiter_pass1_same_decisions(mmh, oracle, fields, n, amp, off):
+    """The mixed form's pass 1 (every cell screened in FP32 from truncated
+    samples with a bounded error, FP64 only where a decision is close)
+    against the oracle: the flux and both trigger masks bit-identical, the
+    expansion count equal; the det extrema and rho2, which come from the
+    float-float det, within 1e-12.  The offset puts the samples far above
+    their differences, which widens the screen's margin."""
+    defpot = np.asfortranarray(smooth_field(n, amp, 77) + off)
+    _, u = fields.initial_state(n, sigma=1.0, seed=78)
+    rho = np.asfortranarray(u[0])
+    tmp0 = np.asfortranarray(np.random.default_rng(n).standard_normal((n, n, n)) * 0.05)
+    to, mxo, mco, do = oracle.limiter_pass1(tmp0, defpot, u)
+    tg = tmp0.copy(order="F")
+    with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL) as ctx:
+        mxg, mcg, dg = ctx.limiter_pass1(tg, defpot, rho)
+    print(f"pass 1 {n}^3 amp {amp} offset {off}: expand {int(mxo.sum())}, compress {int(mco.sum())}; "
+          f"det max {dg['detmax']} vs {do['detmax']}, rho2 {dg['rho2']} vs {do['rho2']}")
+    assert np.array_equal(mxo, mxg) and np.array_equal(mco, mcg)
+    assert np.array_equal(to, tg)
+    assert do["nexpand"] == dg["nexpand"]
+    for key in ("detmax", "detmin", "rho2"):
+        assert abs(dg[key] - do[key]) <= 1e-12 * abs(do[key]), key
+    assert mco.sum() > 0
+
+
+@pytest.mark.parametrize("n,amp,off", [(16, 2.0, 0.0), (32, 4.0, 0.0), (32, 4.0, 300.0), (64, 3.0, 0.0)])
+def test_mixed_limiter_mask_same_decisions(mmh, oracle, n, amp, off):
+    """The mixed form's final compression test (FP32 screen, FP64 for the
+    cells that may matter) against the FP64 form: defplim and the mask
+    bit-identical, the count and the largest compression equal; the mask
+    also equals the oracle's."""
+    defpot = np.asfortranarray(smooth_field(n, amp, 91) + off)
+    defp = smooth_field(n, amp * 0.3, 92)
+    _, mo, do = oracle.limiter_mask(defpot, defp)
+    with mmh.Context(n) as ctx:
+        l64, m64, d64 = ctx.limiter_mask(defpot, defp)
+    with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL) as ctx:
+        lm, mm, dm = ctx.limiter_mask(defpot, defp)
+    print(f"mask {n}^3 amp {amp} offset {off}: limited {int(mm.sum())}, cmax {dm['cmax']}")
+    assert np.array_equal(m64, mm) and np.array_equal(mo, mm)
+    assert np.array_equal(l64, lm)
+    assert d64["ncompress"] == dm["ncompress"] == do["ncompress"] and dm["ncompress"] > 0
+    assert d64["cmax"] == dm["cmax"]
 
 
 @pytest.mark.parametrize("n", [16, 32, 64])
