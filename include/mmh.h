@@ -343,6 +343,12 @@ int mmh_iterate_adjoint_f64(mmh_ctx* ctx, int niter, int checkpoint_every, const
  * reports the shape in use for grid n on the current device (MMH_ERR_ARG when
  * none has been chosen yet). */
 int mmh_gs_tile_pin(int shape);
+/* The FP32 residual and operator stencil of the mixed form's V-cycles and
+ * conjugate gradients: from 64^3 up a CTA marches through 8 planes of its
+ * tile column, keeping a ring of planes in shared memory and copying the next
+ * plane while it computes one (the default, kind -1 or 1); kind 0 pins one
+ * plane per CTA.  Both compute the same bits. */
+int mmh_stencil_pin(int kind);
 int mmh_gs_tile(int n, int* tx, int* ty);
 
 /* ---- kernel timing (no counterpart in the reference) -------------------- */

@@ -39,6 +39,9 @@ template <class T> void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, in
 // timed per grid size and device), and the shape chosen for n (-1: none yet)
 constexpr int kGsShapes = 4;
 extern std::atomic<int> gs_tile_override;
+// FP32 residual/operator stencil: -1 default (marching from 64^3 up), 0 one
+// plane per CTA, 1 marching
+extern std::atomic<int> stencil_march_pin;
 int gs_tile_chosen(int n, int* tx, int* ty);
 template <class T>
 void launch_residual(const T* phi, const T* rhs, const T* coef, int n, T dx, T* r, float* r32,

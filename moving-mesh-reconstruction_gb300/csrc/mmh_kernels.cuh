@@ -710,6 +710,154 @@ __global__ void __launch_bounds__(256) k_stencil_plane(const T* __restrict__ phi
   if (maxbits) block_max_commit(from_bits(mb), maxbits);
 }
 
+// cp.async helpers: 16-byte global -> shared copies that bypass registers
+// (cp.async.cg: cached in L2 only), committed and waited for as groups.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// The FP32 residual (MODE 0: r = rhs - L[phi]) or operator (MODE 1: q = L[p])
+// of k_stencil_plane, with each CTA marching through KC consecutive planes of
+// one 32 x 16 tile column instead of taking one plane.  Shared memory keeps
+// a ring of four planes of phi and of coefficients 3, 5, 6 (the planes k-1,
+// k, k+1 a plane reads, and k+2 in flight) and two of coefficients 1, 2, 4 and
+// of rhs, so every plane of a field is fetched once per column instead of
+// three times (phi) or twice (3, 5, 6), and the next plane's tiles are copied
+// (cp.async) while the current one is computed.  Tiles of phi and of
+// coefficients 1-5 carry a halo of 4 cells in x (aligned 16-byte copies) and
+// 1 in y; coefficient 6 and rhs are read at the cell only.  The arithmetic is
+// k_stencil_plane's, operand for operand.  Needs n >= 32 and KC | n.
+constexpr int kMarchKC = 8;
+struct MarchGeom {
+  static constexpr int TX = 32, TY = 16, HX = 4, W = TX + 2 * HX, HT = TY + 2, S = W * HT, SI = TX * TY;
+  // slots: phi 4, f3 4, f5 4, f1 2, f2 2, f4 2 halo tiles; f6 4, rhs 2 interior tiles
+  static constexpr int PHI = 0, F3 = 4 * S, F5 = 8 * S, F1 = 12 * S, F2 = 14 * S, F4 = 16 * S, F6 = 18 * S,
+                       RHS = 18 * S + 4 * SI, WORDS = 18 * S + 6 * SI;
+};
+template <int MODE>
+__global__ void __launch_bounds__(256) k_stencil_march(const float* __restrict__ phi, const float* __restrict__ rhs,
+                                                       const float* __restrict__ coef, int n, float di2,
+                                                       float* __restrict__ out, unsigned long long* maxbits) {
+  typedef MarchGeom G;
+  constexpr int TX = G::TX, TY = G::TY, HX = G::HX, W = G::W, S = G::S, SI = G::SI, KC = kMarchKC;
+  extern __shared__ __align__(16) float smf[];
+  const i64 n2 = (i64)n * n, n3 = n2 * n;
+  const int i0 = blockIdx.x * TX - HX, j0 = blockIdx.y * TY - 1, k0 = blockIdx.z * KC;
+  const int e = threadIdx.x;
+  // this thread's 16-byte group of a halo tile (e < 180) and of an interior tile (e < 128)
+  const int hxv = e % (W / 4), hy = e / (W / 4);
+  int gi = i0 + 4 * hxv, gj = j0 + hy;
+  gi += (gi < 0) ? n : ((gi >= n) ? -n : 0);
+  gj += (gj < 0) ? n : ((gj >= n) ? -n : 0);
+  const i64 hoff = (i64)gi + (i64)n * gj;
+  const int hdst = hy * W + 4 * hxv;
+  const bool hl = e < (W / 4) * G::HT;
+  const int ixv = e % (TX / 4), iy = (e / (TX / 4)) & (TY - 1);
+  const i64 ioff = (i64)(blockIdx.x * TX + 4 * ixv) + (i64)n * (blockIdx.y * TY + iy);
+  const int idst = iy * TX + 4 * ixv;
+  const bool il = e < SI / 4;  // e < 128: coefficient 6; 128 <= e < 256: rhs
+  const float* f1 = coef;
+  const float* f2 = coef + n3;
+  const float* f3 = coef + 2 * n3;
+  const float* f4 = coef + 3 * n3;
+  const float* f5 = coef + 4 * n3;
+  const float* f6 = coef + 5 * n3;
+  auto ring4 = [&](int kk) { return (kk - k0 + 1) & 3; };
+  auto ring2 = [&](int kk) { return (kk - k0) & 1; };
+  auto plane = [&](int kk) { return kk < 0 ? kk + n : (kk >= n ? kk - n : kk); };
+  // copies of plane kk of a field with a halo tile / the interior tile
+  auto halo = [&](const float* f, int kk, int slot) {
+    if (hl) cp_async16(smf + slot + hdst, f + hoff + n2 * plane(kk));
+  };
+  auto f6_rhs = [&](int k6, int kr) {
+    if (il) cp_async16(smf + G::F6 + ring4(k6) * SI + idst, f6 + ioff + n2 * plane(k6));
+    else if (MODE == 0) cp_async16(smf + G::RHS + ring2(kr) * SI + idst, rhs + ioff + n2 * plane(kr));
+  };
+  // the planes the first plane of the column reads
+#pragma unroll
+  for (int d = -1; d <= 1; ++d) {
+    halo(phi, k0 + d, G::PHI + ring4(k0 + d) * S);
+    halo(f3, k0 + d, G::F3 + ring4(k0 + d) * S);
+    halo(f5, k0 + d, G::F5 + ring4(k0 + d) * S);
+    if (il) cp_async16(smf + G::F6 + ring4(k0 + d) * SI + idst, f6 + ioff + n2 * plane(k0 + d));
+  }
+  halo(f1, k0, G::F1);
+  halo(f2, k0, G::F2);
+  halo(f4, k0, G::F4);
+  if (!il && MODE == 0) cp_async16(smf + G::RHS + idst, rhs + ioff + n2 * k0);
+  cp_async_commit();
+  cp_async_wait_all();
+  __syncthreads();
+  const int tx = threadIdx.x % TX, ty0 = threadIdx.x / TX;
+  constexpr int NCELL = TY / (256 / TX);
+  decltype(abs_bits(0.0f)) mb = 0;
+  for (int k = k0; k < k0 + KC; ++k) {
+    if (k + 1 < k0 + KC) {
+      // what plane k+1 adds: phi and coefficients 3, 5, 6 of k+2; 1, 2, 4 and rhs of k+1
+      halo(phi, k + 2, G::PHI + ring4(k + 2) * S);
+      halo(f3, k + 2, G::F3 + ring4(k + 2) * S);
+      halo(f5, k + 2, G::F5 + ring4(k + 2) * S);
+      halo(f1, k + 1, G::F1 + ring2(k + 1) * S);
+      halo(f2, k + 1, G::F2 + ring2(k + 1) * S);
+      halo(f4, k + 1, G::F4 + ring2(k + 1) * S);
+      f6_rhs(k + 2, k + 1);
+      cp_async_commit();
+    }
+    const float* P = smf + G::PHI + ring4(k) * S;
+    const float* Km = smf + G::PHI + ring4(k - 1) * S;
+    const float* Kp = smf + G::PHI + ring4(k + 1) * S;
+    const float* F1 = smf + G::F1 + ring2(k) * S;
+    const float* F2 = smf + G::F2 + ring2(k) * S;
+    const float* F4 = smf + G::F4 + ring2(k) * S;
+    const float* F3 = smf + G::F3 + ring4(k) * S;
+    const float* F3m = smf + G::F3 + ring4(k - 1) * S;
+    const float* F3p = smf + G::F3 + ring4(k + 1) * S;
+    const float* F5 = smf + G::F5 + ring4(k) * S;
+    const float* F5m = smf + G::F5 + ring4(k - 1) * S;
+    const float* F5p = smf + G::F5 + ring4(k + 1) * S;
+    const float* F6 = smf + G::F6 + ring4(k) * SI;
+    const float* F6m = smf + G::F6 + ring4(k - 1) * SI;
+    const float* F6p = smf + G::F6 + ring4(k + 1) * SI;
+    const float* R = smf + G::RHS + ring2(k) * SI;
+#pragma unroll
+    for (int q = 0; q < NCELL; ++q) {
+      const int ty = ty0 + q * (256 / TX);
+      const int c = (1 + ty) * W + HX + tx, ci = ty * TX + tx;
+      const i64 gt = (i64)(blockIdx.x * TX + tx) + (i64)n * (blockIdx.y * TY + ty) + n2 * k;
+      Stencil<float> st;
+      st.c = P[c]; st.ip = P[c + 1]; st.im = P[c - 1]; st.jp = P[c + W]; st.jm = P[c - W];
+      st.kp = Kp[c]; st.km = Km[c];
+      st.ppk = P[c + 1 + W]; st.mpk = P[c - 1 + W]; st.pmk = P[c + 1 - W]; st.mmk = P[c - 1 - W];
+      st.jpkp = Kp[c + W]; st.jmkp = Kp[c - W]; st.jpkm = Km[c + W]; st.jmkm = Km[c - W];
+      st.ipkp = Kp[c + 1]; st.imkp = Kp[c - 1]; st.ipkm = Km[c + 1]; st.imkm = Km[c - 1];
+      st.f1c = F1[c]; st.f1ip = F1[c + 1]; st.f1im = F1[c - 1];
+      st.f4c = F4[c]; st.f4jp = F4[c + W]; st.f4jm = F4[c - W];
+      st.f2jp = F2[c + W]; st.f2jm = F2[c - W]; st.f2ip = F2[c + 1]; st.f2im = F2[c - 1];
+      st.f5jp = F5[c + W]; st.f5jm = F5[c - W];
+      st.f3ip = F3[c + 1]; st.f3im = F3[c - 1];
+      st.f6c = F6[ci]; st.f6kp = F6p[ci]; st.f6km = F6m[ci];
+      st.f5kp = F5p[c]; st.f5km = F5m[c];
+      st.f3kp = F3p[c]; st.f3km = F3m[c];
+      float tdiag, t1, t2;
+      op_eval(st, tdiag, t1, t2);
+      float v;
+      if (MODE == 0)
+        v = R[ci] - (t1 + t2 + tdiag * st.c) * di2;
+      else
+        v = (t1 + t2 + tdiag * st.c) * di2;
+      if (out) out[gt] = v;
+      const auto vb = abs_bits(v);
+      mb = vb > mb ? vb : mb;
+    }
+    cp_async_wait_all();
+    __syncthreads();
+  }
+  if (maxbits) block_max_commit(from_bits(mb), maxbits);
+}
+
 // Full-weighting restriction of the residual with the reference's
 // accumulation order (calcresid gauss1.f90:819-859 as scheduled by r1lax):
 // coarse plane `special` adds its own-plane part first, all others their

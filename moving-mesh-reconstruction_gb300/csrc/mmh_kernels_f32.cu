@@ -13,6 +13,7 @@ static std::mutex g_tile_mu;
 static signed char g_tile[64][16];
 static bool g_tile_init = false;
 std::atomic<int> gs_tile_override{-1};
+std::atomic<int> stencil_march_pin{-1};
 
 int gs_tile_choice(int n, const float* phi, const float* rhs, const float* coef, float dx2, float* scratch,
                    cudaStream_t s) {

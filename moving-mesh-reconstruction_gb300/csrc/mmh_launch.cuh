@@ -149,13 +149,35 @@ void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nswe
         }
 }
 
+// The marching FP32 stencil (k_stencil_march) for grids of 64 and up, unless
+// pinned to one plane per CTA (mmh_stencil_pin).
+extern std::atomic<int> stencil_march_pin;
+template <int MODE>
+inline void launch_stencil_march(const float* phi, const float* rhs, const float* coef, int n, float di2, float* out,
+                                 unsigned long long* maxbits, cudaStream_t s) {
+  static std::atomic<unsigned long long> attr_done{0};
+  const int smem = (int)(sizeof(float) * MarchGeom::WORDS);
+  smem_attr_once(k_stencil_march<MODE>, smem, attr_done);
+  k_stencil_march<MODE><<<dim3(n / MarchGeom::TX, n / MarchGeom::TY, n / kMarchKC), 256, smem, s>>>(
+      phi, rhs, coef, n, di2, out, maxbits);
+}
+inline bool use_march(int n) { return n >= 64 && stencil_march_pin.load(std::memory_order_relaxed) != 0; }
+
 template <class T>
 void launch_residual(const T* phi, const T* rhs, const T* coef, int n, T dx, T* r, float* r32,
                      unsigned long long* maxbits, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
   T di2 = T(1) / (dx * dx);
   prof_begin(kk<T>(KK_RESIDUAL), s, n3, n);
-  if (n >= 32)
+  bool done = false;
+  if constexpr (std::is_same<T, float>::value) {
+    if (use_march(n) && r32 == nullptr) {
+      launch_stencil_march<0>(phi, rhs, coef, n, di2, r, maxbits, s);
+      done = true;
+    }
+  }
+  if (done) {
+  } else if (n >= 32)
     k_stencil_plane<T, 0><<<dim3(n / 32, n / 16, n), 256, 0, s>>>(phi, rhs, coef, n, di2, r, r32, maxbits);
   else
     k_residual<T><<<grid_of(n3, kBlock), kBlock, 0, s>>>(phi, rhs, coef, n, di2, r, r32, maxbits);

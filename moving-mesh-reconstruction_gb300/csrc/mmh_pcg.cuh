@@ -4,7 +4,7 @@
 // exact for FP32 vectors) is scaled by 2^(96-E), 2^E > max|a|*max|b|,
 // truncated to a 128-bit integer and summed with two 64-bit atomics.
 #pragma once
-#include "mmh_kernels.cuh"
+#include "mmh_launch.cuh"
 
 namespace mmh {
 
@@ -96,7 +96,15 @@ template <class T>
 void launch_apply(const T* p, const T* coef, int n, T dx, T* q, unsigned long long* qbits, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
   prof_begin(kk<T>(KK_APPLY), s, n3, n);
-  if (n >= 32)
+  bool done = false;
+  if constexpr (std::is_same<T, float>::value) {
+    if (use_march(n)) {
+      launch_stencil_march<1>(p, nullptr, coef, n, T(1) / (dx * dx), q, qbits, s);
+      done = true;
+    }
+  }
+  if (done) {
+  } else if (n >= 32)
     k_stencil_plane<T, 1><<<dim3(n / 32, n / 16, n), 256, 0, s>>>(p, nullptr, coef, n, T(1) / (dx * dx), q, nullptr,
                                                                  qbits);
   else

@@ -1573,6 +1573,12 @@ int mmh_gs_tile_pin(int shape) {
   return MMH_OK;
 }
 
+int mmh_stencil_pin(int kind) {
+  if (kind < -1 || kind > 1) return MMH_ERR_ARG;
+  mmh::stencil_march_pin.store(kind);
+  return MMH_OK;
+}
+
 int mmh_gs_tile(int n, int* tx, int* ty) {
   if (!tx || !ty) return MMH_ERR_ARG;
   *tx = *ty = 0;

@@ -44,7 +44,7 @@ EXPORTS = (
     "mmh_relax_noalloc_f64", "mmh_batch_run", "mmh_calcdefp_adjoint_f64",
     "mmh_relaxing_adjoint_f64", "mmh_iterate_adjoint_f64", "mmh_state_stats",
     "mmh_power_spectrum_f64", "mmh_haloden", "mmh_coarsen",
-    "mmh_column_density", "mmh_gridfigure", "mmh_keep_masks", "mmh_masks", "mmh_gs_tile_pin", "mmh_gs_tile",
+    "mmh_column_density", "mmh_gridfigure", "mmh_keep_masks", "mmh_masks", "mmh_gs_tile_pin", "mmh_gs_tile", "mmh_stencil_pin",
 )
 
 # kernel kinds for the timing hooks
@@ -180,6 +180,12 @@ def gs_tile_pin(shape):
     """Pin the FP32 plane Gauss-Seidel tile shape (0..3) for every grid; -1
     returns to timing the shapes per grid size."""
     _chk(lib().mmh_gs_tile_pin(int(shape)), "gs_tile_pin")
+
+
+def stencil_pin(kind):
+    """FP32 residual/operator stencil: -1 default (marching from 64^3 up), 0
+    one plane per CTA, 1 marching."""
+    _chk(lib().mmh_stencil_pin(int(kind)), "stencil_pin")
 
 
 def gs_tile(n):

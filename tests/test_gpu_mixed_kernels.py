@@ -209,3 +209,35 @@ def test_fp32_sweep_tile_shapes_agree_bit_for_bit(mmh, oracle, fields):
     assert all(r == out[0][1] for _, r in out[1:4])
     print("tile kept for 128^3:", chosen)
     assert chosen in [(32, 16), (64, 8), (16, 32), (32, 8)]
+
+
+@pytest.mark.parametrize("n", [64, 128])
+def test_fp32_stencil_marching_agrees_bit_for_bit(mmh, fields, n):
+    """The marching FP32 residual / operator stencil (a CTA walks 8 planes of
+    its tile column and copies the next plane while computing one) gives the
+    bits of the one-plane-per-CTA kernel, each pinned in turn: a relax with
+    its residual norm and restricted residual (iresidopt 3), and a whole
+    mixed solve (V-cycle residuals and the conjugate-gradient operator)."""
+    defpot = smooth_field(n, 0.05, 17)
+    _, u = fields.initial_state(n, sigma=0.5, seed=18)
+    rho = np.asfortranarray(u[0])
+    rng = np.random.default_rng(19)
+    rhs = np.asfortranarray(rng.standard_normal((n, n, n)))
+    phi0 = np.asfortranarray(rng.standard_normal((n, n, n)))
+    rhs0 = np.asfortranarray(rng.standard_normal((n, n, n)) * 0.01)
+    out = {}
+    try:
+        with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL, tol=1e-8, max_cycles=200) as ctx:
+            for kind in (0, 1):
+                mmh.stencil_pin(kind)
+                b = phi0.copy(order="F")
+                resid, rinf = ctx.relax(b, rhs, defpot, rho, 1.0, 2, 19)
+                ug = np.zeros((n, n, n), order="F")
+                rg = rhs0.copy(order="F")
+                d = ctx.multigrid(ug, rg, defpot, u, 1.0, n, n, n, 5)
+                out[kind] = (b, resid, rinf, ug, d["vcycles"], d["resid_rel"])
+    finally:
+        mmh.stencil_pin(-1)
+    print(f"{n}^3: solve {out[1][4]} cycles to {out[1][5]:.2e}")
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
