@@ -34,7 +34,8 @@ template <class T>
 void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_t s, bool fast_div = false);
 void launch_residual_fma(const double* phi, const double* rhs, const double* coef, int n, double dx, float* r32,
                          unsigned long long* maxbits, cudaStream_t s);
-template <class T> void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, T* scratch, cudaStream_t s);
+template <class T> void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, T* scratch, cudaStream_t s,
+                                          bool zero_init = false);
 // FP32 plane-kernel tile autotuning: the shape pinned for every grid (-1:
 // timed per grid size and device), and the shape chosen for n (-1: none yet)
 constexpr int kGsShapes = 4;
@@ -139,6 +140,10 @@ void launch_smooth_sep(double* in, int n, double* out, cudaStream_t s);
 // float-float outer loop of the mixed form (mmh_kernels_f64.cu): a double
 // buffer reinterpreted as (hi, lo) float pairs, in place
 void launch_ff_split(double* a, i64 count, cudaStream_t s);
+// r32 = b rounded through its float-float split (the outer residual of a
+// zero guess), max |r32| into maxbits
+void launch_ff_rhs32(const double* b, i64 count, float* r32, unsigned long long* maxbits, cudaStream_t s);
+void launch_set_u64(unsigned long long* p, unsigned long long v, cudaStream_t s);
 void launch_ff_join(double* a, i64 count, cudaStream_t s);
 void launch_ff_add_f(double* x, const float* e, i64 count, cudaStream_t s);
 void launch_ff_sub_mean(double* x, const double* mean, i64 count, cudaStream_t s);

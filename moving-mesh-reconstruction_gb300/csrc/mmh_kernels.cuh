@@ -470,7 +470,12 @@ __device__ __forceinline__ double2 gs_get(const double* f, int sw, int h2) { ret
 // so no tile can read a halo that another tile has already updated.  Needs
 // n >= TX+8 and n >= TY+8.  The register budget of 4 CTAs per SM lets the
 // compiler keep the tile's global loads in flight together.
-template <class T, int TX, int TY>
+// Z = 1: the planes being updated are zero (src is not read); Z = 2: the
+// neighbour planes are zero too (nbr is not read either).  The first sweep
+// from a zero field runs its half sweeps with Z = 2 and Z = 1, in place: no
+// tile reads a plane that the half sweep writes.  A loaded zero and the
+// constant zero give the same results.
+template <class T, int TX, int TY, int Z = 0>
 __global__ void __launch_bounds__(256, 4) k_gs_plane(const T* __restrict__ src, const T* __restrict__ nbr,
                                                      T* __restrict__ dst, const T* __restrict__ rhs,
                                                      const T* __restrict__ coef, int n, T dx2, int kpar) {
@@ -521,14 +526,18 @@ __global__ void __launch_bounds__(256, 4) k_gs_plane(const T* __restrict__ src, 
     const i64 b = (i64)gi + (i64)n * gj;
     const i64 cP = (b + n2 * k) / VW, cm = (b + n2 * kmn) / VW, cp = (b + n2 * kpn) / VW;
     V v[8];
-    v[0] = vsrc[cP];
-    v[1] = vnbr[cm];
-    v[2] = vnbr[cp];
+    if (Z == 0) v[0] = vsrc[cP];
+    else v[0] = V{};
+    if (Z < 2) {
+      v[1] = vnbr[cm];
+      v[2] = vnbr[cp];
+    }
 #pragma unroll
     for (int f = 0; f < 5; ++f) v[3 + f] = vcoef[f * nv3 + cP];
     const int sw = G::word(x0, y);
 #pragma unroll
-    for (int f = 0; f < 8; ++f) gs_put(sm + f * SF, sw, H2, v[f]);
+    for (int f = 0; f < 8; ++f)
+      if (Z < 2 || (f != 1 && f != 2)) gs_put(sm + f * SF, sw, H2, v[f]);
   }
   __syncthreads();
   T* sP = sm;
@@ -562,10 +571,14 @@ __global__ void __launch_bounds__(256, 4) k_gs_plane(const T* __restrict__ src, 
       st.f3km = cur[4]; st.f5km = cur[5]; st.f3kp = cur[6]; st.f5kp = cur[7];
       const T r = cur[0];
       st.c = sP[c]; st.ip = sP[cxp]; st.im = sP[cxm]; st.jp = sP[cyp]; st.jm = sP[cym];
-      st.kp = sKp[c]; st.km = sKm[c];
       st.ppk = sP[cxp + oyp]; st.mpk = sP[cxm + oyp]; st.pmk = sP[cxp + oym]; st.mmk = sP[cxm + oym];
-      st.jpkp = sKp[cyp]; st.jmkp = sKp[cym]; st.jpkm = sKm[cyp]; st.jmkm = sKm[cym];
-      st.ipkp = sKp[cxp]; st.imkp = sKp[cxm]; st.ipkm = sKm[cxp]; st.imkm = sKm[cxm];
+      if (Z < 2) {
+        st.kp = sKp[c]; st.km = sKm[c];
+        st.jpkp = sKp[cyp]; st.jmkp = sKp[cym]; st.jpkm = sKm[cyp]; st.jmkm = sKm[cym];
+        st.ipkp = sKp[cxp]; st.imkp = sKp[cxm]; st.ipkm = sKm[cxp]; st.imkm = sKm[cxm];
+      } else {
+        st.kp = st.km = st.jpkp = st.jmkp = st.jpkm = st.jmkm = st.ipkp = st.imkp = st.ipkm = st.imkm = T(0);
+      }
       st.f1c = F1[c]; st.f1ip = F1[cxp]; st.f1im = F1[cxm];
       st.f4c = F4[c]; st.f4jp = F4[cyp]; st.f4jm = F4[cym];
       st.f2jp = F2[cyp]; st.f2jm = F2[cym]; st.f2ip = F2[cxp]; st.f2im = F2[cxm];

@@ -1081,6 +1081,31 @@ __global__ void __launch_bounds__(256) k_residual_ff(const float2* __restrict__ 
   if (maxbits) block_max_commit(m, maxbits);
 }
 
+// The outer residual of a zero guess, b itself, as the inner solve's FP32
+// right-hand side: what k_residual_ff gives for phi = 0 (b split into a
+// float-float pair and rounded, hi + lo), with max |r| into maxbits.
+__global__ void k_ff_rhs32(const double* __restrict__ b, i64 count, float* __restrict__ r32,
+                           unsigned long long* maxbits) {
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  float m = 0.0f;
+  if (t < count) {
+    const FF v = ff_of_bits(b[t]);
+    const float r = __fadd_rn(v.hi, v.lo);
+    r32[t] = r;
+    m = fabsf(r);
+  }
+  block_max_commit(m, maxbits);
+}
+void launch_ff_rhs32(const double* b, i64 count, float* r32, unsigned long long* maxbits, cudaStream_t s) {
+  k_ff_rhs32<<<grid_of(count, kBlock), kBlock, 0, s>>>(b, count, r32, maxbits);
+  count_launch();
+}
+__global__ void k_set_u64(unsigned long long* p, unsigned long long v) { *p = v; }
+void launch_set_u64(unsigned long long* p, unsigned long long v, cudaStream_t s) {
+  k_set_u64<<<1, 1, 0, s>>>(p, v);
+  count_launch();
+}
+
 void launch_ff_split(double* a, i64 count, cudaStream_t s) {
   k_ff_split<<<grid_of(count, kBlock), kBlock, 0, s>>>(a, count);
   count_launch();

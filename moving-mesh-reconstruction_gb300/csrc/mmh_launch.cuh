@@ -50,28 +50,30 @@ struct GsShape {
 };
 constexpr GsShape kGsShape[kGsShapes] = {{32, 16}, {64, 8}, {16, 32}, {32, 8}};
 
-template <class T, int TX, int TY>
+template <class T, int TX, int TY, int Z = 0>
 void gs_plane_launch(const T* src, const T* nbr, T* dst, const T* rhs, const T* coef, int n, T dx2, int kpar,
                      cudaStream_t s) {
   const size_t smem = sizeof(T) * GsGeom<T, TX, TY>::WORDS;
   static std::atomic<unsigned long long> attr_done{0};
-  smem_attr_once(k_gs_plane<T, TX, TY>, (int)smem, attr_done);
-  k_gs_plane<T, TX, TY><<<dim3(n / TX, n / TY, n / 2), 256, smem, s>>>(src, nbr, dst, rhs, coef, n, dx2, kpar);
+  smem_attr_once(k_gs_plane<T, TX, TY, Z>, (int)smem, attr_done);
+  k_gs_plane<T, TX, TY, Z><<<dim3(n / TX, n / TY, n / 2), 256, smem, s>>>(src, nbr, dst, rhs, coef, n, dx2, kpar);
 }
 
 // one half sweep with tile shape v (FP64: always (32, 8))
-template <class T>
+// (the zero-field variants Z = 1, 2 exist for FP32 only)
+template <class T, int Z = 0>
 void gs_plane_half(int v, const T* src, const T* nbr, T* dst, const T* rhs, const T* coef, int n, T dx2, int kpar,
                    cudaStream_t s) {
   if constexpr (std::is_same<T, double>::value) {
+    static_assert(Z == 0, "FP64 sweeps read their fields");
     (void)v;
     gs_plane_launch<T, 32, 8>(src, nbr, dst, rhs, coef, n, dx2, kpar, s);
   } else {
     switch (v) {
-      case 1: gs_plane_launch<T, 64, 8>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
-      case 2: gs_plane_launch<T, 16, 32>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
-      case 3: gs_plane_launch<T, 32, 8>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
-      default: gs_plane_launch<T, 32, 16>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
+      case 1: gs_plane_launch<T, 64, 8, Z>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
+      case 2: gs_plane_launch<T, 16, 32, Z>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
+      case 3: gs_plane_launch<T, 32, 8, Z>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
+      default: gs_plane_launch<T, 32, 16, Z>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
     }
   }
 }
@@ -90,19 +92,42 @@ int gs_tile_choice(int n, const float* phi, const float* rhs, const float* coef,
 // nsweeps 8-colour Gauss-Seidel sweeps.  Grids of 64^3 and up run one fused
 // launch per half sweep (all in-plane colours of every plane of one parity);
 // smaller grids run one launch per colour.
+// zero_init: phi holds no field yet and the sweeps start from zero (FP32
+// grids of 64^3 and up run the first sweep in place without reading phi;
+// elsewhere phi is zeroed first).
 template <class T>
-void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, T* scratch, cudaStream_t s) {
+void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, int n, T dx, int nsweeps, T* scratch, cudaStream_t s,
+                      bool zero_init) {
   i64 h3 = (i64)(n / 2) * (n / 2) * (n / 2);
   T dx2 = dx * dx;
+  int sw0 = 0;
+  if (zero_init) {
+    bool done = false;
+    if constexpr (std::is_same<T, float>::value) {
+      if (n >= 64 && nsweeps > 0) {
+        const int v = gs_tile_choice(n, phi, rhs, coef, dx2, scratch, s);
+        prof_begin(kk<T>(KK_GS), s, 4 * h3, n);
+        gs_plane_half<T, 2>(v, phi, phi, phi, rhs, coef, n, dx2, 0, s);
+        prof_end(kk<T>(KK_GS), s, n);
+        prof_begin(kk<T>(KK_GS), s, 4 * h3, n);
+        gs_plane_half<T, 1>(v, phi, phi, phi, rhs, coef, n, dx2, 1, s);
+        prof_end(kk<T>(KK_GS), s, n);
+        count_launch(2);
+        sw0 = 1;
+        done = true;
+      }
+    }
+    if (!done) launch_fill<T>(phi, (i64)n * n * n, T(0), s);
+  }
   if (n >= 64) {
     int v = 0;
     if constexpr (std::is_same<T, float>::value) {
-      if (nsweeps > 0) v = gs_tile_choice(n, phi, rhs, coef, dx2, scratch, s);
+      if (nsweeps > sw0) v = gs_tile_choice(n, phi, rhs, coef, dx2, scratch, s);
     }
     // double buffer: a sweep reads a and leaves the swept field in b
     T* a = phi;
     T* b = scratch;
-    for (int sw = 0; sw < nsweeps; ++sw) {
+    for (int sw = sw0; sw < nsweeps; ++sw) {
       for (int kpar = 0; kpar < 2; ++kpar) {
         prof_begin(kk<T>(KK_GS), s, 4 * h3, n);
         gs_plane_half<T>(v, a, kpar == 0 ? a : b, b, rhs, coef, n, dx2, kpar, s);
@@ -301,7 +326,7 @@ void launch_usum_flag(const unsigned long long* acc, int* flag, cudaStream_t s) 
 
 #define MMH_INSTANTIATE(T)                                                                                          \
   template void launch_metric<T>(const T*, const T*, int, T, T*, cudaStream_t, bool);                             \
-  template void launch_gs_sweeps<T>(T*, const T*, const T*, int, T, int, T*, cudaStream_t);                         \
+  template void launch_gs_sweeps<T>(T*, const T*, const T*, int, T, int, T*, cudaStream_t, bool);                         \
   template void launch_residual<T>(const T*, const T*, const T*, int, T, T*, float*, unsigned long long*,          \
                                    cudaStream_t);                                                                   \
   template void launch_restrict_resid<T>(const T*, int, int, T*, cudaStream_t);                                   \

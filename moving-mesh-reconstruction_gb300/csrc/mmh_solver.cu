@@ -142,6 +142,8 @@ struct mmh_ctx {
   // the finest metric of the resident def is built (calcdefp's mixed pass 1
   // reads its det); the next multigrid call at level 0 uses it as it is
   bool levels_ready = false;
+  // the next solve starts from a zero guess (calcdefp zeroes defp before it)
+  bool u_zero = false;
   uint8_t* mask(int q) { return keep_masks ? masks + q * n3 : nullptr; }
 
   double* defp() { return h64.u[0]; }
@@ -203,12 +205,13 @@ Hier<float>& hier<float>(mmh_ctx* c) { return c->h32; }
 
 // relax(): nrelax 8-colour sweeps, then residual (mode 3: full weighting into
 // rhs[l+1] and max norm; mode 2: max norm only; mode 0: none) into *maxslot.
+// zero_init: H.u[l] holds no field yet; the sweeps start from zero.
 template <class T>
-int relax_level(mmh_ctx* c, int l, int nrelax, int mode, unsigned long long* maxslot) {
+int relax_level(mmh_ctx* c, int l, int nrelax, int mode, unsigned long long* maxslot, bool zero_init = false) {
   Hier<T>& H = hier<T>(c);
   int n = c->nl[l];
   T dx = T(double(1 << l));
-  launch_gs_sweeps<T>(H.u[l], H.rhs[l], H.coef[l], n, dx, nrelax, H.r[l], c->s);
+  launch_gs_sweeps<T>(H.u[l], H.rhs[l], H.coef[l], n, dx, nrelax, H.r[l], c->s, zero_init);
   if (mode == 0) return MMH_OK;
   CK(cudaMemsetAsync(maxslot, 0, 8, c->s));
   launch_residual<T>(H.u[l], H.rhs[l], H.coef[l], n, dx, mode == 3 ? H.r[l] : (T*)nullptr, nullptr, maxslot, c->s);
@@ -240,8 +243,10 @@ int guard_or_zerosum(mmh_ctx* c, int l, double margin, double floor_, bool guard
 int vcycle_fp64(mmh_ctx* c, int l);
 
 // One V-cycle at level l (mgtemplate.f90:6-84; mg4 at multigrid.f90:94-121).
+// u_zero: the level's correction starts from zero (H.u[l] is not yet set);
+// the FP32 cycle then skips zeroing it where its first sweep runs from zero.
 template <class T>
-int vcycle(mmh_ctx* c, int l) {
+int vcycle(mmh_ctx* c, int l, bool u_zero = false) {
   Hier<T>& H = hier<T>(c);
   int n = c->nl[l];
   bool ref = c->cfg.schedule == MMH_SCHED_REF;
@@ -251,6 +256,9 @@ int vcycle(mmh_ctx* c, int l) {
   // diagnostics only; the preconditioner of the tolerance schedule without
   // guards skips them
   const int post = (guard || c->cfg.schedule != MMH_SCHED_TOL) ? 2 : 0;
+  const bool zfirst = u_zero && std::is_same<T, float>::value && n > 4;
+  if (u_zero && !zfirst && !(n == 4 && std::is_same<T, float>::value && c->coarse_inv && !guard))
+    launch_fill<T>(H.u[l], (i64)n * n * n, T(0), c->s);
   if (n == 4) {
     if constexpr (std::is_same<T, float>::value) {
       Hier<float>& F = c->h32;
@@ -274,10 +282,8 @@ int vcycle(mmh_ctx* c, int l) {
   }
   int nrelax = ref ? 4 * c->n / n : c->cfg.nu1;
   int nrelax2 = ref ? 4 * c->n / n : c->cfg.nu2;
-  RET(relax_level<T>(c, l, nrelax, 3, &c->sc->r1bits[l]));
-  int nh = c->nl[l + 1];
-  launch_fill<T>(H.u[l + 1], (i64)nh * nh * nh, T(0), c->s);
-  RET(vcycle<T>(c, l + 1));
+  RET(relax_level<T>(c, l, nrelax, 3, &c->sc->r1bits[l], zfirst));
+  RET(vcycle<T>(c, l + 1, true));
   launch_prolong_add<T>(H.u[l], H.u[l + 1], n, c->s);
   RET(relax_level<T>(c, l, nrelax2, post, &c->sc->errbits[l]));
   return guard_or_zerosum<T>(c, l, 1.0, -HUGE_VAL, guard);
@@ -343,8 +349,7 @@ int precond(mmh_ctx* c, int l0, unsigned long long* zbits) {
   Hier<T>& H = hier<T>(c);
   int n = c->nl[l0];
   i64 n3 = (i64)n * n * n;
-  launch_fill<T>(H.u[l0], n3, T(0), c->s);
-  RET(vcycle<T>(c, l0));
+  RET(vcycle<T>(c, l0, true));
   CK(cudaMemsetAsync(zbits, 0, 8, c->s));
   launch_absmax<T>(H.u[l0], n3, zbits, c->s);
   return MMH_OK;
@@ -408,9 +413,11 @@ void pcg_dot(mmh_ctx* c, const T* a, const T* b, i64 n3, const unsigned long lon
     launch_dot<T>(a, b, n3, abits, bbits, acc, c->s);
 }
 
+// x0_bmax >= 0: x is zero and H.rhs[l0] already holds b, whose max |b| is
+// x0_bmax (the initial residual is b itself: no stencil pass).
 template <class T>
 int pcg_core(mmh_ctx* c, int l0, double dx, T* x, const T* b, T* p, T* q, double bn, double tol, int maxit,
-             int* iters, double* rel_out, double* r0_out) {
+             int* iters, double* rel_out, double* r0_out, double x0_bmax = -1.0) {
   Hier<T>& H = hier<T>(c);
   int n = c->nl[l0];
   i64 n3 = (i64)n * n * n;
@@ -418,10 +425,18 @@ int pcg_core(mmh_ctx* c, int l0, double dx, T* x, const T* b, T* p, T* q, double
   T* r = H.rhs[l0];
   T* z = H.u[l0];
   CK(cudaMemsetAsync(P, 0, sizeof(PcgDev), c->s));
-  launch_residual<T>(x, b, H.coef[l0], n, (T)dx, r, nullptr, &P->rbits, c->s);
-  RET(pull_scal(c));
-  double rel = bits_to_double(c->hsc->pcg.rbits) / bn;
-  *r0_out = bits_to_double(c->hsc->pcg.rbits);
+  double rmax0 = x0_bmax;
+  if (x0_bmax >= 0.0) {
+    unsigned long long bits = 0;
+    std::memcpy(&bits, &x0_bmax, 8);
+    launch_set_u64(&P->rbits, bits, c->s);
+  } else {
+    launch_residual<T>(x, b, H.coef[l0], n, (T)dx, r, nullptr, &P->rbits, c->s);
+    RET(pull_scal(c));
+    rmax0 = bits_to_double(c->hsc->pcg.rbits);
+  }
+  double rel = rmax0 / bn;
+  *r0_out = rmax0;
   int it = 0;
   int status = MMH_OK;
   if (rel > tol) {
@@ -525,9 +540,21 @@ int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_
     auto outer_residual = [&](float* r32, double* r) {
       return ff ? true_residual_ff(c, l0, dx, c->px, c->pb, r32, r) : true_residual(c, l0, dx, c->px, c->pb, r32, r);
     };
+    // A solve from a zero guess (calcdefp's) starts from the residual b itself.
+    const bool x0 = c->u_zero && ff;
+    c->u_zero = false;
     double rmax = 0.0;
     for (int outer = 0;; ++outer) {
-      RET(outer_residual(c->pb32, &rmax));
+      // the outer residual in FP32 is the inner solve's right-hand side and
+      // initial residual (its correction starts from zero)
+      if (outer == 0 && x0) {
+        CK(cudaMemsetAsync(&c->sc->resbits, 0, 8, c->s));
+        launch_ff_rhs32(c->pb, n3, c->h32.rhs[l0], &c->sc->resbits, c->s);
+        RET(pull_scal(c));
+        rmax = bits_to_double(c->hsc->resbits);
+      } else {
+        RET(outer_residual(c->h32.rhs[l0], &rmax));
+      }
       rel = rmax / rn;
       if (outer == 0) *r1_out = rmax;
       if (!(rel == rel)) return MMH_ERR_NAN;
@@ -543,7 +570,7 @@ int pcg_level(mmh_ctx* c, int l0, double dx, double rn, int* iters, double* rel_
       // the outer tolerance still needs (with a margin) when that is less
       const double inner_tol = std::max(kInnerTol, 0.3 * c->cfg.tol * rn / rmax);
       int st = pcg_core<float>(c, l0, dx, c->pe32, c->pb32, c->pp32, c->pq32, rmax, inner_tol, kInnerMax, &it, &rin,
-                               &r0);
+                               &r0, rmax);
       if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
       total += it;
       if (ff)
@@ -761,7 +788,9 @@ int calcdefp_dev(mmh_ctx* c, double dtold, double dtaumesh, uint8_t* mx, uint8_t
   }
   smooth_step(c, c->scr, tmp);
   launch_fill<double>(defp, n3, 0.0, c->s);
+  c->u_zero = true;
   int st = multigrid_level(c, 0, 1.0, d);
+  c->u_zero = false;
   if (st != MMH_OK && st != MMH_ERR_DIVERGED) return st;
   smooth_step(c, defp, c->scr);
   smooth_step(c, c->scr, defp);
@@ -851,7 +880,9 @@ int calcdefp_fwd_keep(mmh_ctx* c, double dtold, double dtaumesh, const CalcKeep&
   launch_limiter_pass1(c->scr, c->def, c->rho, n, dtold, dtaumesh, &c->sc->lim, kp.mk, kp.mk + n3, c->s);
   smooth_step(c, c->scr, tmp);
   launch_fill<double>(defp, n3, 0.0, c->s);
+  c->u_zero = true;
   int st = multigrid_level(c, 0, 1.0, d);
+  c->u_zero = false;
   if (st != MMH_OK) return st;
   CK(cudaMemcpyAsync(kp.ratio, &c->sc->ratio, sizeof(double), cudaMemcpyDeviceToDevice, c->s));
   CK(cudaMemcpyAsync(kp.uf, defp, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->s));
@@ -888,7 +919,9 @@ int calcdefp_adj_core(mmh_ctx* c, double dtold, double dtaumesh, const CalcKeep&
   launch_smooth27<double>(c->scr, n, tmp, c->s);
   RET(zerosum<double>(c, tmp, n3));
   launch_fill<double>(defp, n3, 0.0, c->s);
+  c->u_zero = true;
   int st = multigrid_level(c, 0, 1.0, da);
+  c->u_zero = false;
   if (st != MMH_OK) return st;
   const double* lam = defp;
   launch_det<double>(c->def, n, 1.0, c->det, c->s);
