@@ -59,9 +59,9 @@ UNIT = "s/reconstruction"
 # and the 6 coefficients and writes r: 9 words per cell.
 ALG_WORDS = {"gs": 9, "residual": 9}
 # Words per updated cell the current kernel itself moves: one launch of the
-# fused plane kernel updates the planes of one parity and also reads phi and
-# coefficients 3, 5, 6 of the other parity's planes (4 more words per updated
-# cell).
+# fused plane kernel (or of the strips marching in y) updates the planes of
+# one parity and also reads phi and coefficients 3, 5, 6 of the other
+# parity's planes (4 more words per updated cell).
 KERNEL_WORDS = {"gs": 13, "residual": 9}
 KERNEL_NAME = {"gs32": "k_gs_plane<float,32,16>", "gs64": "k_gs_plane<double,32,8>",
                "res64": "k_residual<double>", "res32": "k_residual<float>"}
@@ -609,8 +609,14 @@ def main():
         alg_bytes = cells * ALG_WORDS[unit] * word
         achieved = alg_bytes / (pms / 1000.0) / 1e9
         kern_bytes = cells * KERNEL_WORDS[unit] * word
-        tr = traffic_from_profiles(KERNEL_NAME[kname])
-        roofline = {"kernel": f"{KERNEL_NAME[kname]} on the {n}^3 level",
+        kernel = KERNEL_NAME[kname]
+        if kname == "gs32":
+            tile = mmh.gs_tile(n)  # the shape the library kept for this grid
+            if tile:
+                kernel = (f"k_gs_strip<{tile[1] // 2}>" if tile[0] == 64 and tile[1] >= 32
+                          else f"k_gs_plane<float,{tile[0]},{tile[1]}>")
+        tr = traffic_from_profiles(kernel)
+        roofline = {"kernel": f"{kernel} on the {n}^3 level",
                     "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else peak_src,
                     "alg_words_per_cell": ALG_WORDS[unit],

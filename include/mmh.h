@@ -336,7 +336,9 @@ int mmh_iterate_adjoint_f64(mmh_ctx* ctx, int niter, int checkpoint_every, const
 /* ---- Gauss-Seidel tile tuning (no counterpart in the reference) -------- */
 /* The FP32 plane Gauss-Seidel kernel (the mixed form's smoother on grids of
  * 64^3 and up) has four tile shapes (TX x TY cells: 0 = 32x16, 1 = 64x8,
- * 2 = 16x32, 3 = 32x8).  All of them compute the same bits; the first sweep on
+ * 2 = 16x32, 3 = 32x8) and two strip lengths of the kernel that marches a
+ * 64-cell strip along y with the four colours as a wavefront (4 = 64x128,
+ * 5 = 64x256).  All of them compute the same bits; the first sweep on
  * a grid size and device outside a stream capture times those that fit (three
  * half sweeps each, phi untouched) and keeps the fastest.  mmh_gs_tile_pin
  * pins one shape for every grid instead (-1: back to timing); mmh_gs_tile

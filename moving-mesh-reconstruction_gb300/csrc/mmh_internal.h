@@ -38,7 +38,7 @@ template <class T> void launch_gs_sweeps(T* phi, const T* rhs, const T* coef, in
                                           bool zero_init = false);
 // FP32 plane-kernel tile autotuning: the shape pinned for every grid (-1:
 // timed per grid size and device), and the shape chosen for n (-1: none yet)
-constexpr int kGsShapes = 4;
+constexpr int kGsShapes = 6;
 extern std::atomic<int> gs_tile_override;
 // FP32 residual/operator stencil: -1 default (marching from 64^3 up), 0 one
 // plane per CTA, 1 marching

@@ -598,6 +598,220 @@ __global__ void __launch_bounds__(256, 4) k_gs_plane(const T* __restrict__ src, 
   }
 }
 
+// cp.async helpers: 16-byte global -> shared copies that bypass registers
+// (cp.async.cg: cached in L2 only), committed and waited for as groups.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// FP32 half sweep by strips marching in y (the same updates as k_gs_plane,
+// operand for operand, so the same bits).  A CTA owns a strip of 64 cells in
+// x and LY sub-rows (2 LY cell rows: sub-row r holds cell rows 2r and 2r+1) of
+// one plane P of parity kpar.  Within a plane the four colours (io, jo) run in
+// the order (0,0), (0,1), (1,0), (1,1); an update reads its 8 in-plane
+// neighbours, and only the colours before it may have been updated.  So the
+// colours can advance as a wavefront: at step s, colour q updates sub-row
+// s - lag[q] with lag = (0, 2, 3, 5).  With those lags every value a colour
+// reads is either final (an earlier colour's rows <= r + 1, finished at an
+// earlier step) or still old (a later colour's rows >= r - 1, not reached yet),
+// and no two updates of one step touch a value the other reads, so a step
+// needs one barrier instead of four per tile, and the recomputed halo of a
+// tile (a third of the updates for 32 x 16 tiles) shrinks to the strip's two
+// ends and one extra column of the first two colours.
+//   Shared memory keeps a ring of R sub-rows of the 8 fields read at
+// neighbours (phi of P, P-1, P+1, coefficients 1-5 of P), each sub-row split
+// into its four colours (sub-cells -2 .. 33: cells x0-4 .. x0+67), so a warp's
+// 32 lanes read 32 consecutive words.  Step s reads sub-rows s-5 .. s, writes
+// back sub-row s-6 (final since step s-1) and stores sub-row s+1 into the
+// ring from 16-byte loads issued at the start of the step.  The fields read
+// at the cell only (rhs, coefficient 6 of P, coefficients 3, 5, 6 of P+-1)
+// are loaded one step ahead.  (Loading two sub-rows ahead in alternating
+// register sets was slower: its registers allow 4 CTAs per SM instead of 5.)
+// Warps 0-3 take colours 0-3 (sub-cells 0..31); warp 4 takes sub-cell 32 of
+// colours 0 and 1 (x0+64, read by the last two colours at x0+63) and the
+// write-back.
+// Z as in k_gs_plane.  Needs n >= 64 and LY | n/2.
+struct StripGeom {
+  // the ring holds sub-rows s-6 .. s+1 at step s
+  static constexpr int SW = 64, PITCH = 36, ROWW = 4 * PITCH, R = 8, FW = R * ROWW, NF = 8;
+  static constexpr int WORDS = NF * FW, NT = 160, NSTAGE = NF * 2 * 18;
+  // ring offset of sub-cell s (-2 <= s < 34) of colour (io, jo) in ring slot sl
+  static __device__ __forceinline__ int at(int sl, int io, int jo, int s) {
+    return sl * ROWW + (2 * jo + io) * PITCH + s + 2;
+  }
+  static __device__ __forceinline__ int slot(int r) { return r & (R - 1); }
+};
+
+template <int IO, int JO, int Z>
+__device__ __forceinline__ float strip_update(const float* __restrict__ sm, int sl, int slm, int slp, int s,
+                                              const float* cur, float dx2) {
+  typedef StripGeom G;
+  const float* P = sm;
+  const float* Km = sm + G::FW;
+  const float* Kp = sm + 2 * G::FW;
+  const float* F1 = sm + 3 * G::FW;
+  const float* F2 = sm + 4 * G::FW;
+  const float* F3 = sm + 5 * G::FW;
+  const float* F4 = sm + 6 * G::FW;
+  const float* F5 = sm + 7 * G::FW;
+  // neighbours in x: the other io's sub-row; in y: the other jo's sub-row
+  // (slots of rows r-1 / r for jo = 0, r / r+1 for jo = 1)
+  const int sy_p = JO ? slp : sl, sy_m = JO ? sl : slm;
+  const int c = G::at(sl, IO, JO, s);
+  const int xp = G::at(sl, 1 - IO, JO, IO ? s + 1 : s), xm = G::at(sl, 1 - IO, JO, IO ? s : s - 1);
+  const int yp = G::at(sy_p, IO, 1 - JO, s), ym = G::at(sy_m, IO, 1 - JO, s);
+  const int ypxp = G::at(sy_p, 1 - IO, 1 - JO, IO ? s + 1 : s);
+  const int ypxm = G::at(sy_p, 1 - IO, 1 - JO, IO ? s : s - 1);
+  const int ymxp = G::at(sy_m, 1 - IO, 1 - JO, IO ? s + 1 : s);
+  const int ymxm = G::at(sy_m, 1 - IO, 1 - JO, IO ? s : s - 1);
+  Stencil<float> st;
+  st.f6c = cur[1]; st.f6km = cur[2]; st.f6kp = cur[3];
+  st.f3km = cur[4]; st.f5km = cur[5]; st.f3kp = cur[6]; st.f5kp = cur[7];
+  st.c = P[c]; st.ip = P[xp]; st.im = P[xm]; st.jp = P[yp]; st.jm = P[ym];
+  st.ppk = P[ypxp]; st.mpk = P[ypxm]; st.pmk = P[ymxp]; st.mmk = P[ymxm];
+  if (Z < 2) {
+    st.kp = Kp[c]; st.km = Km[c];
+    st.jpkp = Kp[yp]; st.jmkp = Kp[ym]; st.jpkm = Km[yp]; st.jmkm = Km[ym];
+    st.ipkp = Kp[xp]; st.imkp = Kp[xm]; st.ipkm = Km[xp]; st.imkm = Km[xm];
+  } else {
+    st.kp = st.km = st.jpkp = st.jmkp = st.jpkm = st.jmkm = st.ipkp = st.imkp = st.ipkm = st.imkm = 0.0f;
+  }
+  st.f1c = F1[c]; st.f1ip = F1[xp]; st.f1im = F1[xm];
+  st.f4c = F4[c]; st.f4jp = F4[yp]; st.f4jm = F4[ym];
+  st.f2jp = F2[yp]; st.f2jm = F2[ym]; st.f2ip = F2[xp]; st.f2im = F2[xm];
+  st.f5jp = F5[yp]; st.f5jm = F5[ym];
+  st.f3ip = F3[xp]; st.f3im = F3[xm];
+  float tdiag, t1, t2;
+  op_eval(st, tdiag, t1, t2);
+  return gs_div(cur[0] * dx2 - t1 - t2, tdiag);
+}
+
+template <int LY, int Z>
+__global__ void __launch_bounds__(160, 5) k_gs_strip(const float* __restrict__ src, const float* __restrict__ nbr,
+                                                     float* __restrict__ dst, const float* __restrict__ rhs,
+                                                     const float* __restrict__ coef, int n, float dx2, int kpar) {
+  typedef StripGeom G;
+  __shared__ __align__(16) float sm[G::WORDS];
+  const int m = n >> 1;
+  const i64 n2 = (i64)n * n, n3 = n2 * n;
+  const int x0 = blockIdx.x * G::SW, Y0 = blockIdx.y * LY, k = 2 * blockIdx.z + kpar;
+  const int kmn = wm(k, n), kpn = wp(k, n);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  auto wrow = [&](int r) { return r < 0 ? r + m : (r >= m ? r - m : r); };
+  const int rlast = Y0 + LY + 1;  // last staged sub-row
+  // ---- staging: item e of a sub-row is (field f, cell row jo, 16-byte group g);
+  // a thread's items are the same in every sub-row, so their global column
+  // pointers and shared offsets are formed once ----
+  const float* gcol[2];
+  int soff[2], gjo[2];
+  bool gld[2], gst[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int e = tid + h * G::NT;
+    const int f = e / 36, jo = (e / 18) & 1, g = e % 18;
+    gst[h] = e < G::NSTAGE && !(Z == 2 && (f == 1 || f == 2));
+    gld[h] = gst[h] && !(Z >= 1 && f == 0);
+    int x = x0 - 4 + 4 * g;
+    x += (x < 0) ? n : ((x >= n) ? -n : 0);
+    const float* base = f == 0 ? src + n2 * k
+                        : f == 1 ? nbr + n2 * kmn
+                        : f == 2 ? nbr + n2 * kpn
+                                 : coef + (i64)(f - 3) * n3 + n2 * k;
+    gcol[h] = base + x;
+    gjo[h] = jo;
+    soff[h] = f * G::FW + G::at(0, 0, jo, 2 * g - 2);
+  }
+  auto stage_load = [&](int r, float4(&ld)[2]) {
+    if (r > rlast) return;
+    const i64 yb = (i64)n * (2 * wrow(r));
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+      if (gld[h]) ld[h] = *reinterpret_cast<const float4*>(gcol[h] + yb + (gjo[h] ? n : 0));
+  };
+  auto stage_store = [&](int r, const float4(&ld)[2]) {
+    if (r > rlast) return;
+    const int so = G::slot(r) * G::ROWW;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (!gst[h]) continue;
+      const float4 v = (Z >= 1 && !gld[h]) ? make_float4(0.f, 0.f, 0.f, 0.f) : ld[h];
+      float* row = sm + soff[h] + so;
+      *reinterpret_cast<float2*>(row) = make_float2(v.x, v.z);
+      *reinterpret_cast<float2*>(row + G::PITCH) = make_float2(v.y, v.w);
+    }
+  };
+  // ---- this thread's cell: colour q, sub-cell sc ----
+  const int q = warp < 4 ? warp : lane;
+  const bool computes = warp < 4 || lane < 2;
+  const int sc = warp < 4 ? lane : 32;
+  const int io = q >> 1, jo = q & 1;
+  const int lag = q == 0 ? 0 : (q == 1 ? 2 : (q == 2 ? 3 : 5));
+  const int rlo = Y0 + (q < 2 ? -1 : 0), rhi = Y0 + (q == 0 ? LY + 1 : (q == 3 ? LY - 1 : LY));
+  int xc = x0 + 2 * sc + io;
+  xc -= (xc >= n) ? n : 0;
+  // the 8 fields read at the cell of sub-row r (nothing outside the colour's rows),
+  // from column pointers formed once
+  const float* cr = rhs + (xc + n2 * k + (jo ? n : 0));
+  const float* c6 = coef + (5 * n3 + xc + n2 * k + (jo ? n : 0));
+  const float* c6m = coef + (5 * n3 + xc + n2 * kmn + (jo ? n : 0));
+  const float* c6p = coef + (5 * n3 + xc + n2 * kpn + (jo ? n : 0));
+  const i64 d3m = (i64)3 * n3;       // coefficient 6 -> 3
+  const i64 d5 = n3;                 // coefficient 6 -> 5 is -n3
+  auto centre = [&](int r, float(&o)[8]) {
+    if (!computes || r < rlo || r > rhi) return;
+    const i64 yb = (i64)n * (2 * wrow(r));
+    o[0] = cr[yb]; o[1] = c6[yb]; o[2] = c6m[yb]; o[3] = c6p[yb];
+    o[4] = c6m[yb - d3m]; o[5] = c6m[yb - d5]; o[6] = c6p[yb - d3m]; o[7] = c6p[yb - d5];
+  };
+  const int s0 = Y0 - 1, s1 = Y0 + LY + 5;
+  float4 ld[2];
+  float pre[8];
+  // sub-rows Y0-2 and Y0-1 (read by the first step)
+  stage_load(Y0 - 2, ld);
+  stage_store(Y0 - 2, ld);
+  stage_load(Y0 - 1, ld);
+  stage_store(Y0 - 1, ld);
+  centre(s0 - lag, pre);
+  __syncthreads();
+  // step s: the colour updates of step s with the cell fields in pre (then
+  // refilled with those of the colour's next row), the write-back of sub-row
+  // s-6, and sub-row s+1 loaded and stored
+  for (int s = s0; s <= s1; ++s) {
+    stage_load(s + 1, ld);
+    const int r = s - lag;
+    if (computes && r >= rlo && r <= rhi) {
+      float cur[8];
+#pragma unroll
+      for (int z = 0; z < 8; ++z) cur[z] = pre[z];
+      centre(r + 1, pre);
+      const int sl = G::slot(r), slm = G::slot(r - 1), slp = G::slot(r + 1);
+      float v;
+      switch (q) {
+        case 0: v = strip_update<0, 0, Z>(sm, sl, slm, slp, sc, cur, dx2); break;
+        case 1: v = strip_update<0, 1, Z>(sm, sl, slm, slp, sc, cur, dx2); break;
+        case 2: v = strip_update<1, 0, Z>(sm, sl, slm, slp, sc, cur, dx2); break;
+        default: v = strip_update<1, 1, Z>(sm, sl, slm, slp, sc, cur, dx2); break;
+      }
+      sm[G::at(sl, io, jo, sc)] = v;
+    } else if (r + 1 == rlo) {
+      centre(rlo, pre);  // the colour starts at the next step
+    }
+    const int rb = s - 6;
+    if (warp == 4 && rb >= Y0 && rb < Y0 + LY) {
+      const int wj = lane >> 4, g = lane & 15, sl = G::slot(rb);
+      const float2 a = *reinterpret_cast<const float2*>(sm + G::at(sl, 0, wj, 2 * g));
+      const float2 b = *reinterpret_cast<const float2*>(sm + G::at(sl, 1, wj, 2 * g));
+      const i64 o = (i64)(x0 + 4 * g) + (i64)n * (2 * wrow(rb) + wj) + n2 * k;
+      *reinterpret_cast<float4*>(dst + o) = make_float4(a.x, b.x, a.y, b.y);
+    }
+    stage_store(s + 1, ld);
+    __syncthreads();
+  }
+}
+
 // Residual r = rhs - L[phi] on every cell (calcresid), max-norm into maxbits.
 // r may be null; r32 (float copy of the residual) may be null.  Contract
 // only names a separate instantiation: the translation unit that instantiates
@@ -722,15 +936,6 @@ __global__ void __launch_bounds__(256) k_stencil_plane(const T* __restrict__ phi
   }
   if (maxbits) block_max_commit(from_bits(mb), maxbits);
 }
-
-// cp.async helpers: 16-byte global -> shared copies that bypass registers
-// (cp.async.cg: cached in L2 only), committed and waited for as groups.
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // The FP32 residual (MODE 0: r = rhs - L[phi]) or operator (MODE 1: q = L[p])
 // of k_stencil_plane, with each CTA marching through KC consecutive planes of

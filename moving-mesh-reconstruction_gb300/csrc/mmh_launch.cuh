@@ -42,13 +42,22 @@ void launch_metric(const T* def, const T* rho, int n, T dx, T* coef, cudaStream_
 // Tile shapes of the fused plane kernel.  Every shape updates every cell with
 // the same operations in the same colour order, so the swept field is the
 // same bit for bit whichever runs; the shapes differ in halo overhead, active
-// threads per colour phase and shared memory.  FP32 levels try the shapes
-// below once per grid size and device and keep the fastest (gs_tile_choice);
-// FP64 levels keep (32, 8).
+// threads per colour phase and shared memory.  Shapes 4-5 are the strips of
+// 64 cells marching in y over 128 or 256 cell rows (k_gs_strip, LY = ty/2
+// sub-rows).  FP32 levels try the shapes below once per grid size and device
+// and keep the fastest (gs_tile_choice); FP64 levels keep (32, 8).
 struct GsShape {
   int tx, ty;
 };
-constexpr GsShape kGsShape[kGsShapes] = {{32, 16}, {64, 8}, {16, 32}, {32, 8}};
+constexpr GsShape kGsShape[kGsShapes] = {{32, 16}, {64, 8}, {16, 32}, {32, 8}, {64, 128}, {64, 256}};
+constexpr int kGsFirstStrip = 4;
+
+template <int LY, int Z>
+void gs_strip_launch(const float* src, const float* nbr, float* dst, const float* rhs, const float* coef, int n,
+                     float dx2, int kpar, cudaStream_t s) {
+  k_gs_strip<LY, Z><<<dim3(n / StripGeom::SW, (n / 2) / LY, n / 2), StripGeom::NT, 0, s>>>(src, nbr, dst, rhs, coef,
+                                                                                            n, dx2, kpar);
+}
 
 template <class T, int TX, int TY, int Z = 0>
 void gs_plane_launch(const T* src, const T* nbr, T* dst, const T* rhs, const T* coef, int n, T dx2, int kpar,
@@ -73,13 +82,19 @@ void gs_plane_half(int v, const T* src, const T* nbr, T* dst, const T* rhs, cons
       case 1: gs_plane_launch<T, 64, 8, Z>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
       case 2: gs_plane_launch<T, 16, 32, Z>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
       case 3: gs_plane_launch<T, 32, 8, Z>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
+      case 4: gs_strip_launch<64, Z>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
+      case 5: gs_strip_launch<128, Z>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
       default: gs_plane_launch<T, 32, 16, Z>(src, nbr, dst, rhs, coef, n, dx2, kpar, s); break;
     }
   }
 }
 
-// the kernel needs n >= TX + 8 and n >= TY + 8
-inline bool gs_shape_fits(int v, int n) { return n >= kGsShape[v].tx + 8 && n >= kGsShape[v].ty + 8; }
+// the plane kernel needs n >= TX + 8 and n >= TY + 8; the strips n >= 64 and
+// their LY sub-rows dividing the n/2 sub-rows of a plane
+inline bool gs_shape_fits(int v, int n) {
+  if (v >= kGsFirstStrip) return n >= 64 && (n / 2) % (kGsShape[v].ty / 2) == 0;
+  return n >= kGsShape[v].tx + 8 && n >= kGsShape[v].ty + 8;
+}
 
 // Tile shape for an FP32 grid of size n on the current device: the one
 // chosen before, else (outside a stream capture) each shape is timed on

@@ -177,8 +177,9 @@ def launch_count():
 
 
 def gs_tile_pin(shape):
-    """Pin the FP32 plane Gauss-Seidel tile shape (0..3) for every grid; -1
-    returns to timing the shapes per grid size."""
+    """Pin the FP32 plane Gauss-Seidel tile shape (0..3: tiles; 4..5: strips
+    marching in y) for every grid; -1 returns to timing the shapes per grid
+    size."""
     _chk(lib().mmh_gs_tile_pin(int(shape)), "gs_tile_pin")
 
 

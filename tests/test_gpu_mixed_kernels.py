@@ -179,36 +179,68 @@ def test_mixed_relax_fp32_sweeps(mmh, oracle, fields, n, nrelax, iopt):
         assert np.abs(rg - ro).max() <= 1e-4 * np.abs(ro).max()
 
 
-def test_fp32_sweep_tile_shapes_agree_bit_for_bit(mmh, oracle, fields):
-    """The four tile shapes of the FP32 plane kernel compute the same bits
-    (each pinned in turn); left to itself, the library times them on a grid's
-    first sweeps and reports the one it keeps."""
-    n, nrelax = 128, 2
+SHAPES = [(32, 16), (64, 8), (16, 32), (32, 8), (64, 128), (64, 256)]
+
+
+@pytest.mark.parametrize("n", [64, 128, 256])
+def test_fp32_sweep_tile_shapes_agree_bit_for_bit(mmh, oracle, fields, n):
+    """The tile shapes of the FP32 plane kernel and the strips marching in y
+    (shapes 4-6) compute the same bits, each pinned in turn: two sweeps with
+    their residual norm (relax), and a whole mixed solve, whose V-cycles run
+    the first sweep of every level from zero with the zero-field variants.
+    Left to itself, the library times the shapes on a grid's first sweeps and
+    reports the one it keeps."""
+    nrelax = 2
+    defpot = smooth_field(n, 0.05, 7)
+    _, u = fields.initial_state(n, sigma=0.5, seed=8)
+    rho = np.asfortranarray(u[0])
+    rng = np.random.default_rng(9)
+    rhs = np.asfortranarray(rng.standard_normal((n, n, n)))
+    phi0 = np.asfortranarray(rng.standard_normal((n, n, n)))
+    rhs0 = np.asfortranarray(rng.standard_normal((n, n, n)) * 0.01)
+    out = []
+    nfit = 0
+    try:
+        with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL, tol=1e-8, max_cycles=200) as ctx:
+            for shape, (tx, ty) in enumerate(SHAPES):
+                fits = n >= tx + 8 and n >= ty + 8 if shape < 4 else (n // 2) % (ty // 2) == 0
+                if not fits:
+                    continue
+                nfit += 1
+                mmh.gs_tile_pin(shape)
+                b = phi0.copy(order="F")
+                _, rinf = ctx.relax(b, rhs, defpot, rho, 1.0, nrelax, 18)
+                ug = np.zeros((n, n, n), order="F")
+                rg = rhs0.copy(order="F")
+                d = ctx.multigrid(ug, rg, defpot, u, 1.0, n, n, n, 5)
+                out.append((shape, b, rinf, ug, d["vcycles"]))
+            mmh.gs_tile_pin(-1)
+    finally:
+        mmh.gs_tile_pin(-1)
+    assert len(out) == nfit >= 2
+    for shape, b, rinf, ug, cyc in out[1:]:
+        assert np.array_equal(b, out[0][1]), shape
+        assert rinf == out[0][2], shape
+        assert np.array_equal(ug, out[0][3]), shape
+        assert cyc == out[0][4], shape
+    print(f"{n}^3: {len(out)} shapes agree; solve {out[0][4]} cycles")
+
+
+def test_fp32_tile_shape_kept_after_timing(mmh, fields):
+    """With no shape pinned, the first sweep on a grid times the shapes that
+    fit and keeps one of them."""
+    n = 128
     defpot = smooth_field(n, 0.05, 7)
     rho = fields.lognormal_density(n, sigma=0.5, seed=8)
     rng = np.random.default_rng(9)
     rhs = np.asfortranarray(rng.standard_normal((n, n, n)))
-    phi0 = np.asfortranarray(rng.standard_normal((n, n, n)))
-    out = []
-    try:
-        with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL) as ctx:
-            for shape in range(4):
-                mmh.gs_tile_pin(shape)
-                b = phi0.copy(order="F")
-                _, rinf = ctx.relax(b, rhs, defpot, rho, 1.0, nrelax, 18)
-                out.append((b, rinf))
-            mmh.gs_tile_pin(-1)
-            b = phi0.copy(order="F")
-            ctx.relax(b, rhs, defpot, rho, 1.0, nrelax, 18)
-            out.append((b, None))
-            chosen = mmh.gs_tile(n)
-    finally:
-        mmh.gs_tile_pin(-1)
-    for b, rinf in out[1:]:
-        assert np.array_equal(b, out[0][0])
-    assert all(r == out[0][1] for _, r in out[1:4])
+    b = np.asfortranarray(rng.standard_normal((n, n, n)))
+    mmh.gs_tile_pin(-1)
+    with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL) as ctx:
+        ctx.relax(b, rhs, defpot, rho, 1.0, 2, 18)
+        chosen = mmh.gs_tile(n)
     print("tile kept for 128^3:", chosen)
-    assert chosen in [(32, 16), (64, 8), (16, 32), (32, 8)]
+    assert chosen in SHAPES
 
 
 @pytest.mark.parametrize("n", [64, 128])
