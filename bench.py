@@ -63,6 +63,8 @@ ALG_WORDS = {"gs": 9, "residual": 9}
 # one parity and also reads phi and coefficients 3, 5, 6 of the other
 # parity's planes (4 more words per updated cell).
 KERNEL_WORDS = {"gs": 13, "residual": 9}
+# (TX, TY) of the FP32 Gauss-Seidel shapes: 0-3 tiles, 4-5 strips marching in y
+GS_SHAPES = [(32, 16), (64, 8), (16, 32), (32, 8), (64, 128), (64, 256)]
 KERNEL_NAME = {"gs32": "k_gs_plane<float,32,16>", "gs64": "k_gs_plane<double,32,8>",
                "res64": "k_residual<double>", "res32": "k_residual<float>"}
 
@@ -97,6 +99,8 @@ def parse():
     ap.add_argument("--adj-tol", type=float, default=1e-10)
     ap.add_argument("--batch-workers", type=int, default=8)
     ap.add_argument("--batch-niter", type=int, default=4)
+    ap.add_argument("--gs-shape", type=int, default=-1,
+                    help="pin the FP32 Gauss-Seidel shape (0-3 tiles, 4-5 strips); -1: the library times them")
     return ap.parse_args()
 
 
@@ -447,6 +451,7 @@ def main():
     import mmh
     import fields
 
+    mmh.gs_tile_pin(args.gs_shape)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -611,7 +616,8 @@ def main():
         kern_bytes = cells * KERNEL_WORDS[unit] * word
         kernel = KERNEL_NAME[kname]
         if kname == "gs32":
-            tile = mmh.gs_tile(n)  # the shape the library kept for this grid
+            # the pinned shape, or the one the library kept for this grid
+            tile = GS_SHAPES[args.gs_shape] if args.gs_shape >= 0 else mmh.gs_tile(n)
             if tile:
                 kernel = (f"k_gs_strip<{tile[1] // 2}>" if tile[0] == 64 and tile[1] >= 32
                           else f"k_gs_plane<float,{tile[0]},{tile[1]}>")

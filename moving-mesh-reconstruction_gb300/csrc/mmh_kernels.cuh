@@ -645,9 +645,11 @@ struct StripGeom {
   static __device__ __forceinline__ int slot(int r) { return r & (R - 1); }
 };
 
+// JO < 0: the colour's jo is the runtime value jo (one path for the two
+// lanes of the last warp, which update colours (0,0) and (0,1) together).
 template <int IO, int JO, int Z>
 __device__ __forceinline__ float strip_update(const float* __restrict__ sm, int sl, int slm, int slp, int s,
-                                              const float* cur, float dx2) {
+                                              const float* cur, float dx2, int jo = JO) {
   typedef StripGeom G;
   const float* P = sm;
   const float* Km = sm + G::FW;
@@ -659,14 +661,15 @@ __device__ __forceinline__ float strip_update(const float* __restrict__ sm, int 
   const float* F5 = sm + 7 * G::FW;
   // neighbours in x: the other io's sub-row; in y: the other jo's sub-row
   // (slots of rows r-1 / r for jo = 0, r / r+1 for jo = 1)
-  const int sy_p = JO ? slp : sl, sy_m = JO ? sl : slm;
-  const int c = G::at(sl, IO, JO, s);
-  const int xp = G::at(sl, 1 - IO, JO, IO ? s + 1 : s), xm = G::at(sl, 1 - IO, JO, IO ? s : s - 1);
-  const int yp = G::at(sy_p, IO, 1 - JO, s), ym = G::at(sy_m, IO, 1 - JO, s);
-  const int ypxp = G::at(sy_p, 1 - IO, 1 - JO, IO ? s + 1 : s);
-  const int ypxm = G::at(sy_p, 1 - IO, 1 - JO, IO ? s : s - 1);
-  const int ymxp = G::at(sy_m, 1 - IO, 1 - JO, IO ? s + 1 : s);
-  const int ymxm = G::at(sy_m, 1 - IO, 1 - JO, IO ? s : s - 1);
+  const int J = JO >= 0 ? JO : jo;
+  const int sy_p = J ? slp : sl, sy_m = J ? sl : slm;
+  const int c = G::at(sl, IO, J, s);
+  const int xp = G::at(sl, 1 - IO, J, IO ? s + 1 : s), xm = G::at(sl, 1 - IO, J, IO ? s : s - 1);
+  const int yp = G::at(sy_p, IO, 1 - J, s), ym = G::at(sy_m, IO, 1 - J, s);
+  const int ypxp = G::at(sy_p, 1 - IO, 1 - J, IO ? s + 1 : s);
+  const int ypxm = G::at(sy_p, 1 - IO, 1 - J, IO ? s : s - 1);
+  const int ymxp = G::at(sy_m, 1 - IO, 1 - J, IO ? s + 1 : s);
+  const int ymxm = G::at(sy_m, 1 - IO, 1 - J, IO ? s : s - 1);
   Stencil<float> st;
   st.f6c = cur[1]; st.f6km = cur[2]; st.f6kp = cur[3];
   st.f3km = cur[4]; st.f5km = cur[5]; st.f3kp = cur[6]; st.f5kp = cur[7];
@@ -789,11 +792,15 @@ __global__ void __launch_bounds__(160, 5) k_gs_strip(const float* __restrict__ s
       centre(r + 1, pre);
       const int sl = G::slot(r), slm = G::slot(r - 1), slp = G::slot(r + 1);
       float v;
-      switch (q) {
-        case 0: v = strip_update<0, 0, Z>(sm, sl, slm, slp, sc, cur, dx2); break;
-        case 1: v = strip_update<0, 1, Z>(sm, sl, slm, slp, sc, cur, dx2); break;
-        case 2: v = strip_update<1, 0, Z>(sm, sl, slm, slp, sc, cur, dx2); break;
-        default: v = strip_update<1, 1, Z>(sm, sl, slm, slp, sc, cur, dx2); break;
+      if (warp == 4) {
+        v = strip_update<0, -1, Z>(sm, sl, slm, slp, sc, cur, dx2, jo);
+      } else {
+        switch (q) {
+          case 0: v = strip_update<0, 0, Z>(sm, sl, slm, slp, sc, cur, dx2); break;
+          case 1: v = strip_update<0, 1, Z>(sm, sl, slm, slp, sc, cur, dx2); break;
+          case 2: v = strip_update<1, 0, Z>(sm, sl, slm, slp, sc, cur, dx2); break;
+          default: v = strip_update<1, 1, Z>(sm, sl, slm, slp, sc, cur, dx2); break;
+        }
       }
       sm[G::at(sl, io, jo, sc)] = v;
     } else if (r + 1 == rlo) {
