@@ -629,7 +629,8 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // ring from 16-byte loads issued at the start of the step.  The fields read
 // at the cell only (rhs, coefficient 6 of P, coefficients 3, 5, 6 of P+-1)
 // are loaded one step ahead.  (Loading two sub-rows ahead in alternating
-// register sets was slower: its registers allow 4 CTAs per SM instead of 5.)
+// register sets was slower: its registers allow 4 CTAs per SM instead of 5;
+// so was a 64-register build for 6 CTAs per SM.)
 // Warps 0-3 take colours 0-3 (sub-cells 0..31); warp 4 takes sub-cell 32 of
 // colours 0 and 1 (x0+64, read by the last two colours at x0+63) and the
 // write-back.
