@@ -16,6 +16,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "mmh_internal.h"
 
 namespace mmh {
@@ -1173,6 +1175,44 @@ __global__ void k_prolong_add(T* __restrict__ u, const T* __restrict__ uh, int n
   u[t] = u[t] + (H_(ibl, jbl, kbl) + H_(ibl, jbl, kbh) + H_(ibl, jbh, kbl) + H_(ibl, jbh, kbh) + H_(ibh, jbh, kbl) +
                  H_(ibh, jbh, kbh) + H_(ibh, jbl, kbl) + H_(ibh, jbl, kbh)) * T(0.125);
 #undef H_
+}
+
+// The same prolongation with one thread per coarse cell (ci, cj, ck), which
+// writes the 2 x 2 x 2 fine cells (2ci + x, 2cj + y, 2ck + z).  A fine cell's
+// ibl = ci and ibh = ci + x (wrapped), so its eight terms are the coarse
+// values h[a][b][d] = uh(ci + a x, cj + b y, ck + d z): the block reads the
+// 8 coarse values once instead of 8 per fine cell, and each fine row pair
+// (x = 0, 1) is one vector load and store.  Operand order as k_prolong_add.
+template <class T>
+__global__ void k_prolong_add_blk(T* __restrict__ u, const T* __restrict__ uh, int n) {
+  typedef typename std::conditional<sizeof(T) == 4, float2, double2>::type V2;
+  const int nh = n >> 1;
+  const i64 nh3 = (i64)nh * nh * nh;
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nh3) return;
+  int ci, cj, ck;
+  cell_of(t, nh, ci, cj, ck);
+  const int ch[2] = {ci, ci + 1 < nh ? ci + 1 : 0}, cjh[2] = {cj, cj + 1 < nh ? cj + 1 : 0},
+            ckh[2] = {ck, ck + 1 < nh ? ck + 1 : 0};
+  T h[2][2][2];
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int d = 0; d < 2; ++d) h[a][b][d] = uh[IDX(ch[a], cjh[b], ckh[d], nh)];
+#pragma unroll
+  for (int z = 0; z < 2; ++z)
+#pragma unroll
+    for (int y = 0; y < 2; ++y) {
+      V2* p = reinterpret_cast<V2*>(u + IDX(2 * ci, 2 * cj + y, 2 * ck + z, n));
+      V2 v = *p;
+      v.x = v.x + (h[0][0][0] + h[0][0][z] + h[0][y][0] + h[0][y][z] + h[0][y][0] + h[0][y][z] + h[0][0][0] +
+                   h[0][0][z]) * T(0.125);
+      v.y = v.y + (h[0][0][0] + h[0][0][z] + h[0][y][0] + h[0][y][z] + h[1][y][0] + h[1][y][z] + h[1][0][0] +
+                   h[1][0][z]) * T(0.125);
+      *p = v;
+    }
 }
 
 // Exact sum of a[0..count) into acc (lo, hi); flag |= 1 on a term out of range.
