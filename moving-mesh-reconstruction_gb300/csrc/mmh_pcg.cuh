@@ -123,15 +123,78 @@ void launch_dot(const T* a, const T* b, i64 count, const unsigned long long* abi
   count_launch();
 }
 
+// The FP32 updates of the mixed form's inner solve over whole vectors of four:
+// a fixed grid of at most 8 blocks per SM walks the vectors with 16-byte
+// loads and commits one maximum per block (the elementwise results and the
+// maximum are those of k_pcg_update / k_pcg_pupdate).  count % 4 == 0.
+static __global__ void __launch_bounds__(256) k_pcg_update_v4(float4* __restrict__ x, float4* __restrict__ r,
+                                                       const float4* __restrict__ p, const float4* __restrict__ q,
+                                                       i64 count4, const double* __restrict__ alpha,
+                                                       unsigned long long* rbits) {
+  const float a = (float)*alpha;
+  unsigned m = 0;
+  for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < count4; t += (i64)gridDim.x * blockDim.x) {
+    float4 xv = x[t], rv = r[t];
+    const float4 pv = p[t], qv = q[t];
+    xv.x = xv.x + a * pv.x; xv.y = xv.y + a * pv.y; xv.z = xv.z + a * pv.z; xv.w = xv.w + a * pv.w;
+    rv.x = rv.x - a * qv.x; rv.y = rv.y - a * qv.y; rv.z = rv.z - a * qv.z; rv.w = rv.w - a * qv.w;
+    x[t] = xv;
+    r[t] = rv;
+    const unsigned b0 = __float_as_uint(fabsf(rv.x)), b1 = __float_as_uint(fabsf(rv.y));
+    const unsigned b2 = __float_as_uint(fabsf(rv.z)), b3 = __float_as_uint(fabsf(rv.w));
+    m = max(m, max(max(b0, b1), max(b2, b3)));
+  }
+  block_max_commit(__uint_as_float(m), rbits);
+}
+static __global__ void __launch_bounds__(256) k_pcg_pupdate_v4(float4* __restrict__ p, const float4* __restrict__ z,
+                                                        i64 count4, const double* __restrict__ beta,
+                                                        unsigned long long* pbits) {
+  const float b = (float)*beta;
+  unsigned m = 0;
+  for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < count4; t += (i64)gridDim.x * blockDim.x) {
+    float4 pv = p[t];
+    const float4 zv = z[t];
+    pv.x = zv.x + b * pv.x; pv.y = zv.y + b * pv.y; pv.z = zv.z + b * pv.z; pv.w = zv.w + b * pv.w;
+    p[t] = pv;
+    const unsigned b0 = __float_as_uint(fabsf(pv.x)), b1 = __float_as_uint(fabsf(pv.y));
+    const unsigned b2 = __float_as_uint(fabsf(pv.z)), b3 = __float_as_uint(fabsf(pv.w));
+    m = max(m, max(max(b0, b1), max(b2, b3)));
+  }
+  block_max_commit(__uint_as_float(m), pbits);
+}
+
+inline unsigned vec_blocks(i64 count4) {
+  i64 b = (count4 + kBlock - 1) / kBlock;
+  const i64 cap = 152 * 8;
+  return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
 template <class T>
 void launch_pcg_update(T* x, T* r, const T* p, const T* q, i64 count, const double* alpha, unsigned long long* rbits,
                        cudaStream_t s) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (count % 4 == 0) {
+      k_pcg_update_v4<<<vec_blocks(count / 4), kBlock, 0, s>>>(
+          reinterpret_cast<float4*>(x), reinterpret_cast<float4*>(r), reinterpret_cast<const float4*>(p),
+          reinterpret_cast<const float4*>(q), count / 4, alpha, rbits);
+      count_launch();
+      return;
+    }
+  }
   k_pcg_update<T><<<grid_of(count, kBlock), kBlock, 0, s>>>(x, r, p, q, count, alpha, rbits);
   count_launch();
 }
 
 template <class T>
 void launch_pcg_pupdate(T* p, const T* z, i64 count, const double* beta, unsigned long long* pbits, cudaStream_t s) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (count % 4 == 0) {
+      k_pcg_pupdate_v4<<<vec_blocks(count / 4), kBlock, 0, s>>>(
+          reinterpret_cast<float4*>(p), reinterpret_cast<const float4*>(z), count / 4, beta, pbits);
+      count_launch();
+      return;
+    }
+  }
   k_pcg_pupdate<T><<<grid_of(count, kBlock), kBlock, 0, s>>>(p, z, count, beta, pbits);
   count_launch();
 }
