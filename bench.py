@@ -99,6 +99,9 @@ def parse():
     ap.add_argument("--adj-tol", type=float, default=1e-10)
     ap.add_argument("--batch-workers", type=int, default=8)
     ap.add_argument("--batch-niter", type=int, default=4)
+    ap.add_argument("--relax-case", type=int, default=0,
+                    help="instead of the benchmark: two FP32 Gauss-Seidel sweeps (mmh_relax_f64 on a mixed "
+                         "context) on an N^3 grid, the small case of the committed ncu captures of the sweep kernel")
     ap.add_argument("--gs-shape", type=int, default=-1,
                     help="pin the FP32 Gauss-Seidel shape (0-3 tiles, 4-5 strips); -1: the library times them")
     return ap.parse_args()
@@ -437,6 +440,22 @@ def adjoint_arm(args):
     return 0
 
 
+def relax_case(n, mmh, fields):
+    """Two FP32 sweeps and the residual norm on an n^3 grid (a smooth deformation
+    potential of amplitude 0.05, a lognormal density with sigma 0.5, random phi
+    and rhs): one small, quick launch sequence of the sweep kernel to profile."""
+    g = np.log(fields.lognormal_density(n, sigma=1.0, ns=-2.0, seed=7))
+    defpot = np.asfortranarray((g - g.mean()) * 0.05)
+    rho = fields.lognormal_density(n, sigma=0.5, seed=8)
+    rng = np.random.default_rng(9)
+    rhs = np.asfortranarray(rng.standard_normal((n, n, n)))
+    phi = np.asfortranarray(rng.standard_normal((n, n, n)))
+    with mmh.Context(n, precision=mmh.MMH_MIXED, schedule=mmh.MMH_SCHED_TOL) as ctx:
+        _, rinf = ctx.relax(phi, rhs, defpot, rho, 1.0, 2, 18)
+    print(json.dumps({"case": "relax", "n": n, "sweeps": 2, "rinf": rinf}))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -452,6 +471,8 @@ def main():
     import fields
 
     mmh.gs_tile_pin(args.gs_shape)
+    if args.relax_case > 0:
+        return relax_case(args.relax_case, mmh, fields)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
