@@ -1158,31 +1158,16 @@ __global__ void k_smooth27(const T* __restrict__ in, int n, T* __restrict__ out)
   out[t] = smooth27(in, n, i, j, k);
 }
 
-// inject (mgutil.f90:38-71): u += trilinear prolongation of uh.
-template <class T>
-__global__ void k_prolong_add(T* __restrict__ u, const T* __restrict__ uh, int n) {
-  i64 n3 = (i64)n * n * n;
-  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n3) return;
-  int i, j, k;
-  cell_of(t, n, i, j, k);
-  int nh = n >> 1;
-  int ibl = i >> 1, ibh = (i + 1) >> 1, jbl = j >> 1, jbh = (j + 1) >> 1, kbl = k >> 1, kbh = (k + 1) >> 1;
-  if (ibh >= nh) ibh = 0;
-  if (jbh >= nh) jbh = 0;
-  if (kbh >= nh) kbh = 0;
-#define H_(x, y, z) uh[IDX(x, y, z, nh)]
-  u[t] = u[t] + (H_(ibl, jbl, kbl) + H_(ibl, jbl, kbh) + H_(ibl, jbh, kbl) + H_(ibl, jbh, kbh) + H_(ibh, jbh, kbl) +
-                 H_(ibh, jbh, kbh) + H_(ibh, jbl, kbl) + H_(ibh, jbl, kbh)) * T(0.125);
-#undef H_
-}
-
-// The same prolongation with one thread per coarse cell (ci, cj, ck), which
-// writes the 2 x 2 x 2 fine cells (2ci + x, 2cj + y, 2ck + z).  A fine cell's
-// ibl = ci and ibh = ci + x (wrapped), so its eight terms are the coarse
-// values h[a][b][d] = uh(ci + a x, cj + b y, ck + d z): the block reads the
-// 8 coarse values once instead of 8 per fine cell, and each fine row pair
-// (x = 0, 1) is one vector load and store.  Operand order as k_prolong_add.
+// inject (mgutil.f90:38-71): u += trilinear prolongation of uh.  Fine cell
+// (i, j, k) adds (H(ibl,jbl,kbl) + H(ibl,jbl,kbh) + H(ibl,jbh,kbl) +
+// H(ibl,jbh,kbh) + H(ibh,jbh,kbl) + H(ibh,jbh,kbh) + H(ibh,jbl,kbl) +
+// H(ibh,jbl,kbh)) * 1/8 with ibl = i/2, ibh = (i+1)/2 wrapped (the same for j,
+// k), summed in that order.  One thread per coarse cell (ci, cj, ck) writes
+// the 2 x 2 x 2 fine cells (2ci + x, 2cj + y, 2ck + z), whose ibl = ci and
+// ibh = ci + x, so their terms are the coarse values h[a][b][d] =
+// uh(ci + a x, cj + b y, ck + d z): the block reads the 8 coarse values once
+// instead of 8 per fine cell, and each fine pair x = 0, 1 is one vector load
+// and store.
 template <class T>
 __global__ void k_prolong_add_blk(T* __restrict__ u, const T* __restrict__ uh, int n) {
   typedef typename std::conditional<sizeof(T) == 4, float2, double2>::type V2;

@@ -256,7 +256,6 @@ template <class T>
 void launch_prolong_add(T* u, const T* uh, int n, cudaStream_t s) {
   i64 n3 = (i64)n * n * n;
   prof_begin(kk<T>(KK_PROLONG), s, n3, n);
-  (void)n3;
   k_prolong_add_blk<T><<<grid_of((i64)(n / 2) * (n / 2) * (n / 2), kBlock), kBlock, 0, s>>>(u, uh, n);
   prof_end(kk<T>(KK_PROLONG), s, n);
   count_launch();
